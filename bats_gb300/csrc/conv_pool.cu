@@ -1,0 +1,344 @@
+// Convolutional LIF layer (valid convolution, stride 1) and 2x2 spike-union pooling.
+//
+// Neuron layouts follow the reference: a neuron (x, y, c) of a (X, Y, C) layer has index
+// (x*Y + y)*C + c; filters are (C_out, fx, fy, C_in) (bats/Layers/ConvLIFLayer.py:20-37).
+//
+// Forward (replaces compute_spike_times_conv, bats/CudaKernels/CuFiles/Inference/compute_spike_times_conv.cu:93-174):
+// the reference tests every event of the sample against every post neuron's receptive field and
+// runs the crossing search after each event, relevant or not. Here a CTA owns a spatial tile of
+// post positions x all output channels, keeps only the events inside the tile's receptive field,
+// and each thread integrates only the events of its own receptive field, searching for crossings
+// in (t_prev_relevant, t_this_relevant] before adding the next one. Because the neuron state does
+// not change at an irrelevant event and the reference's windows between consecutive events tile
+// that interval, this finds the same spikes with the same arithmetic.
+//
+// Backward (replaces compute_weights_gradient_conv and propagate_errors_to_pre_spikes_conv,
+// .../Backpropagation/compute_weights_gradient_conv.cu:11-61, propagate_errors_to_pre_spikes_conv.cu:11-89):
+// one CTA per sample, one thread per filter tap (c_out, dx, dy); per event the thread looks up the
+// post neuron (x-dx, y-dy, c_out), its first spike after the event, and adds the gradient to the
+// filter entry it owns (no atomics) and the weighted error term to the event's error.
+//
+// Pooling (replaces aggregate_spikes_conv + argsort, .../Inference/aggregate_spikes_conv.cu:6-43,
+// Wrappers/Inference/aggregate_spikes_conv.py:10-28; backward bats/Layers/PoolingLayer.py:55-66):
+// a stable 4-way merge of the children's sorted spike lists, inf slots last in concatenation order.
+#include "common.cuh"
+#include "abi_util.h"
+
+namespace bats {
+
+struct ConvEvent {
+    float t, es, e;
+    int xyc;  // x | y << 10 | c << 20
+};
+
+constexpr int CONV_CHUNK = 256;
+
+__global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
+                                    const float* __restrict__ W, int X, int Y, int C, int fx, int fy, int C_out,
+                                    int Xo, int Yo, int TX, int TY, int tiles_y, int k_post, float c, float dtt,
+                                    float tau, float max_sim, int w_in_smem, int* __restrict__ n_spikes,
+                                    float* __restrict__ a_out, float* __restrict__ x_out, float* __restrict__ t_out,
+                                    float* __restrict__ z_out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ConvEvent* sev = reinterpret_cast<ConvEvent*>(smem_raw);
+    int* swarp = reinterpret_cast<int*>(sev + CONV_CHUNK);
+    float* sW = reinterpret_cast<float*>(swarp + 32);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    const int s = blockIdx.y;
+    const int tx0 = (blockIdx.x / tiles_y) * TX, ty0 = (blockIdx.x % tiles_y) * TY;
+    const int nw = C_out * fx * fy * C;
+    const float* Wsrc = W;
+    if (w_in_smem) {
+        for (int q = tid; q < nw; q += blockDim.x) sW[q] = W[q];
+        Wsrc = sW;
+    }
+    const int co = tid % C_out, pl = tid / C_out;
+    const int xo = tx0 + pl / TY, yo = ty0 + pl % TY;
+    const bool active = pl < TX * TY && xo < Xo && yo < Yo;
+    const int n_post = Xo * Yo * C_out;
+    const int post = (xo * Yo + yo) * C_out + co;
+    const long long obase = ((long long)s * n_post + (active ? post : 0)) * k_post;
+    float* ao = a_out + obase;
+    float* xo_ = x_out + obase;
+    float* to = t_out + obase;
+    float* zo = z_out + obase;
+    // Receptive field of the whole tile.
+    const int rx0 = tx0, rx1 = min(X, tx0 + TX + fx - 1), ry0 = ty0, ry1 = min(Y, ty0 + TY + fy - 1);
+
+    float a = 0.0f, b = 0.0f, last_t = 0.0f;
+    bool has_prev = false;
+    int n = 0;
+    bool done = !active;
+    const int E = ev_count[s];
+    const Event* evs = ev + (long long)s * ev_cap;
+    for (int m0 = 0; m0 < E; m0 += CONV_CHUNK) {
+        // Stage the chunk's events that fall in the tile's receptive field, in time order.
+        __syncthreads();
+        int kept = 0;
+        for (int r0 = 0; r0 < CONV_CHUNK && m0 + r0 < E; r0 += blockDim.x) {
+            const int q = r0 + tid;
+            bool keep = false;
+            ConvEvent ce;
+            if (q < CONV_CHUNK && m0 + q < E) {
+                const Event e = evs[m0 + q];
+                const int j = e.j;
+                const int cc = j % C, xy = j / C, yy = xy % Y, xx = xy / Y;
+                keep = xx >= rx0 && xx < rx1 && yy >= ry0 && yy < ry1;
+                ce.t = e.t;
+                ce.es = e.es;
+                ce.e = e.e;
+                ce.xyc = xx | (yy << 10) | (cc << 20);
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) swarp[warp] = __popc(bal);
+            __syncthreads();
+            int off = kept;
+            int tot = 0;
+            for (int w = 0; w < nwarps; ++w) {
+                if (w < warp) off += swarp[w];
+                tot += swarp[w];
+            }
+            if (keep) sev[off + __popc(bal & lanemask_lt())] = ce;
+            __syncthreads();
+            kept += tot;
+        }
+        __syncthreads();
+        if (done) continue;
+        for (int m = 0; m < kept && !done; ++m) {
+            const ConvEvent e = sev[m];
+            const int dx = (e.xyc & 1023) - xo, dy = ((e.xyc >> 10) & 1023) - yo;
+            if (dx < 0 || dx >= fx || dy < 0 || dy >= fy) continue;
+            if (has_prev) {
+                done = solve_crossings<true>(a, b, last_t, e.t, c, dtt, tau, max_sim, n, k_post, ao, xo_, to, zo);
+                if (done) break;
+            }
+            const float w = Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)];
+            a += w * e.es;
+            b += w * e.e;
+            last_t = e.t;
+            has_prev = true;
+        }
+    }
+    if (active) {
+        if (has_prev && !done) solve_crossings<true>(a, b, last_t, BATS_INF, c, dtt, tau, max_sim, n, k_post, ao, xo_, to, zo);
+        n_spikes[(long long)s * n_post + post] = n;
+        for (int k = n; k < k_post; ++k) {
+            to[k] = BATS_INF;
+            zo[k] = BATS_INF;
+        }
+    }
+}
+
+// One CTA per sample; thread q handles filter taps q, q + blockDim, ... of (C_out, fx, fy).
+__global__ void conv_backward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_slot,
+                                     const int* __restrict__ ev_count, long long ev_cap, const float* __restrict__ W,
+                                     int Y, int C, int fx, int fy, int C_out, int Xo, int Yo,
+                                     const float* __restrict__ post_t, const float2* __restrict__ tab,
+                                     const int* __restrict__ nvalid, int k_post, float tau_s, float tau,
+                                     long long pre_slots, float* __restrict__ grad, float* __restrict__ pre_err) {
+    __shared__ float sred[32][33];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int s = blockIdx.x;
+    const int taps = C_out * fx * fy;
+    const int n_post = Xo * Yo * C_out;
+    const int E = ev_count[s];
+    const Event* evs = ev + (long long)s * ev_cap;
+    float* gs = grad + (long long)s * taps * C;
+    for (int m0 = 0; m0 < E; m0 += 32) {
+        const int cnt = min(32, E - m0);
+        for (int q = 0; q < cnt; ++q) {
+            const Event e = evs[m0 + q];
+            const int cc = e.j % C, xy = e.j / C, yy = xy % Y, xx = xy / Y;
+            float term = 0.0f;
+            for (int tp = tid; tp < taps; tp += blockDim.x) {
+                const int co = tp / (fx * fy), dx = (tp / fy) % fx, dy = tp % fy;
+                const int xo = xx - dx, yo = yy - dy;
+                if (xo < 0 || yo < 0 || xo >= Xo || yo >= Yo) continue;
+                const long long pn = (long long)s * n_post + (xo * Yo + yo) * C_out + co;
+                const int n = nvalid[pn];
+                const float* tp_ = post_t + pn * k_post;
+                int p = 0;
+                while (p < n && tp_[p] <= e.t) ++p;
+                if (p >= n) continue;
+                const float2 AB = tab[pn * (k_post + 1) + p];
+                gs[(long long)tp * C + cc] += fmaf(e.es, AB.x, -(e.e * AB.y));
+                if (pre_err) term += W[(long long)tp * C + cc] * (AB.x * e.es / tau_s - AB.y * e.e / tau);
+            }
+            if (pre_err) {
+#pragma unroll
+                for (int o = 16; o >= 1; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+                if (lane == 0) sred[q][warp] = term;
+            }
+        }
+        if (pre_err) {
+            __syncthreads();
+            if (tid < cnt) {
+                float acc = 0.0f;
+                for (int w = 0; w < nwarps; ++w) acc += sred[tid][w];
+                pre_err[(long long)s * pre_slots + ev_slot[(long long)s * ev_cap + m0 + tid]] = acc;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Pool forward: one thread per (sample, pooled neuron).
+__global__ void pool_forward_kernel(const int* __restrict__ n_spikes, const float* __restrict__ times, int batch, int X,
+                                    int Y, int C, int K, int* __restrict__ out_n, float* __restrict__ out_t,
+                                    int* __restrict__ out_idx) {
+    const int Xo = X / 2, Yo = Y / 2;
+    const long long n_out = (long long)Xo * Yo * C;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)batch * n_out) return;
+    const int s = (int)(q / n_out);
+    const int o = (int)(q % n_out);
+    const int c = o % C, xy = o / C, yo = xy % Yo, xo = xy / Yo;
+    long long src[4];
+    int cnt[4], pos[4];
+    int total = 0;
+    for (int ch = 0; ch < 4; ++ch) {
+        const int px = 2 * xo + (ch >> 1), py = 2 * yo + (ch & 1);
+        const long long pidx = ((long long)s * X + px) * Y * C + (long long)py * C + c;
+        src[ch] = pidx * K;
+        // Spikes of a child are its leading finite slots.
+        int nn = 0;
+        while (nn < K && times[src[ch] + nn] < BATS_INF) ++nn;
+        cnt[ch] = nn;
+        pos[ch] = 0;
+        total += n_spikes[pidx];
+    }
+    const long long obase = q * 4LL * K;
+    int w = 0;
+    while (true) {
+        int best = -1;
+        float bt = BATS_INF;
+        for (int ch = 0; ch < 4; ++ch) {
+            if (pos[ch] < cnt[ch]) {
+                const float tt = times[src[ch] + pos[ch]];
+                if (best < 0 || tt < bt) {
+                    best = ch;
+                    bt = tt;
+                }
+            }
+        }
+        if (best < 0) break;
+        out_t[obase + w] = bt;
+        out_idx[obase + w] = (int)(src[best] + pos[best]);
+        ++pos[best];
+        ++w;
+    }
+    for (int ch = 0; ch < 4; ++ch) {
+        for (int k = cnt[ch]; k < K; ++k) {
+            out_t[obase + w] = times[src[ch] + k];
+            out_idx[obase + w] = (int)(src[ch] + k);
+            ++w;
+        }
+    }
+    out_n[q] = total;
+}
+
+__global__ void pool_backward_kernel(const float* __restrict__ errors, const int* __restrict__ idx, long long count,
+                                     float* __restrict__ pre_err) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
+         q += (long long)gridDim.x * blockDim.x)
+        pre_err[idx[q]] = errors[q];
+}
+
+}  // namespace bats
+
+// ---------------------------------------------------------------------------------------------
+// C-ABI
+
+static void conv_tile(int C_out, int& TX, int& TY) {
+    int P = 512 / C_out;
+    if (P < 1) P = 1;
+    TX = 1;
+    while ((TX + 1) * (TX + 1) <= P) ++TX;
+    TY = P / TX;
+}
+
+extern "C" int bats_conv_forward(const void* events, const int* ev_count, long long ev_cap, const float* weights,
+                                 int batch, int X, int Y, int C, int fx, int fy, int C_out, int k_post, float c,
+                                 float delta_theta_tau, float tau, float max_simulation, int* n_spikes, float* a,
+                                 float* x, float* times, float* post_exp_tau, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && X >= fx && Y >= fy && fx > 0 && fy > 0 && C > 0 && C_out > 0 && k_post > 0 &&
+                     X < 1024 && Y < 1024 && C < 2048 && C_out <= 1024,
+                 BATS_ERR_BAD_SHAPE, "conv_forward: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(events && ev_count && weights && n_spikes && a && x && times && post_exp_tau, BATS_ERR_NULL,
+                 "conv_forward: null pointer");
+    const int Xo = X - fx + 1, Yo = Y - fy + 1;
+    int TX, TY;
+    conv_tile(C_out, TX, TY);
+    const int threads = ((TX * TY * C_out + 31) / 32) * 32;
+    const int tiles_x = (Xo + TX - 1) / TX, tiles_y = (Yo + TY - 1) / TY;
+    const size_t nw = (size_t)C_out * fx * fy * C;
+    const size_t base_smem = bats::CONV_CHUNK * sizeof(bats::ConvEvent) + 32 * sizeof(int);
+    const int w_in_smem = (base_smem + nw * sizeof(float)) <= 200 * 1024;
+    const size_t smem = base_smem + (w_in_smem ? nw * sizeof(float) : 0);
+    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_forward_kernel, (int)smem));
+    dim3 grid(tiles_x * tiles_y, batch);
+    bats::conv_forward_kernel<<<grid, threads, smem, stream>>>(
+        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, weights, X, Y, C, fx, fy, C_out, Xo, Yo, TX,
+        TY, tiles_y, k_post, c, delta_theta_tau, tau, max_simulation, w_in_smem, n_spikes, a, x, times, post_exp_tau);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_conv_backward(const void* events, const int* ev_slot, const int* ev_count, long long ev_cap,
+                                  const float* weights, int batch, int X, int Y, int C, int fx, int fy, int C_out,
+                                  int k_pre, const float* post_times, const void* tables, const int* nvalid,
+                                  int k_post, float tau_s, float tau, float* grad_per_sample, float* pre_errors,
+                                  cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && X >= fx && Y >= fy && fx > 0 && fy > 0 && C > 0 && C_out > 0 && k_post > 0 &&
+                     k_pre > 0,
+                 BATS_ERR_BAD_SHAPE, "conv_backward: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(events && ev_slot && ev_count && weights && post_times && tables && nvalid && grad_per_sample,
+                 BATS_ERR_NULL, "conv_backward: null pointer");
+    const int Xo = X - fx + 1, Yo = Y - fy + 1;
+    const long long taps = (long long)C_out * fx * fy;
+    const long long pre_slots = (long long)X * Y * C * k_pre;
+    BATS_CUDA(cudaMemsetAsync(grad_per_sample, 0, (size_t)batch * taps * C * sizeof(float), stream));
+    if (pre_errors) BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)batch * pre_slots * sizeof(float), stream));
+    int threads = (int)std::min<long long>(1024, ((taps + 31) / 32) * 32);
+    bats::conv_backward_kernel<<<batch, threads, 0, stream>>>(
+        reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights, Y, C, fx, fy, C_out, Xo, Yo,
+        post_times, reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots, grad_per_sample,
+        pre_errors);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_pool_forward(const int* n_spikes, const float* times, int batch, int X, int Y, int C, int K,
+                                 int* out_n_spikes, float* out_times, int* out_indices, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && X >= 2 && Y >= 2 && C > 0 && K > 0, BATS_ERR_BAD_SHAPE, "pool_forward: bad shape");
+    BATS_REQUIRE((long long)batch * X * Y * C * K < (1LL << 31), BATS_ERR_CAPACITY,
+                 "pool_forward: indices exceed int32");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(n_spikes && times && out_n_spikes && out_times && out_indices, BATS_ERR_NULL,
+                 "pool_forward: null pointer");
+    const long long total = (long long)batch * (X / 2) * (Y / 2) * C;
+    bats::pool_forward_kernel<<<(unsigned)((total + 127) / 128), 128, 0, stream>>>(n_spikes, times, batch, X, Y, C, K,
+                                                                                 out_n_spikes, out_times, out_indices);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_pool_backward(const float* errors, const int* indices, long long count, float* pre_errors,
+                                  long long pre_count, cudaStream_t stream) {
+    BATS_REQUIRE(count >= 0 && pre_count >= 0, BATS_ERR_BAD_SHAPE, "pool_backward: bad shape");
+    if (pre_count > 0) {
+        BATS_REQUIRE(pre_errors, BATS_ERR_NULL, "pool_backward: null pointer");
+        BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)pre_count * sizeof(float), stream));
+    }
+    if (count == 0) return BATS_OK;
+    BATS_REQUIRE(errors && indices, BATS_ERR_NULL, "pool_backward: null pointer");
+    long long b = (count + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    bats::pool_backward_kernel<<<(unsigned)b, 256, 0, stream>>>(errors, indices, count, pre_errors);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}

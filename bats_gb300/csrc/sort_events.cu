@@ -1,0 +1,213 @@
+// Per-sample time sort of all pre-synaptic spikes of a layer (one CTA per sample).
+//
+// Replaces get_sorted_spikes_indices + the three take_along_axis gathers + compute_pre_exps
+// (bats/CudaKernels/Wrappers/Inference/get_sorted_spikes_indices.py:7-17,
+//  bats/Layers/LIFLayer.py:66-84, bats/CudaKernels/CuFiles/Inference/compute_pre_exps.cu:2-22).
+// The reference sorts every (neuron, slot) of the batch on the device with argpartition after a
+// host sync on the largest spike count; here every sample's valid slots (time < +inf) are
+// compacted and sorted by a stable LSD radix sort in shared memory (8-bit digits, warp ranks
+// from __match_any_sync ballots), so the event list needs no host sync and no padding to the
+// batch maximum. Ties keep slot order, which makes the order deterministic.
+#include "common.cuh"
+
+namespace bats {
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int SORT_SMEM_ITEMS = 4096;  // items sorted fully in shared memory
+
+struct SortShared {
+    int hist[256];
+    int base[256];
+    int wcnt[SORT_WARPS][256];
+    int wofs[SORT_WARPS][256];
+    int warp_tot[SORT_WARPS];
+    int total;
+};
+
+__device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh, int& block_total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    const int in_warp = __popc(bal & lanemask_lt());
+    if (lane == 0) sh.warp_tot[warp] = __popc(bal);
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < SORT_WARPS; ++w) {
+        const int c = sh.warp_tot[w];
+        off += (w < warp) ? c : 0;
+        tot += c;
+    }
+    __syncthreads();
+    block_total = tot;
+    return off + in_warp;
+}
+
+__global__ void __launch_bounds__(SORT_THREADS)
+sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, float tau_s, float tau,
+                   const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out, int* __restrict__ slot_out, int* __restrict__ ev_count,
+                   long long cap, uint32_t* __restrict__ scratch) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SortShared& sh = *reinterpret_cast<SortShared*>(smem_raw);
+    uint32_t* smem_items = reinterpret_cast<uint32_t*>(smem_raw + sizeof(SortShared));
+
+    const int s = blockIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const float* tsrc = times + (long long)s * n_slots;
+
+    // Count valid slots first so that the buffers can be chosen.
+    int n = 0;
+    for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
+        const int slot = r0 + tid;
+        const bool f = slot < n_slots && tsrc[slot] < BATS_INF;
+        int tot;
+        block_exclusive_flag_scan(f, sh, tot);
+        n += tot;
+    }
+
+    uint32_t *ka, *va, *kb, *vb;
+    if (n <= SORT_SMEM_ITEMS) {
+        ka = smem_items;
+        va = ka + SORT_SMEM_ITEMS;
+        kb = va + SORT_SMEM_ITEMS;
+        vb = kb + SORT_SMEM_ITEMS;
+    } else {
+        ka = scratch + (long long)s * 4 * cap;
+        va = ka + cap;
+        kb = va + cap;
+        vb = kb + cap;
+    }
+
+    // Compaction in slot order (stable).
+    int base = 0;
+    for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
+        const int slot = r0 + tid;
+        float t = BATS_INF;
+        if (slot < n_slots) t = tsrc[slot];
+        const bool f = t < BATS_INF;
+        int tot;
+        const int pos = block_exclusive_flag_scan(f, sh, tot);
+        if (f) {
+            ka[base + pos] = float_to_key(t);
+            va[base + pos] = (uint32_t)slot;
+        }
+        base += tot;
+    }
+    __syncthreads();
+
+    // LSD radix sort, 4 passes of 8 bits; passes whose digit is uniform are skipped.
+    for (int shift = 0; shift < 32; shift += 8) {
+        sh.hist[tid] = 0;
+        __syncthreads();
+        for (int i = tid; i < n; i += SORT_THREADS) atomicAdd(&sh.hist[(ka[i] >> shift) & 255u], 1);
+        __syncthreads();
+        const bool uniform = __syncthreads_or(sh.hist[tid] == n);
+        if (uniform) continue;
+        // Exclusive scan of the 256 bins (one bin per thread).
+        {
+            const int lane = tid & 31;
+            int v = sh.hist[tid];
+            int incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) sh.warp_tot[warp] = incl;
+            __syncthreads();
+            int woff = 0;
+            for (int w = 0; w < warp; ++w) woff += sh.warp_tot[w];
+            sh.base[tid] = woff + incl - v;
+#pragma unroll
+            for (int w = 0; w < SORT_WARPS; ++w) sh.wcnt[w][tid] = 0;
+            __syncthreads();
+        }
+        for (int r0 = 0; r0 < n; r0 += SORT_THREADS) {
+            const int i = r0 + tid;
+            const bool valid = i < n;
+            uint32_t key = 0, val = 0;
+            int d = 256;
+            if (valid) {
+                key = ka[i];
+                val = va[i];
+                d = (key >> shift) & 255u;
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const int rank = __popc(peers & lanemask_lt());
+            if (valid && rank == 0) sh.wcnt[warp][d] = __popc(peers);
+            __syncthreads();
+            {
+                int off = sh.base[tid];
+#pragma unroll
+                for (int w = 0; w < SORT_WARPS; ++w) {
+                    sh.wofs[w][tid] = off;
+                    off += sh.wcnt[w][tid];
+                    sh.wcnt[w][tid] = 0;
+                }
+                sh.base[tid] = off;
+            }
+            __syncthreads();
+            if (valid) {
+                const int pos = sh.wofs[warp][d] + rank;
+                kb[pos] = key;
+                vb[pos] = val;
+            }
+        }
+        __syncthreads();
+        uint32_t* t0 = ka; ka = kb; kb = t0;
+        t0 = va; va = vb; vb = t0;
+    }
+
+    Event* eo = ev_out + (long long)s * cap;
+    int* so = slot_out ? slot_out + (long long)s * cap : nullptr;
+    for (int m = tid; m < n; m += SORT_THREADS) {
+        const float t = key_to_float(ka[m]);
+        const int slot = (int)va[m];
+        Event e;
+        e.t = t;
+        e.j = slot / k_pre;
+        if (exp_s_in) {
+            e.es = exp_s_in[(long long)s * n_slots + slot];
+            e.e = exp_in[(long long)s * n_slots + slot];
+        } else {
+            e.es = __expf(t / tau_s);
+            e.e = __expf(t / tau);
+        }
+        eo[m] = e;
+        if (so) so[m] = slot;
+    }
+    if (tid == 0) ev_count[s] = n;
+}
+
+}  // namespace bats
+
+// ---------------------------------------------------------------------------------------------
+// C-ABI launchers (declared in include/bats_gb300.h).
+#include "abi_util.h"
+
+extern "C" size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_pre) {
+    const long long cap = (long long)n_pre * k_pre;
+    if (cap <= bats::SORT_SMEM_ITEMS) return 0;
+    return (size_t)batch * 4 * cap * sizeof(uint32_t);
+}
+
+extern "C" int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, float tau_s,
+                                float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out, int* slot_out, int* ev_count, void* workspace,
+                                size_t workspace_bytes, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_pre >= 0 && k_pre > 0, BATS_ERR_BAD_SHAPE, "sort_events: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(pre_times && ev_out && ev_count, BATS_ERR_NULL, "sort_events: null pointer");
+    BATS_REQUIRE((exp_tau_s == nullptr) == (exp_tau == nullptr), BATS_ERR_NULL, "sort_events: give both exps or none");
+    const long long cap = (long long)n_pre * k_pre;
+    BATS_REQUIRE(cap < (1LL << 30), BATS_ERR_CAPACITY, "sort_events: n_pre*k_pre too large");
+    const size_t need = bats_sort_events_workspace_bytes(batch, n_pre, k_pre);
+    BATS_REQUIRE(workspace_bytes >= need && (need == 0 || workspace), BATS_ERR_WORKSPACE,
+                 "sort_events: workspace too small");
+    const size_t smem = sizeof(bats::SortShared) + 4 * bats::SORT_SMEM_ITEMS * sizeof(uint32_t);
+    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel, (int)smem));
+    bats::sort_events_kernel<<<batch, bats::SORT_THREADS, smem, stream>>>(
+        pre_times, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out, ev_count, cap,
+        reinterpret_cast<uint32_t*>(workspace));
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}

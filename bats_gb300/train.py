@@ -1,0 +1,254 @@
+"""Batched training step of a fully-connected BATS network with every buffer preallocated.
+
+FCTrainStep runs forward (per-layer event sort + LIF forward), the spike-count classification loss,
+the exact backward with batch-mean weight gradients, and Adam updates of the weights and of their
+transposed copies, with no host synchronisation and no allocation after construction, so that the
+whole step can be captured once as a CUDA graph and replayed (capture()). It computes the same
+arithmetic as the layer-by-layer API (Network + LIFLayer + SpikeCountClassLoss + AdamOptimizer +
+the caller's batch mean), only without materialising the per-sample gradients.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import kernels as K
+from ._lib import call, ptr, stream_ptr
+
+
+@dataclass
+class FCLayerSpec:
+    n_neurons: int
+    tau_s: float
+    theta: float
+    delta_theta: float
+    max_n_spike: int
+
+
+class FCTrainStep:
+    def __init__(self, batch: int, n_inputs: int, k_input: int, layers: Sequence[FCLayerSpec],
+                 weights: Sequence[torch.Tensor], target_true: float, target_false: float,
+                 learning_rate: float = 3e-3, beta_1: float = 0.9, beta_2: float = 0.999, epsilon: float = 1e-8,
+                 max_simulation: float = np.inf, grad_group: int = 16, device="cuda"):
+        self.B = int(batch)
+        self.dev = torch.device(device)
+        self.specs = list(layers)
+        self.max_sim = float(max_simulation)
+        self.tt, self.tf = np.float32(target_true), np.float32(target_false)
+        self.lr, self.b1, self.b2, self.eps = (np.float32(v) for v in (learning_rate, beta_1, beta_2, epsilon))
+        self.t = 0
+        self.grad_group = int(grad_group)
+        B, dev = self.B, self.dev
+        f32, i32 = torch.float32, torch.int32
+        # Inputs (device-resident).
+        self.in_times = torch.full((B, n_inputs, k_input), float("inf"), dtype=f32, device=dev)
+        self.labels = torch.zeros((B,), dtype=i32, device=dev)
+        # Per-layer state.
+        self.W, self.Wt, self.m, self.v, self.ev, self.out, self.tabs, self.grad, self.pre_err = ([] for _ in range(9))
+        n_prev, k_prev = n_inputs, k_input
+        for spec, w in zip(self.specs, weights):
+            w = w.to(device=dev, dtype=f32).contiguous().clone()
+            assert w.shape == (spec.n_neurons, n_prev)
+            self.W.append(w)
+            self.Wt.append(K.transpose_weights(w))
+            self.m.append(torch.zeros_like(w))
+            self.v.append(torch.zeros_like(w))
+            self.ev.append(K.alloc_events(B, n_prev, k_prev, dev))
+            N, Kp = spec.n_neurons, spec.max_n_spike
+            self.out.append((torch.empty((B, N), dtype=i32, device=dev),
+                             *(torch.empty((B, N, Kp), dtype=f32, device=dev) for _ in range(4))))
+            self.tabs.append(K.BackwardTables(torch.empty((B, N, Kp), dtype=f32, device=dev),
+                                              torch.empty((B, N, Kp), dtype=f32, device=dev),
+                                              torch.empty((B, N, Kp + 1, 2), dtype=f32, device=dev),
+                                              torch.empty((B, N), dtype=i32, device=dev)))
+            self.grad.append(torch.empty((N, n_prev), dtype=f32, device=dev))
+            self.pre_err.append(torch.empty((B, n_prev, k_prev), dtype=f32, device=dev))
+            n_prev, k_prev = N, Kp
+        self.loss = torch.empty((B,), dtype=f32, device=dev)
+        self.errors = torch.empty((B, n_prev, k_prev), dtype=f32, device=dev)
+        # Scratch sized for the largest user.
+        ws = 0
+        n_prev, k_prev = n_inputs, k_input
+        for spec in self.specs:
+            ws = max(ws, K.call_size("bats_sort_events_workspace_bytes", B, n_prev, k_prev),
+                     K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev,
+                                 max(2, self.grad_group)),
+                     K.call_size("bats_pre_errors_workspace_bytes", B, n_prev * k_prev, spec.n_neurons))
+            n_prev, k_prev = spec.n_neurons, spec.max_n_spike
+        self.ws = torch.empty(max(ws, 256), dtype=torch.uint8, device=dev)
+        self.graph: Optional[torch.cuda.CUDAGraph] = None
+        self.capture_error = None
+        # beta_1^t, beta_2^t on the device, advanced by one launch per step (keeps the step capturable).
+        self.powers = torch.ones((2,), dtype=torch.float64, device=dev)
+        # Host staging for end-to-end steps.
+        self.h_times = torch.empty(self.in_times.shape, dtype=f32, pin_memory=True)
+        self.h_labels = torch.empty((B,), dtype=i32, pin_memory=True)
+        self.h_loss = torch.empty((B,), dtype=f32, pin_memory=True)
+        self.launches = self._build_launches()
+        self.launches_per_step = self._count_launches()
+
+    # -- the step as a fixed list of launches --------------------------------------------------------
+    def _build_launches(self):
+        """(name, fn(stream)) for every entry-point call of one step, in order. All pointers are fixed."""
+        B = self.B
+        ws, wsb = ptr(self.ws), self.ws.numel()
+        L = []
+        pre_times = self.in_times
+        for li, spec in enumerate(self.specs):
+            ev = self.ev[li]
+            tau32, c, dtt = K.lif_constants(spec.tau_s, spec.theta, spec.delta_theta)
+            tag = f"L{li + 1}"
+            L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), ev=ev, spec=spec, tau32=tau32: call(
+                "bats_sort_events", pt, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32), None,
+                None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ws, wsb, s)))
+            n, a, x, t, z = self.out[li]
+            L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
+                      call("bats_lif_forward_fc", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
+                           self.Wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt),
+                           float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o), s)))
+            pre_times = t
+        n_out = self.out[-1][0]
+        L.append(("loss", lambda s: call("bats_spike_count_loss", ptr(n_out), 0, None, ptr(self.labels),
+                                         float(self.tt), float(self.tf), B, n_out.shape[1],
+                                         self.specs[-1].max_n_spike, ptr(self.loss), ptr(self.errors), s)))
+        errors = self.errors
+        for li in range(len(self.specs) - 1, -1, -1):
+            spec = self.specs[li]
+            ev = self.ev[li]
+            n, a, x, t, z = self.out[li]
+            tau32, c, dtt = K.lif_constants(spec.tau_s, spec.theta, spec.delta_theta)
+            tb = self.tabs[li]
+            tag = f"L{li + 1}"
+            L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt, tb=tb:
+                      call("bats_backward_prep", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]), ptr(e), B,
+                           spec.n_neurons, spec.max_n_spike, float(c), float(tau32), float(dtt), 1, 1, ptr(tb.f1),
+                           ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
+            L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
+                "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(t), ptr(tb.tables),
+                ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons, max(2, self.grad_group),
+                ptr(self.grad[li]), ws, wsb, s)))
+            if li > 0:
+                pe = self.pre_err[li]
+                L.append((f"{tag}.pre_err", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, pe=pe, tau32=tau32: call(
+                    "bats_pre_errors", ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
+                    self.Wt[li].shape[1], ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons,
+                    spec.max_n_spike, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32), ptr(pe), ws,
+                    wsb, s)))
+                errors = pe
+        L.append(("adam.powers", lambda s: call("bats_adam_powers_advance", ptr(self.powers), float(self.b1),
+                                                float(self.b2), s)))
+        for li in range(len(self.specs)):
+            w = self.W[li]
+            L.append((f"L{li + 1}.adam", lambda s, li=li, w=w: call(
+                "bats_adam_step_device", ptr(self.grad[li]), ptr(self.m[li]), ptr(self.v[li]), w.numel(),
+                float(self.b1), float(self.b2), float(self.eps), float(self.lr), ptr(self.powers), ptr(w),
+                ptr(self.Wt[li]), w.shape[0], w.shape[1], self.Wt[li].shape[1], s)))
+        return L
+
+    # Kernels launched by each entry point (memsets counted as launches too).
+    KERNELS_PER_CALL = {"sort": 1, "forward": 1, "loss": 1, "prep": 1, "grad": 2, "pre_err": 3, "powers": 1,
+                        "adam": 1}
+
+    def _count_launches(self):
+        return sum(self.KERNELS_PER_CALL[name.split(".")[-1]] for name, _ in self.launches)
+
+    def step(self) -> None:
+        """One training step on the device-resident inputs (in_times, labels), launched eagerly."""
+        s = stream_ptr()
+        for _, fn in self.launches:
+            fn(s)
+        self.t += 1
+
+    def try_capture(self) -> bool:
+        """Record one step as a CUDA graph (after an eager warm-up step); False if capture fails."""
+        try:
+            self.step()
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side):
+                    s = stream_ptr()
+                    for _, fn in self.launches:
+                        fn(s)
+            torch.cuda.current_stream().wait_stream(side)
+            torch.cuda.synchronize()
+            self.graph = g
+            return True
+        except Exception as exc:  # pragma: no cover - reported by the caller
+            self.graph = None
+            self.capture_error = repr(exc)
+            return False
+
+    def replay(self) -> None:
+        self.graph.replay()
+        self.t += 1
+
+    def run(self) -> None:
+        if self.graph is not None:
+            self.replay()
+        else:
+            self.step()
+
+    def profile_step(self):
+        """One eager step with CUDA events around every launch: {name: (start, end)}."""
+        s = stream_ptr()
+        rec = {}
+        for name, fn in self.launches:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn(s)
+            b.record()
+            rec[name] = (a, b)
+        self.t += 1
+        return rec
+
+    def time_launch(self, name, steps, flush=None) -> float:
+        """Average device time (ms) of one named launch over `steps` eager steps."""
+        s = stream_ptr()
+        total = 0.0
+        evs = []
+        for _ in range(steps):
+            if flush is not None:
+                flush.add_(1.0)
+            for nm, fn in self.launches:
+                if nm == name:
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record()
+                    fn(s)
+                    b.record()
+                    evs.append((a, b))
+                else:
+                    fn(s)
+            self.t += 1
+        torch.cuda.synchronize()
+        for a, b in evs:
+            total += a.elapsed_time(b)
+        return total / max(1, len(evs))
+
+    def set_inputs(self, times, labels) -> None:
+        self.in_times.copy_(torch.as_tensor(times), non_blocking=True)
+        self.labels.copy_(torch.as_tensor(labels).to(torch.int32), non_blocking=True)
+
+    def step_host(self, times: np.ndarray, labels: np.ndarray) -> np.ndarray:
+        """End-to-end step from host arrays: pinned host -> device copy, step, loss back to the host."""
+        self.h_times.numpy()[...] = times
+        self.h_labels.numpy()[...] = labels
+        self.in_times.copy_(self.h_times, non_blocking=True)
+        self.labels.copy_(self.h_labels, non_blocking=True)
+        self.run()
+        self.h_loss.copy_(self.loss, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return self.h_loss.numpy()
+
+    @property
+    def h2d_bytes(self) -> int:
+        return self.h_times.numel() * 4 + self.h_labels.numel() * 4
+
+    @property
+    def d2h_bytes(self) -> int:
+        return self.h_loss.numel() * 4

@@ -1,0 +1,423 @@
+"""Benchmark of the BATS train step on GB300: samples/s of forward + spike-count loss + exact backward
++ Adam on the 784-800-800-10 network, batch 256 (synthetic MNIST-like spike input).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is the device-resident batched train step (bats_gb300.train.FCTrainStep,
+replayed as a CUDA graph when capture works) at the literal configuration (weights N(0, 1/sqrt(fan_in)),
+thresholds 1.0 hidden / 1.3 output); `active` repeats it in the reference's MNIST training regime
+(weights U(-1, 1), hidden threshold 0.2) where every layer spikes. `e2e` is the same step through the
+public API with host inputs (pinned host -> device copy and the loss read back inside the timed
+region). `plain_api` is the layer-by-layer drop-in API (Network / LIFLayer / AdamOptimizer with
+per-sample gradients and the caller's batch mean); `refkern` runs the reference's own CUDA kernels on
+the same GPU; `cpu_baseline` is the float64 oracle on the host cores. `--impl reference` times the
+reference path on the host cores (the reference has no CPU implementation of its own, so this is the
+oracle port of it).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "samples/s fwd+exact-bwd and serve p99 ms vs plain kernels, 1 GB300, tol 1e-5"
+B = 256
+SIZES = [784, 800, 800, 10]
+TAU_S = 0.13
+K_SPIKE = 30
+MAX_SIM = 0.2
+TARGET_TRUE, TARGET_FALSE = 15.0, 3.0
+LR = 3e-3
+
+
+def make_inputs(batch, seed):
+    rng = np.random.default_rng(seed)
+    fire = rng.random((batch, SIZES[0])) < 0.19
+    t = np.where(fire, rng.uniform(0, 0.01, (batch, SIZES[0])), np.inf).astype(np.float32)[:, :, None]
+    labels = rng.integers(0, SIZES[-1], batch).astype(np.int32)
+    return t, fire.astype(np.int32), labels
+
+
+def make_weights(variant, seed=0):
+    rng = np.random.default_rng(seed)
+    ws = []
+    for n_pre, n_post in zip(SIZES[:-1], SIZES[1:]):
+        if variant == "literal":
+            ws.append(rng.normal(0, 1 / np.sqrt(n_pre), (n_post, n_pre)).astype(np.float32))
+        else:
+            ws.append(rng.uniform(-1, 1, (n_post, n_pre)).astype(np.float32))
+    return ws
+
+
+def thresholds(variant):
+    hidden = 1.0 if variant == "literal" else 0.2
+    return [hidden] * (len(SIZES) - 2) + [1.3]
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# CPU baseline (float64 oracle), run in spawned worker processes
+
+def _oracle_train_samples(args):
+    """Forward + loss + exact backward of a few samples with the float64 oracle (no GPU)."""
+    times, labels, weights, ths = args
+    sys.path.insert(0, ROOT)
+    from oracle import bats_ref64 as R
+    tau = 2 * TAU_S
+    outs = []
+    pre = times.astype(np.float64)
+    layer_in = [pre]
+    for w, th in zip(weights, ths):
+        o = R.lif_forward(layer_in[-1], w.astype(np.float64), TAU_S, th, th, K_SPIKE, MAX_SIM)
+        outs.append(o)
+        layer_in.append(o[3])
+    n_out = outs[-1][0]
+    targets = R.class_targets(labels, SIZES[-1], TARGET_TRUE, TARGET_FALSE)
+    _, err = R.spike_count_loss(n_out, targets, K_SPIKE)
+    grads = []
+    for li in range(len(weights) - 1, -1, -1):
+        n, a, x, t, z = outs[li]
+        th = ths[li]
+        R.propagate_recurrent_errors(x, z, err, th / tau)
+        f1, f2 = R.compute_factors(t, a, th / tau, x, z, tau)
+        pin = layer_in[li]
+        es, ee = R.compute_pre_exps(pin, TAU_S, tau)
+        grads.append(R.compute_weights_gradient(f1, f2, t, (pin, es, ee), err).sum(0))
+        if li > 0:
+            err = R.propagate_errors_to_pre_spikes(f1, f2, t, (pin, es, ee), weights[li], err, TAU_S, tau)
+    return times.shape[0]
+
+
+def cpu_baseline(variant, budget_s=12.0, cores=None):
+    cores = cores or os.cpu_count() or 1
+    times, _, labels = make_inputs(4 * cores, seed=1)
+    ws = make_weights(variant)
+    ths = thresholds(variant)
+    ctx = mp.get_context("spawn")
+    chunks = [(times[i:i + 1], labels[i:i + 1], ws, ths) for i in range(times.shape[0])]
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_train_samples, chunks[:cores])  # warm the workers up
+        t0 = time.perf_counter()
+        done = 0
+        while True:
+            done += sum(pool.map(_oracle_train_samples, chunks))
+            el = time.perf_counter() - t0
+            if el >= budget_s or done >= 64 * cores:
+                break
+    return {"value": done / el, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": f"{done} samples of the {variant} 784-800-800-10 train step (forward, loss, exact backward; "
+                      f"float64 NumPy oracle, one process per core), {el:.1f} s"}
+
+
+# ---------------------------------------------------------------------------------------------------------------------
+# GPU helpers
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip().lower() == "active"})
+        loaded = [v for v in sm if v > 0.5 * mx] or sm
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].strip() not in ("", "[N/A]"))}
+
+
+def flush_l2(buf):
+    buf.add_(1.0)  # 512 MB read-modify-write: evicts the 129 MB L2 between timed steps
+
+
+def time_steps(fn, steps, warmup, flush_buf, kernel_timer=None, dist=None):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        flush_l2(flush_buf)
+        starts[i].record()
+        fn()
+        ends[i].record()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    wall = time.perf_counter() - t0
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    return ms, wall
+
+
+def build_train_step(variant, graph=True):
+    import torch
+    from bats_gb300.train import FCLayerSpec, FCTrainStep
+    ths = thresholds(variant)
+    specs = [FCLayerSpec(n, TAU_S, th, th, K_SPIKE) for n, th in zip(SIZES[1:], ths)]
+    ws = [torch.tensor(w) for w in make_weights(variant)]
+    ts = FCTrainStep(B, SIZES[0], 1, specs, ws, TARGET_TRUE, TARGET_FALSE, learning_rate=LR, max_simulation=MAX_SIM)
+    t, _, labels = make_inputs(B, seed=0)
+    ts.set_inputs(torch.tensor(t), torch.tensor(labels))
+    return ts
+
+
+def kernel_breakdown(ts):
+    """Device time of each launch of one step (CUDA events around every launch)."""
+    import torch
+    rec = ts.profile_step()
+    torch.cuda.synchronize()
+    return {k: s.elapsed_time(e) for k, (s, e) in rec.items()}
+
+
+def spike_counts(ts):
+    return [int(o[0].sum().item()) for o in ts.out]
+
+
+def algorithmic_bytes(ts, name):
+    """SpMM-convention bytes of one launch (one FP32 weight read per event x post-neuron synapse)."""
+    li = int(name[1]) - 1
+    kind = name.split(".")[1]
+    ev = ts.ev[li]
+    S = int(ev.counts.sum().item())
+    spec = ts.specs[li]
+    N = spec.n_neurons
+    if kind == "forward":
+        return 8 * S + 4 * S * N + ts.B * N * (4 + 16 * spec.max_n_spike)
+    if kind in ("grad", "pre_err"):
+        n_spk = int(ts.out[li][0].sum().item())
+        return 4 * S * N + 16 * n_spk + (4 * N * ev.n_neurons if kind == "grad" else 0)
+    if kind == "sort":
+        return ts.B * ev.cap * 4 + 20 * S
+    return None
+
+
+def run_ours(args, dist, rank, world):
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    import bats_gb300
+    bats_gb300.load_library()
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    result = {}
+    for variant in ("literal", "active"):
+        ts = build_train_step(variant)
+        graphed = ts.try_capture()
+        fn = ts.replay if graphed else ts.step
+        with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+            ms, wall = time_steps(fn, args.steps, args.warmup, flush, dist=dist)
+        clocks = clk.summary()
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        sps = world * B * args.steps / (ms / 1e3)
+        kb = kernel_breakdown(ts)
+        top = max(kb, key=kb.get)
+        # Live timing of the dominant kernel over timed steps.
+        top_ms = ts.time_launch(top, args.steps, flush)
+        abytes = algorithmic_bytes(ts, top)
+        achieved = abytes / (top_ms / 1e3) / 1e9 if abytes else None
+        e2e = None
+        if variant == "literal" or True:
+            t_host, _, l_host = make_inputs(B, seed=0)
+            for _ in range(args.warmup):
+                ts.step_host(t_host, l_host)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                ts.step_host(t_host, l_host)
+            e2e_s = time.perf_counter() - t0
+            e2e = {"value": world * B * args.steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": ts.h2d_bytes,
+                   "d2h_bytes_per_step": ts.d2h_bytes}
+        result[variant] = {
+            "value": sps, "ms_per_step": ms / args.steps, "graph": graphed, "clocks": clocks, "e2e": e2e,
+            "spikes_per_layer_last_step": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
+            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                         "algorithmic_bytes_per_launch": abytes, "launch_ms": top_ms,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
+            "gpu_launches": ts.launches_per_step * args.steps,
+        }
+        del ts
+        torch.cuda.empty_cache()
+    # Plain (layer-by-layer) drop-in API and the reference kernels, active regime (few steps).
+    result["active"]["plain_api"] = plain_api_rate("active", max(2, args.steps // 4), flush)
+    result["active"]["refkern"] = refkern_rate("active", 2, flush)
+    return result
+
+
+def plain_api_rate(variant, steps, flush):
+    import torch
+    from bats_gb300 import Network, SpikeCountClassLoss
+    from bats_gb300.Layers import InputLayer, LIFLayer
+    from bats_gb300.Optimizers import AdamOptimizer
+    ws = make_weights(variant)
+    ths = thresholds(variant)
+    net = Network()
+    prev = InputLayer(n_neurons=SIZES[0], name="in")
+    net.add_layer(prev, input=True)
+    for i, (w, th) in enumerate(zip(ws, ths)):
+        layer = LIFLayer(prev, n_neurons=w.shape[0], tau_s=TAU_S, theta=th, delta_theta=th,
+                         weight_initializer=lambda a, b, w=w: torch.tensor(w, device="cuda"), max_n_spike=K_SPIKE,
+                         name=f"l{i}")
+        net.add_layer(layer)
+        prev = layer
+    loss_fn = SpikeCountClassLoss(TARGET_TRUE, TARGET_FALSE)
+    opt = AdamOptimizer(learning_rate=LR)
+    t, n, labels = make_inputs(B, 0)
+    labels_d = torch.tensor(labels, device="cuda")
+
+    def step():
+        net.reset()
+        net.forward(t, n, max_simulation=MAX_SIM, training=True)
+        sp, nsp = net.output_spike_trains
+        loss, err = loss_fn.compute_loss_and_errors(sp, nsp, labels_d)
+        g = net.backward(err)
+        d = opt.step([None if x is None else x.mean(0) for x in g])
+        net.apply_deltas(d)
+
+    ms, _ = time_steps(step, steps, 1, flush)
+    return {"value": B * steps / (ms / 1e3), "unit": "samples/s", "steps": steps,
+            "what": "Network/LIFLayer/SpikeCountClassLoss/AdamOptimizer drop-in API, per-sample gradients"}
+
+
+def refkern_rate(variant, steps, flush):
+    import torch
+    from oracle import refkern
+    if not refkern.available():
+        return {"unavailable": "reference kernels not built (oracle/_ref)"}
+    ws = [torch.tensor(w, device="cuda") for w in make_weights(variant)]
+    ths = thresholds(variant)
+    layers = [refkern.RefLIF(w, TAU_S, th, th, K_SPIKE) for w, th in zip(ws, ths)]
+    t, n, labels = make_inputs(B, 0)
+    td, nd = torch.tensor(t, device="cuda"), torch.tensor(n, device="cuda")
+    m = [torch.zeros_like(w) for w in ws]
+    v = [torch.zeros_like(w) for w in ws]
+    state = {"t": 0}
+    tt = torch.full((B, SIZES[-1]), TARGET_FALSE, device="cuda")
+    tt[torch.arange(B), torch.tensor(labels, device="cuda").long()] = TARGET_TRUE
+
+    def step():
+        x, c = td, nd
+        for L in layers:
+            o = L.forward(x, c, np.float32(MAX_SIM))
+            x, c = o[3], o[0]
+        err = (tt - c.float())[:, :, None].repeat(1, 1, K_SPIKE).contiguous()
+        grads = []
+        for i in range(len(layers) - 1, -1, -1):
+            g, err = layers[i].backward(err, want_pre=i > 0)
+            grads.insert(0, g.mean(0))
+        state["t"] += 1
+        for i, g in enumerate(grads):
+            m[i].mul_(0.9).add_(0.1 * g)
+            v[i].mul_(0.999).add_(0.001 * g * g)
+            mh = m[i] / (1 - 0.9 ** state["t"])
+            vh = v[i] / (1 - 0.999 ** state["t"])
+            layers[i].w.add_(-(LR * mh / (vh.sqrt() + 1e-8)))
+
+    ms, _ = time_steps(step, steps, 1, flush)
+    return {"value": B * steps / (ms / 1e3), "unit": "samples/s", "steps": steps,
+            "what": "reference CUDA kernels (unmodified, oracle/_ref) with the reference wrappers' launch shapes"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline("active", budget_s=max(5.0, min(60.0, args.cpu_budget * args.steps / 10)))
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "samples/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "784-800-800-10 BATS train step, batch 256, active regime (host cores)"},
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    # CPU baseline first (spawned workers, before any GPU context exists in this process).
+    cb = cpu_baseline("active", budget_s=args.cpu_budget) if rank == 0 else None
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+    res = run_ours(args, dist, rank, world)
+    if rank != 0:
+        return
+    lit, act = res["literal"], res["active"]
+    line = {
+        "metric": METRIC, "value": lit["value"], "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": lit["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "784-800-800-10 BATS train step (forward, spike-count loss, exact backward, Adam)",
+                   "global_batch": B * world, "variant": "literal: W~N(0,1/sqrt(fan_in)), theta 1.0 hidden/1.3 out",
+                   "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (512 MB write)",
+                   "cuda_graph": lit["graph"]},
+        "roofline": lit["roofline"], "e2e": lit["e2e"], "gpu_launches": lit["gpu_launches"], "clocks": lit["clocks"],
+        "cpu_baseline": cb, "spikes_per_layer": lit["spikes_per_layer_last_step"], "kernels_ms": lit["kernels_ms"],
+        "active": act,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+/*
+ * bats_gb300 — C ABI of the GB300 (sm_103a) kernels for event-based LIF simulation and exact
+ * multi-spike error backpropagation (the BATS method).
+ *
+ * Conventions
+ *   - Every pointer is a device pointer owned by the caller (for example a torch tensor's
+ *     data_ptr()); the library never allocates device memory. Entry points that need scratch
+ *     memory take (workspace, workspace_bytes) and have a *_workspace_bytes() query.
+ *   - Every entry point returns a status (BATS_OK == 0); bats_last_error() describes the last
+ *     failure of the calling thread. Launches are asynchronous on `stream`.
+ *   - Spike trains are (B, N, K) float32 row-major, +inf after the neuron's spikes, with counts
+ *     (B, N) int32. Weights of a fully-connected layer are (N_post, N_pre); the forward and
+ *     error-propagation kernels read the transposed copy wt (N_pre, ld), ld >= N_post and
+ *     ld % 4 == 0 (bats_transpose builds it). Conv filters are (C_out, fx, fy, C_in).
+ *   - `events` is an array of 16-byte records {float t; int j; float exp(t/tau_s); float exp(t/tau)}
+ *     of shape (B, ev_cap), ev_cap = N_pre * K_pre, filled by bats_sort_events.
+ *
+ * The reference is the CuPy implementation (Florian-BACHO/bats); each entry point names the
+ * wrapper(s) in bats/CudaKernels/Wrappers/ (and the .cu kernels under bats/CudaKernels/CuFiles/)
+ * whose job it takes over.
+ */
+#ifndef BATS_GB300_H
+#define BATS_GB300_H
+
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BATS_ABI_VERSION 1
+
+#define BATS_OK 0
+#define BATS_ERR_BAD_SHAPE 1
+#define BATS_ERR_NULL 2
+#define BATS_ERR_CAPACITY 3
+#define BATS_ERR_WORKSPACE 4
+#define BATS_ERR_CUDA 5
+#define BATS_ERR_TIMEOUT 6
+
+int bats_abi_version(void);
+const char* bats_status_string(int status);
+const char* bats_last_error(void);
+
+/* ---- Inference ------------------------------------------------------------------------------ */
+
+/* exp(t/tau_s), exp(t/tau) elementwise.
+ * Replaces compute_pre_exps (bats/CudaKernels/Wrappers/Inference/compute_pre_exps.py:10-18). */
+int bats_compute_pre_exps(const float* times, long long count, float tau_s, float tau, float* exp_tau_s,
+                          float* exp_tau, cudaStream_t stream);
+
+/* Per-sample time sort of the valid (time < +inf) pre-synaptic spike slots into `events`
+ * (B, N_pre*K_pre) plus the slot index n*K_pre+k of each event (slot_out, may be NULL) and the
+ * per-sample count. The events' exponentials are __expf(t/tau_s), __expf(t/tau), or gathered from
+ * exp_tau_s / exp_tau (B, N_pre, K_pre) when those are given. Replaces get_sorted_spikes_indices + take_along_axis + compute_pre_exps
+ * (bats/CudaKernels/Wrappers/Inference/get_sorted_spikes_indices.py:7-17; bats/Layers/LIFLayer.py:66-84). */
+size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_pre);
+int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, float tau_s, float tau,
+                     const float* exp_tau_s, const float* exp_tau, void* events,
+                     int* slot_out, int* ev_count, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* Fully-connected LIF forward: spike counts (B, N_post) and a, x, times, post_exp_tau (B, N_post, K_post);
+ * times/post_exp_tau are +inf after the spikes, a/x are undefined there. c = theta/tau,
+ * delta_theta_tau = delta_theta/tau. Replaces get_spike_weights + compute_spike_times
+ * (bats/CudaKernels/Wrappers/Inference/get_spike_weights.py:9-18, compute_spike_times.py:11-32). */
+int bats_lif_forward_fc(const void* events, const int* ev_count, long long ev_cap, const float* weights_t, int ld,
+                        int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,
+                        float max_simulation, int* n_spikes, float* a, float* x, float* times, float* post_exp_tau,
+                        cudaStream_t stream);
+
+/* Convolutional LIF forward on a (X, Y, C) input with (C_out, fx, fy, C) filters, valid, stride 1.
+ * Replaces compute_spike_times_conv (bats/CudaKernels/Wrappers/Inference/compute_spike_times_conv.py:11-35). */
+int bats_conv_forward(const void* events, const int* ev_count, long long ev_cap, const float* weights, int batch,
+                      int X, int Y, int C, int fx, int fy, int C_out, int k_post, float c, float delta_theta_tau,
+                      float tau, float max_simulation, int* n_spikes, float* a, float* x, float* times,
+                      float* post_exp_tau, cudaStream_t stream);
+
+/* 2x2 spike-union pooling of a (X, Y, C) layer with K slots: counts, times sorted over 4K slots and
+ * the flat (batch-global) source slot of every output slot. Replaces aggregate_spikes_conv
+ * (bats/CudaKernels/Wrappers/Inference/aggregate_spikes_conv.py:10-28). */
+int bats_pool_forward(const int* n_spikes, const float* times, int batch, int X, int Y, int C, int K,
+                      int* out_n_spikes, float* out_times, int* out_indices, cudaStream_t stream);
+
+/* ---- Backpropagation ------------------------------------------------------------------------ */
+
+/* Per (sample, post neuron): reset errors in place on `errors` (if do_recurrent), factors f1/f2
+ * (if do_factors) and, if `tables` is given, the suffix tables (B, N_post, K_post+1) float2 of
+ * (sum_{k>=p} err_k f1_k, sum_{k>=p} err_k f2_k) with the count of leading spikes in nvalid (B, N_post).
+ * Replaces propagate_recurrent_errors and compute_factors
+ * (bats/CudaKernels/Wrappers/Backpropagation/propagate_recurrent_errors.py:9-16, compute_factors.py:11-22). */
+int bats_backward_prep(const float* post_times, const float* a, const float* x, const float* post_exp_tau,
+                       float* errors, int batch, int n_post, int k_post, float c, float tau, float delta_theta_tau,
+                       int do_recurrent, int do_factors, float* f1, float* f2, void* tables, int* nvalid,
+                       cudaStream_t stream);
+
+/* Weight gradient of a fully-connected layer. group == 1: per-sample gradient (B, N_post, N_pre) like the
+ * reference; group > 1: the batch mean (N_post, N_pre), accumulated per group of samples and reduced in a
+ * fixed order (deterministic). Replaces compute_weights_gradient (+ the caller's mean over the batch)
+ * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24). */
+size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, int n_pre, int group);
+int bats_weights_gradient(const void* events, const int* ev_count, long long ev_cap, const float* post_times,
+                          const void* tables, const int* nvalid, int batch, int n_post, int k_post, int n_pre,
+                          int group, float* grad, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* Errors of the pre-synaptic spikes (B, N_pre, K_pre), zero where there is no spike. Replaces
+ * propagate_errors_to_pre_spikes and its (B, N_pre, K_pre, N_post) temporary + sum
+ * (bats/CudaKernels/Wrappers/Backpropagation/propagate_errors_to_pre_spikes.py:11-27). */
+size_t bats_pre_errors_workspace_bytes(int batch, long long ev_cap, int n_post);
+int bats_pre_errors(const void* events, const int* ev_slot, const int* ev_count, long long ev_cap,
+                    const float* weights_t, int ld, const float* post_times, const void* tables, const int* nvalid,
+                    int batch, int n_post, int k_post, int n_pre, int k_pre, float tau_s, float tau,
+                    float* pre_errors, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* Convolutional backward: per-sample filter gradient (B, C_out, fx, fy, C) and, if pre_errors is not
+ * NULL, the pre-spike errors (B, X*Y*C, k_pre). Replaces compute_weights_gradient_conv and
+ * propagate_errors_to_pre_spikes_conv (bats/CudaKernels/Wrappers/Backpropagation/
+ * compute_weights_gradient_conv.py:11-32, propagate_errors_to_pre_spikes_conv.py:11-32). */
+int bats_conv_backward(const void* events, const int* ev_slot, const int* ev_count, long long ev_cap,
+                       const float* weights, int batch, int X, int Y, int C, int fx, int fy, int C_out, int k_pre,
+                       const float* post_times, const void* tables, const int* nvalid, int k_post, float tau_s,
+                       float tau, float* grad_per_sample, float* pre_errors, cudaStream_t stream);
+
+/* Pooling backward: pre_errors[indices[q]] = errors[q] (zero elsewhere).
+ * Replaces the cp.put scatter of PoolingLayer.backward (bats/Layers/PoolingLayer.py:55-66). */
+int bats_pool_backward(const float* errors, const int* indices, long long count, float* pre_errors,
+                       long long pre_count, cudaStream_t stream);
+
+/* ---- Losses and optimizer ------------------------------------------------------------------- */
+
+/* loss (B) = 1/2 sum (target - count)^2, errors (B, N, K) = target - count broadcast over K. counts are
+ * int32 or float32 (count_is_float). Either targets (B, N) or labels (B) with target_true/target_false.
+ * Replaces SpikeCountLoss / SpikeCountClassLoss (bats/Losses/SpikeCountLoss.py:17-38,
+ * bats/Losses/SpikeCountClassLoss.py:15-33). loss or errors may be NULL. */
+int bats_spike_count_loss(const void* counts, int count_is_float, const float* targets, const int* labels,
+                          float target_true, float target_false, int batch, int n, int k, float* loss,
+                          float* errors, cudaStream_t stream);
+
+/* Softmax cross-entropy of first-spike times with errors in slot 0.
+ * Replaces TTFSSoftmaxCrossEntropy (bats/Losses/TTFSSoftmaxCrossEntropy.py:23-56). */
+int bats_ttfs_softmax_cross_entropy(const float* spikes, const int* labels, int batch, int n, int k, double tau,
+                                    float* loss, float* errors, cudaStream_t stream);
+
+/* Squared error of first-spike times (mode 0 loss, 1 errors, 2 both); targets modified in place (inf -> 1).
+ * Replaces SpikeTimeLoss (bats/Losses/SpikeTimeLoss.py:20-47). */
+int bats_spike_time_loss(const float* spikes, float* targets, int batch, int n, int k, int mode, float* loss,
+                         float* errors, cudaStream_t stream);
+
+/* One Adam step on one tensor: m, v in place; delta written (if not NULL) and/or added to weights (if not
+ * NULL), the new weights also written transposed into weights_t (n_pre, ld) if given.
+ * bias_correction_i = 1 - beta_i^t. Replaces AdamOptimizer.step + Network.apply_deltas
+ * (bats/Optimizers/AdamOptimizer.py:35-55, bats/Network.py:50-54). */
+int bats_adam_step(const float* grad, float* m, float* v, long long count, float beta_1, float beta_2, float epsilon,
+                   float learning_rate, double bias_correction_1, double bias_correction_2, float* delta,
+                   float* weights, float* weights_t, int n_post, int n_pre, int ld, cudaStream_t stream);
+
+/* Device-side Adam bias-correction state for captured steps: powers[0..1] (double) *= beta_1, beta_2.
+ * Start from {1, 1}; call once per step before bats_adam_step_device. Replaces the host-side
+ * `self.__t += 1` and `beta ** t` of AdamOptimizer.step (bats/Optimizers/AdamOptimizer.py:36, 49-50). */
+int bats_adam_powers_advance(double* powers, float beta_1, float beta_2, cudaStream_t stream);
+
+/* bats_adam_step with the bias corrections 1 - powers[i] read from device memory and the delta added to
+ * the weights (and their transposed copy) in place. Replaces AdamOptimizer.step + Network.apply_deltas. */
+int bats_adam_step_device(const float* grad, float* m, float* v, long long count, float beta_1, float beta_2,
+                          float epsilon, float learning_rate, const double* powers, float* weights, float* weights_t,
+                          int n_post, int n_pre, int ld, cudaStream_t stream);
+
+/* weights += delta, optionally refreshing the transposed copy. Replaces LIFLayer.add_deltas
+ * (bats/Layers/LIFLayer.py:112-113). */
+int bats_add_deltas(float* weights, const float* delta, long long count, float* weights_t, int n_pre, int ld,
+                    cudaStream_t stream);
+
+/* out (cols, ld) = in (rows, cols)^T. Builds the transposed weights read by the FC kernels. */
+int bats_transpose(const float* in, int rows, int cols, float* out, int ld, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BATS_GB300_H */

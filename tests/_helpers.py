@@ -1,0 +1,57 @@
+"""Shared input generators and comparison helpers of the parity tests."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import bats_ref64 as R
+
+
+def mnist_like_input(batch, n_in=784, p=0.19, t_max=0.01, seed=0):
+    """Each input neuron fires once with probability p at U(0, t_max), else stays silent (inf, count 0):
+    the synthetic stand-in of the reference's MNIST encoding (experiments/mnist/Dataset.py:66-71)."""
+    rng = np.random.default_rng(seed)
+    fire = rng.random((batch, n_in)) < p
+    t = np.where(fire, rng.uniform(0, t_max, (batch, n_in)), np.inf).astype(np.float32)
+    return t[:, :, None], fire.astype(np.int32)
+
+
+def multi_spike_input(batch, n_in, k, t_max, seed=0, p_silent=0.2):
+    """Per neuron 0..k sorted spikes at U(0, t_max)."""
+    rng = np.random.default_rng(seed)
+    t = np.full((batch, n_in, k), np.inf, dtype=np.float32)
+    n = rng.integers(0, k + 1, (batch, n_in))
+    n[rng.random((batch, n_in)) < p_silent] = 0
+    for s in range(batch):
+        for j in range(n_in):
+            t[s, j, :n[s, j]] = np.sort(rng.uniform(0, t_max, n[s, j]))
+    return t, n.astype(np.int32)
+
+
+def grazing_mask(pre_t, W, tau_s, theta, delta_theta, K, max_sim, rel=1e-5, conv=None):
+    """Neurons whose float64 spike count changes when theta moves by +-rel: their membrane maximum lies
+    within rel of the threshold, where an FP32 evaluation may legitimately flip the count.
+    Returns (n_low_theta, n_high_theta)."""
+    f = R.lif_forward if conv is None else (lambda t, w, *a: R.conv_forward(t, w, conv, *a))
+    n_lo = f(pre_t.astype(np.float64), W, tau_s, theta * (1 - rel), delta_theta, K, max_sim)[0]
+    n_hi = f(pre_t.astype(np.float64), W, tau_s, theta * (1 + rel), delta_theta, K, max_sim)[0]
+    return np.minimum(n_lo, n_hi), np.maximum(n_lo, n_hi)
+
+
+def count_mismatches(n_gpu, n_ref, bounds=None):
+    """(# differing counts, # not explained by grazing)."""
+    diff = n_gpu != n_ref
+    if bounds is None:
+        return int(diff.sum()), int(diff.sum())
+    lo, hi = bounds
+    unexplained = diff & ~((n_gpu >= lo) & (n_gpu <= hi))
+    return int(diff.sum()), int(unexplained.sum())
+
+
+def leading_mask(n, K):
+    return np.arange(K)[None, None, :] < n[:, :, None]
+
+
+def rel_err(a, b, floor=0.0):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b) / np.maximum(np.abs(b), floor)

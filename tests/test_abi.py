@@ -1,0 +1,75 @@
+"""CPU checks of the C ABI boundary: the shared library loads and exports every entry point that
+include/bats_gb300.h declares, with the signatures the Python binding uses. No kernel is launched."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "bats_gb300.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(bats_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from bats_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from bats_gb300.build import build
+        build()
+    return ctypes.CDLL(_lib.LIB_PATH)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "bats_lif_forward_fc" in syms and "bats_pre_errors" in syms
+    assert len(syms) >= 20
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_every_declared_symbol():
+    from bats_gb300 import _lib
+    missing = [s for s in declared_symbols() if s not in _lib.SIGNATURES]
+    assert not missing, missing
+
+
+def test_status_strings_and_version(lib):
+    lib.bats_status_string.restype = ctypes.c_char_p
+    lib.bats_abi_version.restype = ctypes.c_int
+    assert lib.bats_abi_version() == 1
+    assert lib.bats_status_string(0) == b"ok"
+    assert b"workspace" in lib.bats_status_string(4)
+
+
+def test_shape_validation_without_a_gpu(lib):
+    """Argument checks happen on the host before any launch and return a status."""
+    from bats_gb300 import _lib
+    L = _lib.load()
+    st = L.bats_lif_forward_fc(None, None, 0, None, 1, 2, 4, 3, 1.0, 1.0, 1.0, 1.0, None, None, None, None, None,
+                               None, None)
+    assert st == 1  # BATS_ERR_BAD_SHAPE: ld < n_post
+    st = L.bats_sort_events(None, 2, 3, 0, 1.0, 1.0, None, None, None, None, None, None, 0, None)
+    assert st == 1
+    assert b"sort_events" in L.bats_last_error()
+    # batch 0 is a no-op
+    assert L.bats_adam_step(None, None, None, 0, 0.9, 0.999, 1e-8, 1e-3, 0.1, 0.001, None, None, None, 0, 0, 0,
+                            None) == 0
+
+
+def test_workspace_queries(lib):
+    from bats_gb300 import _lib
+    L = _lib.load()
+    assert L.bats_sort_events_workspace_bytes(4, 10, 3) == 0  # fits in shared memory
+    assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 4 * 30000 * 4
+    assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == 16 * 800 * 784 * 4
+    assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 1) == 0
+    assert L.bats_pre_errors_workspace_bytes(2, 100, 300) == 2 * 100 * 3 * 4

@@ -1,0 +1,184 @@
+"""GPU parity of the exact backward (reset errors, factors, weight gradient, pre-spike errors).
+
+Kernel-level checks use the golden fixtures built from the reference tests' own CPU loops
+(tests/golden/*.npz); layer-level checks run the reference's CUDA kernels (oracle/refkern.py) on the
+same forward state. Gradients are sums of many signed terms; the tolerance is stated relative to the
+sum of the terms' magnitudes (the float64 oracle evaluated with |err|, |f1|, -|f2| for the gradient
+and |W|, |err|, |f1|, |f2|, -tau for the pre errors, so that every term is added):
+    |g - g_ref| <= 1e-5 * |g_ref| + 1e-5 * G_abs.
+Spike-time-level quantities (factors, recurrent errors) use 1e-5 relative.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from bats_gb300 import kernels as K
+from oracle import bats_ref64 as R
+from oracle import refkern
+from tests._helpers import mnist_like_input, multi_spike_input
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def cu(a, dtype=torch.float32):
+    return torch.tensor(np.asarray(a), device="cuda", dtype=dtype)
+
+
+def assert_sum_close(got, ref, abs_scale, rtol=1e-5, what=""):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    tol = rtol * np.abs(ref) + rtol * np.asarray(abs_scale, dtype=np.float64) + 1e-30
+    err = np.abs(got - ref)
+    worst = np.max(err / tol) if err.size else 0.0
+    assert worst <= 1.0, f"{what}: worst error / tolerance = {worst:.3f}"
+
+
+def leading_only(post_t, f1, f2, err):
+    """Zero the factors after a neuron's first inf post time (the kernels stop there)."""
+    inf = np.isinf(post_t)
+    after = np.cumsum(inf, axis=-1) > 0
+    return np.where(after, 0, f1), np.where(after, 0, f2), np.where(after, 0, err)
+
+
+def test_weights_gradient_and_pre_errors_vs_reference_test_loops(cuda):
+    d = load("fc_backward_kernels")
+    g = K.compute_weights_gradient(cu(d["f1"]), cu(d["f2"]), cu(d["post_t"]), cu(d["pre_t"]), cu(d["es"]),
+                                   cu(d["ee"]), cu(d["errors"])).cpu().numpy()
+    pre = (d["pre_t"].astype(np.float64), d["es"].astype(np.float64), d["ee"].astype(np.float64))
+    f1, f2, e = leading_only(d["post_t"], d["f1"], d["f2"], d["errors"])
+    exp = R.compute_weights_gradient(f1, f2, d["post_t"], pre, e)
+    gabs = R.compute_weights_gradient(np.abs(f1), -np.abs(f2), d["post_t"], pre, np.abs(e))
+    assert_sum_close(g, exp, gabs, what="weights gradient")
+    full = ~np.isinf(d["post_t"]).any(-1)
+    assert_sum_close(g[full], d["grad"][full], gabs[full], what="weights gradient vs reference test loop")
+    pe = K.propagate_errors_to_pre_spikes(cu(d["f1"]), cu(d["f2"]), cu(d["post_t"]), cu(d["pre_t"]), cu(d["es"]),
+                                          cu(d["ee"]), cu(d["weights"]), cu(d["errors"]), float(d["tau_s"]),
+                                          float(d["tau"])).cpu().numpy()
+    pabs = R.propagate_errors_to_pre_spikes(np.abs(f1), np.abs(f2), d["post_t"], pre, np.abs(d["weights"]),
+                                            np.abs(e), float(d["tau_s"]), -float(d["tau"]))
+    assert_sum_close(pe, d["pre_errors"], pabs, what="pre errors vs reference test loop")
+
+
+def test_conv_backward_kernels_vs_reference_test_loops(cuda):
+    d = load("conv_backward_kernels")
+    g = K.compute_weights_gradient_conv(cu(d["f1"]), cu(d["f2"]), cu(d["post_t"]), cu(d["pre_t"]), cu(d["es"]),
+                                        cu(d["ee"]), d["pre_shape"], d["post_shape"], d["filter_shape"],
+                                        cu(d["errors"])).cpu().numpy()
+    pre = (d["pre_t"].astype(np.float64), d["es"].astype(np.float64), d["ee"].astype(np.float64))
+    gabs = R.conv_weights_gradient(np.abs(d["f1"]), -np.abs(d["f2"]), d["post_t"], pre, np.abs(d["errors"]),
+                                   tuple(d["filter_shape"]), tuple(d["pre_shape"]))
+    assert_sum_close(g, d["grad"], gabs, what="conv gradient")
+    pe = K.propagate_errors_to_pre_spikes_conv(cu(d["f1"]), cu(d["f2"]), cu(d["post_t"]), cu(d["pre_t"]), cu(d["es"]),
+                                               cu(d["ee"]), cu(d["filters"]), cu(d["errors"]), float(d["tau_s"]),
+                                               float(d["tau"]), d["pre_shape"]).cpu().numpy()
+    pabs = R.conv_pre_errors(np.abs(d["f1"]), np.abs(d["f2"]), d["post_t"], pre, np.abs(d["filters"]),
+                             np.abs(d["errors"]), float(d["tau_s"]), -float(d["tau"]), tuple(d["pre_shape"]))
+    assert_sum_close(pe, d["pre_errors"], pabs, what="conv pre errors")
+
+
+def test_factors_and_recurrent_known_answers(cuda):
+    d = load("factors")
+    f1, f2 = K.compute_factors(cu(d["spike_times"]), cu(d["a"]), float(d["c"]), cu(d["x"]), cu(d["exp_tau"]),
+                               float(d["tau"]))
+    np.testing.assert_allclose(f1.cpu().numpy(), d["f1"], rtol=1e-5)
+    np.testing.assert_allclose(f2.cpu().numpy(), d["f2"], rtol=1e-5)
+    r = load("kat_recurrent")
+    e = cu(r["errors"])
+    K.propagate_recurrent_errors(cu(r["x"]), cu(r["exp_tau"]), e, float(r["delta_theta_tau"]))
+    np.testing.assert_allclose(e.cpu().numpy(), r["expected"], rtol=1e-5, atol=1e-6)
+
+
+def _layer_case(variant, B=16):
+    t, n_in = mnist_like_input(B, seed=1)
+    rng = np.random.default_rng(2)
+    if variant == "active":
+        W1 = rng.uniform(-1, 1, (120, 784)).astype(np.float32)
+        W2 = rng.uniform(-1, 1, (10, 120)).astype(np.float32)
+        th1, th2 = 0.2, 1.3
+    else:
+        W1 = rng.normal(0, 1 / np.sqrt(784), (120, 784)).astype(np.float32)
+        W2 = rng.normal(0, 1 / np.sqrt(120), (10, 120)).astype(np.float32)
+        th1, th2 = 1.0, 1.3
+    return t, n_in, W1, W2, th1, th2
+
+
+@pytest.mark.parametrize("variant", ["active", "literal"])
+def test_two_layer_backward_vs_reference_kernels(cuda, variant):
+    if not refkern.available():
+        pytest.skip("reference kernels not built")
+    t, n_in, W1, W2, th1, th2 = _layer_case(variant)
+    tau_s, K_post = np.float32(0.13), 30
+    tau = np.float32(2 * tau_s)
+    # Ours.
+    tt = cu(t)
+    ev1 = K.sort_events(tt, tau_s, tau)
+    wt1 = K.transpose_weights(cu(W1))
+    n1, a1, x1, t1, z1 = K.lif_forward_fc(ev1, wt1, 120, K_post, tau_s, th1, th1, 0.2)
+    ev2 = K.sort_events(t1, tau_s, tau)
+    wt2 = K.transpose_weights(cu(W2))
+    n2, a2, x2, t2, z2 = K.lif_forward_fc(ev2, wt2, 10, K_post, tau_s, th2, th2, 0.2)
+    labels = np.arange(t.shape[0]) % 10
+    _, err2 = K.spike_count_loss(n2, labels=cu(labels, torch.int32), target_true=15, target_false=3, k=K_post)
+    err2_ref = err2.clone()
+    tau32, c2, dtt2 = K.lif_constants(tau_s, th2, th2)
+    tab2 = K.backward_prep(t2, a2, x2, z2, err2, c2, tau32, dtt2)
+    g2 = K.weights_gradient(ev2, t2, tab2, 120, per_sample=True)
+    pe2 = K.pre_errors(ev2, wt2, t2, tab2, tau_s, tau32)
+    _, c1, dtt1 = K.lif_constants(tau_s, th1, th1)
+    e1 = pe2.clone()
+    tab1 = K.backward_prep(t1, a1, x1, z1, e1, c1, tau32, dtt1)
+    g1 = K.weights_gradient(ev1, t1, tab1, 784, per_sample=True)
+    g1_mean = K.weights_gradient(ev1, t1, tab1, 784, per_sample=False, group=4)
+    # Reference kernels on the same inputs.
+    L1 = refkern.RefLIF(cu(W1), tau_s, th1, th1, K_post)
+    L2 = refkern.RefLIF(cu(W2), tau_s, th2, th2, K_post)
+    r1 = L1.forward(tt, cu(n_in, torch.int32), np.float32(0.2))
+    r2 = L2.forward(r1[3], r1[0], np.float32(0.2))
+    for ours, ref in ((n1, r1[0]), (n2, r2[0])):
+        assert torch.equal(ours, ref), "forward spike counts differ from the reference kernels"
+    rg2, rpe2 = L2.backward(err2_ref, want_pre=True)
+    rg1, _ = L1.backward(rpe2.clone(), want_pre=False)
+    torch.cuda.synchronize()
+    # Scales from the float64 oracle with absolute values.
+    f1_2, f2_2 = tab2.f1.cpu().numpy(), tab2.f2.cpu().numpy()
+    e2n = err2.cpu().numpy()
+    pre1 = (t1.cpu().numpy().astype(np.float64),) + R.compute_pre_exps(t1.cpu().numpy(), float(tau_s), float(tau32))
+    g2abs = R.compute_weights_gradient(np.abs(f1_2), -np.abs(f2_2), t2.cpu().numpy(), pre1, np.abs(e2n))
+    assert_sum_close(g2.cpu().numpy(), rg2.cpu().numpy(), g2abs, what="layer 2 gradient")
+    p2abs = R.propagate_errors_to_pre_spikes(np.abs(f1_2), np.abs(f2_2), t2.cpu().numpy(), pre1, np.abs(W2),
+                                             np.abs(e2n), float(tau_s), -float(tau32))
+    assert_sum_close(pe2.cpu().numpy(), rpe2.cpu().numpy(), p2abs, what="layer 2 pre errors")
+    f1_1, f2_1 = tab1.f1.cpu().numpy(), tab1.f2.cpu().numpy()
+    e1n = e1.cpu().numpy()
+    pre0 = (t.astype(np.float64),) + R.compute_pre_exps(t, float(tau_s), float(tau32))
+    g1abs = R.compute_weights_gradient(np.abs(f1_1), -np.abs(f2_1), t1.cpu().numpy(), pre0, np.abs(e1n))
+    assert_sum_close(g1.cpu().numpy(), rg1.cpu().numpy(), g1abs, what="layer 1 gradient")
+    # Batch mean path equals the mean of the per-sample gradients.
+    assert_sum_close(g1_mean.cpu().numpy(), g1.mean(0).cpu().numpy(), g1abs.mean(0), rtol=1e-6, what="batch mean")
+    if variant == "active":
+        assert int(n1.sum()) > 0 and float(g1.abs().sum()) > 0
+
+
+def test_backward_is_deterministic(cuda):
+    t, n_in = multi_spike_input(8, 64, 4, 0.1, seed=5)
+    rng = np.random.default_rng(5)
+    W = rng.uniform(-1, 1, (96, 64)).astype(np.float32)
+    outs = []
+    for _ in range(2):
+        ev = K.sort_events(cu(t), 0.1, 0.2)
+        wt = K.transpose_weights(cu(W))
+        n, a, x, ts, z = K.lif_forward_fc(ev, wt, 96, 20, 0.1, 0.1, 0.1)
+        err = torch.ones_like(ts)
+        tau32, c, dtt = K.lif_constants(0.1, 0.1, 0.1)
+        tab = K.backward_prep(ts, a, x, z, err, c, tau32, dtt)
+        g = K.weights_gradient(ev, ts, tab, 64, per_sample=False, group=3)
+        pe = K.pre_errors(ev, wt, ts, tab, 0.1, tau32)
+        outs.append((g.cpu(), pe.cpu()))
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])

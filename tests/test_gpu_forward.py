@@ -1,0 +1,153 @@
+"""GPU parity of the forward path (event sort + FC LIF forward) against the reference's CUDA kernels
+(oracle/refkern.py) and the float64 oracle.
+
+Tolerances (the spec contract): spike times within 1e-5 relative; spike counts exact except
+for neurons whose membrane maximum lies within 1e-5 (relative) of the threshold, identified by the
+float64 oracle at theta*(1 -+ 1e-5), which are counted and must stay rare.
+"""
+import numpy as np
+import pytest
+import torch
+
+from bats_gb300 import kernels as K
+from oracle import bats_ref64 as R
+from oracle import refkern
+from tests._helpers import count_mismatches, grazing_mask, leading_mask, mnist_like_input, multi_spike_input
+
+pytestmark = pytest.mark.gpu
+
+RTOL_T = 1e-5
+
+
+def run_fc(t, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
+    tt = torch.tensor(t, device="cuda")
+    ev = K.sort_events(tt, np.float32(tau_s), np.float32(2 * tau_s))
+    wt = K.transpose_weights(torch.tensor(W, device="cuda"))
+    n, a, x, ts, z = K.lif_forward_fc(ev, wt, W.shape[0], K_post, tau_s, theta, dtheta, max_sim)
+    torch.cuda.synchronize()
+    return [v.cpu().numpy() for v in (n, a, x, ts, z)], ev
+
+
+def run_ref(t, n_in, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
+    if not refkern.available():
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    layer = refkern.RefLIF(torch.tensor(W, device="cuda"), tau_s, theta, dtheta, K_post)
+    out = layer.forward(torch.tensor(t, device="cuda"), torch.tensor(n_in, device="cuda"), max_sim)
+    torch.cuda.synchronize()
+    return [v.cpu().numpy() for v in out]
+
+
+def check_against(ours, ref, bounds, max_unexplained=0, rtol=RTOL_T, what="", fields=("t", "z", "a", "x"), t_atol=0.0):
+    """Counts exact up to grazing neurons; the listed fields within rtol on neurons with equal counts."""
+    n, a, x, t, z = ours
+    rn, ra, rx, rt, rz = ref
+    diff, unexplained = count_mismatches(n, rn, bounds)
+    assert unexplained <= max_unexplained, f"{what}: {unexplained} unexplained count mismatches ({diff} total)"
+    same = (n == rn)[:, :, None] & leading_mask(rn, t.shape[2])
+    got = {"t": t, "z": z, "a": a, "x": x}
+    exp = {"t": rt, "z": rz, "a": ra, "x": rx}
+    for name in fields:
+        u = got[name][same].astype(np.float64)
+        v = exp[name][same].astype(np.float64)
+        e = np.abs(u - v)
+        tol = rtol * np.abs(v) + (t_atol if name == "t" else 0.0)
+        assert not (e > tol).any(), f"{what}: {name} max err {np.max(e - tol):.3e} over tolerance"
+    pad = ~leading_mask(n, t.shape[2])
+    assert np.isinf(t[pad]).all() and np.isinf(z[pad]).all()
+    return diff
+
+
+# Against the float64 oracle, t = tau ln z turns the relative error of z into an absolute error of
+# about tau * 1e-7 per FP32 rounding, so the time tolerance there is 1e-5 relative plus 1e-5 * tau.
+ORACLE = dict(fields=("t", "z"), t_atol=1e-5 * 0.26)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_small_multi_spike_vs_oracle_and_reference(cuda, seed):
+    t, n_in = multi_spike_input(4, 40, 3, 0.3, seed=seed)
+    rng = np.random.default_rng(100 + seed)
+    W = rng.normal(0, 1, (16, 40)).astype(np.float32)
+    tau_s, theta, dth, Kp = 0.1, 0.1, 0.2, 16
+    ours, _ = run_fc(t, W, tau_s, theta, dth, Kp, 0.5)
+    o64 = R.lif_forward(t.astype(np.float64), W.astype(np.float64), np.float32(tau_s), theta, dth, Kp, np.float32(0.5))
+    bounds = grazing_mask(t, W.astype(np.float64), np.float32(tau_s), theta, dth, Kp, np.float32(0.5))
+    assert ours[0].sum() > 20, "test input should make the layer spike"
+    check_against(ours, o64, bounds, what="vs oracle", **ORACLE)
+    ref = run_ref(t, n_in, W, tau_s, theta, dth, Kp, 0.5)
+    d = check_against(ours, ref, bounds, rtol=1e-6, what="vs reference kernels")
+    assert d == 0
+
+
+@pytest.mark.parametrize("variant", ["literal", "active"])
+def test_mnist_config_vs_reference_kernels(cuda, variant):
+    """784-800 hidden layer of the spike-count MNIST configuration, batch 50, seed 0."""
+    t, n_in = mnist_like_input(50, seed=0)
+    rng = np.random.default_rng(0)
+    if variant == "literal":
+        W = rng.normal(0, 1 / np.sqrt(784), (800, 784)).astype(np.float32)
+        theta = 1.0
+    else:
+        W = rng.uniform(-1, 1, (800, 784)).astype(np.float32)
+        theta = 0.2
+    ours, ev = run_fc(t, W, 0.13, theta, theta, 30, 0.2)
+    ref = run_ref(t, n_in, W, 0.13, theta, theta, 30, 0.2)
+    bounds = grazing_mask(t, W.astype(np.float64), np.float32(0.13), theta, theta, 30, np.float32(0.2))
+    check_against(ours, ref, bounds, what=f"{variant} vs reference kernels")
+    o64 = R.lif_forward(t[:8].astype(np.float64), W.astype(np.float64), np.float32(0.13), theta, theta, 30,
+                        np.float32(0.2))
+    b8 = (bounds[0][:8], bounds[1][:8])
+    check_against([v[:8] for v in ours], o64, b8, what=f"{variant} vs oracle", **ORACLE)
+    if variant == "active":
+        assert ours[0].sum() > 1000
+    assert np.array_equal(ev.counts.cpu().numpy(), n_in.sum(1))
+
+
+def test_sort_events(cuda):
+    t, n_in = multi_spike_input(3, 500, 12, 0.1, seed=3)
+    ev = K.sort_events(torch.tensor(t, device="cuda"), 0.1, 0.2)
+    e = ev.events.cpu().numpy()
+    sl = ev.slots.cpu().numpy()
+    cnt = ev.counts.cpu().numpy()
+    for s in range(3):
+        et, ej, es = R.sort_events(t[s:s + 1])[0]
+        assert cnt[s] == et.size
+        assert np.array_equal(sl[s, :cnt[s]], es)
+        assert np.array_equal(e[s, :cnt[s], 0], et.astype(np.float32))
+        assert np.array_equal(e[s, :cnt[s], 1].view(np.int32), ej)
+        np.testing.assert_allclose(e[s, :cnt[s], 2], np.exp(et / np.float32(0.1)), rtol=2e-6)
+
+
+def test_sort_events_large_sample_uses_global_path(cuda):
+    """More valid slots than the shared-memory sort holds (4096)."""
+    rng = np.random.default_rng(4)
+    t = rng.uniform(0, 1, (2, 1000, 6)).astype(np.float32)
+    t[1, :, 3:] = np.inf
+    ev = K.sort_events(torch.tensor(t, device="cuda"), 0.1, 0.2)
+    cnt = ev.counts.cpu().numpy()
+    assert cnt.tolist() == [6000, 3000]
+    e = ev.events.cpu().numpy()
+    for s in range(2):
+        et, ej, slots = R.sort_events(t[s:s + 1])[0]
+        assert np.array_equal(e[s, :cnt[s], 0], et.astype(np.float32))
+        assert np.array_equal(ev.slots.cpu().numpy()[s, :cnt[s]], slots)
+
+
+def test_edge_cases(cuda):
+    rng = np.random.default_rng(9)
+    W = rng.uniform(-1, 1, (37, 20)).astype(np.float32)
+    # Empty batch input: all outputs silent.
+    t = np.full((3, 20, 2), np.inf, dtype=np.float32)
+    (n, a, x, ts, z), _ = run_fc(t, W, 0.1, 0.1, 0.1, 5)
+    assert (n == 0).all() and np.isinf(ts).all() and np.isinf(z).all()
+    # One sample silent, one busy; buffer cap reached; max_simulation cut.
+    t, n_in = multi_spike_input(2, 20, 4, 0.2, seed=1, p_silent=0.0)
+    t[0] = np.inf
+    W2 = np.abs(W) * 3
+    ours, _ = run_fc(t, W2, 0.1, 0.05, 0.05, 3)
+    assert (ours[0][0] == 0).all() and (ours[0][1] == 3).any()
+    ref = run_ref(t, n_in, W2, 0.1, 0.05, 0.05, 3)
+    check_against(ours, ref, None, what="cap")
+    ours, _ = run_fc(t, W2, 0.1, 0.05, 0.05, 40, 0.1)
+    assert np.nanmax(np.where(np.isinf(ours[3]), np.nan, ours[3])) <= np.float32(0.1)
+    ref = run_ref(t, n_in, W2, 0.1, 0.05, 0.05, 40, 0.1)
+    check_against(ours, ref, None, what="max_simulation")
