@@ -273,8 +273,8 @@ extern "C" size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, i
 
 extern "C" int bats_weights_gradient(const void* events, const int* ev_count, long long ev_cap, const float* post_times,
                                      const void* tables, const int* nvalid, int batch, int n_post, int k_post,
-                                     int n_pre, int group, float* grad, void* workspace, size_t workspace_bytes,
-                                     cudaStream_t stream) {
+                                     int n_pre, int group, int mean, float* grad, void* workspace,
+                                     size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 1, BATS_ERR_BAD_SHAPE,
                  "weights_gradient: bad shape");
     if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
@@ -305,7 +305,7 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, lo
     BATS_CUDA(cudaGetLastError());
     const long long per = (long long)n_post * n_pre;
     const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
-    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, (float)batch, grad);
+    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, mean ? (float)batch : 1.0f, grad);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

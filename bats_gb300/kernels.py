@@ -250,9 +250,9 @@ def compute_factors(spike_times, a, c, x, exp_tau, tau):
 
 
 def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: int, per_sample: bool = True,
-                     group: int | None = None, out=None):
+                     group: int | None = None, out=None, reduce: str = "mean"):
     """Per-sample gradient (B, N_post, N_pre) like compute_weights_gradient
-    (Wrappers/Backpropagation/compute_weights_gradient.py:10-24), or its batch mean (N_post, N_pre)."""
+    (Wrappers/Backpropagation/compute_weights_gradient.py:10-24), or its batch mean / sum (N_post, N_pre)."""
     B, n_post, k_post = post_times.shape
     dev = post_times.device
     if per_sample:
@@ -266,7 +266,8 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
     ws_bytes = call_size("bats_weights_gradient_workspace_bytes", B, n_post, n_pre, g)
     ws = workspace(ws_bytes, dev) if ws_bytes else None
     call("bats_weights_gradient", ptr(events.events), ptr(events.counts), events.cap, ptr(post_times),
-         ptr(tabs.tables), ptr(tabs.nvalid), B, n_post, k_post, n_pre, g, ptr(out), ptr(ws), ws_bytes, stream_ptr())
+         ptr(tabs.tables), ptr(tabs.nvalid), B, n_post, k_post, n_pre, g, int(reduce == "mean"), ptr(out), ptr(ws),
+         ws_bytes, stream_ptr())
     return out
 
 

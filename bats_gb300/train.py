@@ -128,7 +128,7 @@ class FCTrainStep:
                            ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
             L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
                 "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(t), ptr(tb.tables),
-                ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons, max(2, self.grad_group),
+                ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons, max(2, self.grad_group), 1,
                 ptr(self.grad[li]), ws, wsb, s)))
             if li > 0:
                 pe = self.pre_err[li]

@@ -95,13 +95,14 @@ int bats_backward_prep(const float* post_times, const float* a, const float* x, 
                        cudaStream_t stream);
 
 /* Weight gradient of a fully-connected layer. group == 1: per-sample gradient (B, N_post, N_pre) like the
- * reference; group > 1: the batch mean (N_post, N_pre), accumulated per group of samples and reduced in a
- * fixed order (deterministic). Replaces compute_weights_gradient (+ the caller's mean over the batch)
+ * reference; group > 1: the batch mean (mean != 0) or sum (N_post, N_pre), accumulated per group of samples
+ * and reduced in a fixed order (deterministic). Replaces compute_weights_gradient (+ the caller's mean over the batch)
  * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24). */
 size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, int n_pre, int group);
 int bats_weights_gradient(const void* events, const int* ev_count, long long ev_cap, const float* post_times,
                           const void* tables, const int* nvalid, int batch, int n_post, int k_post, int n_pre,
-                          int group, float* grad, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+                          int group, int mean, float* grad, void* workspace, size_t workspace_bytes,
+                          cudaStream_t stream);
 
 /* Errors of the pre-synaptic spikes (B, N_pre, K_pre), zero where there is no spike. Replaces
  * propagate_errors_to_pre_spikes and its (B, N_pre, K_pre, N_post) temporary + sum

@@ -431,6 +431,27 @@ class Adam:
         return out
 
 
+def threshold_sensitivity(pre_times, weights, tau_s, theta, delta_theta, max_n_spike, max_simulation=INF,
+                          rel_count=1e-5, rel_time=1e-6):
+    """Conditioning of the forward pass, for comparing an FP32 evaluation with this float64 one.
+
+    Returns (n_lo, n_hi, t_sens): the spike-count range over thresholds theta*(1 -+ rel_count) (a count
+    outside [n_lo, n_hi] is a real disagreement; inside it, the membrane maximum lies within rel_count of
+    the threshold) and, per spike slot, |t(theta*(1+rel_time)) - t(theta*(1-rel_time))| / 2, the spike
+    time's sensitivity to a relative perturbation of the neuron state of size rel_time (inf where the
+    count changes within that range)."""
+    args = (pre_times, weights, tau_s)
+    n1 = lif_forward(*args, theta * (1 - rel_count), delta_theta, max_n_spike, max_simulation)[0]
+    n2 = lif_forward(*args, theta * (1 + rel_count), delta_theta, max_n_spike, max_simulation)[0]
+    m1 = lif_forward(*args, theta * (1 - rel_time), delta_theta, max_n_spike, max_simulation)
+    m2 = lif_forward(*args, theta * (1 + rel_time), delta_theta, max_n_spike, max_simulation)
+    same = (m1[0] == m2[0])[:, :, None]
+    with np.errstate(invalid="ignore"):
+        sens = np.where(same, np.abs(m2[3] - m1[3]) / 2, INF)
+    sens = np.where(np.isnan(sens), 0.0, sens)
+    return np.minimum(n1, n2), np.maximum(n1, n2), sens
+
+
 # --------------------------------------------------------------------------------------------
 # Independent check of the closed-form forward
 # --------------------------------------------------------------------------------------------

@@ -37,6 +37,16 @@ def grazing_mask(pre_t, W, tau_s, theta, delta_theta, K, max_sim, rel=1e-5, conv
     return np.minimum(n_lo, n_hi), np.maximum(n_lo, n_hi)
 
 
+def conditioned_reference(pre_t, W, tau_s, theta, delta_theta, K, max_sim, conv=None):
+    """float64 forward + (count bounds, time sensitivity) for an FP32-vs-FP64 comparison."""
+    Wd = W if conv is None else R.conv_dense_weights(W, conv)
+    pre = pre_t.astype(np.float64)
+    o64 = R.lif_forward(pre, np.asarray(Wd, dtype=np.float64), tau_s, theta, delta_theta, K, max_sim)
+    lo, hi, sens = R.threshold_sensitivity(pre, np.asarray(Wd, dtype=np.float64), tau_s, theta, delta_theta, K,
+                                           max_sim)
+    return o64, (lo, hi), sens
+
+
 def count_mismatches(n_gpu, n_ref, bounds=None):
     """(# differing counts, # not explained by grazing)."""
     diff = n_gpu != n_ref

@@ -12,7 +12,8 @@ import torch
 from bats_gb300 import kernels as K
 from oracle import bats_ref64 as R
 from oracle import refkern
-from tests._helpers import count_mismatches, grazing_mask, leading_mask, mnist_like_input, multi_spike_input
+from tests._helpers import (conditioned_reference, count_mismatches, grazing_mask, leading_mask, mnist_like_input,
+                            multi_spike_input)
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +38,8 @@ def run_ref(t, n_in, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
     return [v.cpu().numpy() for v in out]
 
 
-def check_against(ours, ref, bounds, max_unexplained=0, rtol=RTOL_T, what="", fields=("t", "z", "a", "x"), t_atol=0.0):
+def check_against(ours, ref, bounds, max_unexplained=0, rtol=RTOL_T, what="", fields=("t", "z", "a", "x"), t_atol=0.0,
+                  t_sens=None):
     """Counts exact up to grazing neurons; the listed fields within rtol on neurons with equal counts."""
     n, a, x, t, z = ours
     rn, ra, rx, rt, rz = ref
@@ -51,6 +53,11 @@ def check_against(ours, ref, bounds, max_unexplained=0, rtol=RTOL_T, what="", fi
         v = exp[name][same].astype(np.float64)
         e = np.abs(u - v)
         tol = rtol * np.abs(v) + (t_atol if name == "t" else 0.0)
+        if t_sens is not None and name in ("t", "z"):
+            # 20x the spike time's sensitivity to a 1e-6 relative change of the neuron state (FP32 rounding
+            # of the accumulated sums is a few 1e-7); z = exp(t/tau) inherits it through dz = z dt / tau.
+            sens = t_sens[same]
+            tol = tol + 20 * (sens if name == "t" else sens * np.abs(v) / 0.26)
         assert not (e > tol).any(), f"{what}: {name} max err {np.max(e - tol):.3e} over tolerance"
     pad = ~leading_mask(n, t.shape[2])
     assert np.isinf(t[pad]).all() and np.isinf(z[pad]).all()
@@ -58,7 +65,8 @@ def check_against(ours, ref, bounds, max_unexplained=0, rtol=RTOL_T, what="", fi
 
 
 # Against the float64 oracle, t = tau ln z turns the relative error of z into an absolute error of
-# about tau * 1e-7 per FP32 rounding, so the time tolerance there is 1e-5 relative plus 1e-5 * tau.
+# about tau * 1e-7 per FP32 rounding, so the time tolerance there is 1e-5 relative plus 1e-5 * tau, plus a
+# term proportional to the spike time's conditioning (near-tangential crossings).
 ORACLE = dict(fields=("t", "z"), t_atol=1e-5 * 0.26)
 
 
@@ -69,10 +77,9 @@ def test_small_multi_spike_vs_oracle_and_reference(cuda, seed):
     W = rng.normal(0, 1, (16, 40)).astype(np.float32)
     tau_s, theta, dth, Kp = 0.1, 0.1, 0.2, 16
     ours, _ = run_fc(t, W, tau_s, theta, dth, Kp, 0.5)
-    o64 = R.lif_forward(t.astype(np.float64), W.astype(np.float64), np.float32(tau_s), theta, dth, Kp, np.float32(0.5))
-    bounds = grazing_mask(t, W.astype(np.float64), np.float32(tau_s), theta, dth, Kp, np.float32(0.5))
+    o64, bounds, sens = conditioned_reference(t, W, np.float32(tau_s), theta, dth, Kp, np.float32(0.5))
     assert ours[0].sum() > 20, "test input should make the layer spike"
-    check_against(ours, o64, bounds, what="vs oracle", **ORACLE)
+    check_against(ours, o64, bounds, what="vs oracle", t_sens=sens, **ORACLE)
     ref = run_ref(t, n_in, W, tau_s, theta, dth, Kp, 0.5)
     d = check_against(ours, ref, bounds, rtol=1e-6, what="vs reference kernels")
     assert d == 0
@@ -93,10 +100,8 @@ def test_mnist_config_vs_reference_kernels(cuda, variant):
     ref = run_ref(t, n_in, W, 0.13, theta, theta, 30, 0.2)
     bounds = grazing_mask(t, W.astype(np.float64), np.float32(0.13), theta, theta, 30, np.float32(0.2))
     check_against(ours, ref, bounds, what=f"{variant} vs reference kernels")
-    o64 = R.lif_forward(t[:8].astype(np.float64), W.astype(np.float64), np.float32(0.13), theta, theta, 30,
-                        np.float32(0.2))
-    b8 = (bounds[0][:8], bounds[1][:8])
-    check_against([v[:8] for v in ours], o64, b8, what=f"{variant} vs oracle", **ORACLE)
+    o64, b8, sens = conditioned_reference(t[:8], W, np.float32(0.13), theta, theta, 30, np.float32(0.2))
+    check_against([v[:8] for v in ours], o64, b8, what=f"{variant} vs oracle", t_sens=sens, **ORACLE)
     if variant == "active":
         assert ours[0].sum() > 1000
     assert np.array_equal(ev.counts.cpu().numpy(), n_in.sum(1))

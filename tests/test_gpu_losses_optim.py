@@ -1,0 +1,135 @@
+"""GPU checks of the losses, Adam and the layer API (known answers of the reference tests and the
+float64 oracle), including the reference's 200-epoch LIF training known answer."""
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from bats_gb300 import Network, SpikeCountClassLoss, SpikeCountLoss, SpikeTimeLoss, TTFSSoftmaxCrossEntropy
+from bats_gb300.Layers import InputLayer, LIFLayer
+from bats_gb300.Optimizers import AdamOptimizer, GradientDescentOptimizer
+from oracle import bats_ref64 as R
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def cu(a, dtype=torch.float32):
+    return torch.tensor(np.asarray(a), device="cuda", dtype=dtype)
+
+
+def test_spike_count_class_loss(cuda):
+    rng = np.random.default_rng(0)
+    counts = rng.integers(0, 15, (100, 10))
+    labels = rng.integers(0, 10, 100)
+    targets = R.class_targets(labels, 10, 10, 2)
+    exp_loss, exp_err = R.spike_count_loss(counts, targets, 15)
+    loss_fn = SpikeCountClassLoss(target_true=10, target_false=2)
+    for dtype in (torch.int32, torch.float32):
+        loss, err = loss_fn.compute_loss_and_errors(torch.empty((100, 10, 15), device="cuda"), cu(counts, dtype),
+                                                    cu(labels, torch.int32))
+        np.testing.assert_allclose(loss.cpu().numpy(), exp_loss, rtol=1e-6)
+        np.testing.assert_allclose(err.cpu().numpy(), exp_err, rtol=1e-6)
+    np.testing.assert_allclose(loss_fn.compute_loss(None, cu(counts, torch.int32), cu(labels, torch.int32)).cpu(),
+                               exp_loss, rtol=1e-6)
+    assert torch.equal(loss_fn.predict(None, cu(counts, torch.int32)).cpu(), torch.tensor(counts).argmax(1))
+    plain = SpikeCountLoss()
+    loss, err = plain.compute_loss_and_errors(torch.empty((100, 10, 3), device="cuda"), cu(counts), cu(targets))
+    np.testing.assert_allclose(loss.cpu().numpy(), exp_loss, rtol=1e-6)
+
+
+def test_ttfs_known_answer(cuda):
+    d = np.load(os.path.join(GOLDEN, "kat_ttfs.npz"))
+    fn = TTFSSoftmaxCrossEntropy(float(d["tau"]))
+    loss, err = fn.compute_loss_and_errors(cu(d["spikes"]), None, cu(d["labels"], torch.int32))
+    np.testing.assert_allclose(loss.cpu().numpy(), d["loss"], rtol=1e-5)
+    np.testing.assert_allclose(err.cpu().numpy(), d["errors"], rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(fn.compute_loss(cu(d["spikes"]), None, cu(d["labels"], torch.int32)).cpu().numpy(),
+                               d["loss"], rtol=1e-5)
+
+
+def test_spike_time_loss(cuda):
+    rng = np.random.default_rng(3)
+    sp = rng.uniform(0, 0.5, (5, 4, 3)).astype(np.float32)
+    sp[0, 1, :] = np.inf
+    tg = rng.uniform(0, 0.5, (5, 4, 3)).astype(np.float32)
+    tg[1, 2, 0] = np.inf
+    t_dev = cu(tg)
+    loss, err = SpikeTimeLoss().compute_loss_and_errors(cu(sp), None, t_dev)
+    tg64 = tg.astype(np.float64)
+    el, ee = R.spike_time_loss(sp, tg64)
+    np.testing.assert_allclose(loss.cpu().numpy(), el, rtol=1e-5)
+    np.testing.assert_allclose(err.cpu().numpy(), ee, rtol=1e-5)
+    assert float(t_dev[1, 2, 0]) == 1.0  # targets modified in place like the reference
+
+
+def test_adam_matches_oracle_over_steps(cuda):
+    rng = np.random.default_rng(1)
+    g = [None, rng.normal(size=(5, 10)).astype(np.float32), rng.normal(size=(2, 5)).astype(np.float32)]
+    ours = AdamOptimizer(learning_rate=0.05)
+    ref = R.Adam(0.05)
+    for step in range(20):
+        d = ours.step([None if x is None else cu(x) for x in g])
+        e = ref.step(g)
+        for a, b in zip(d, e):
+            if b is None:
+                assert a is None
+                continue
+            np.testing.assert_allclose(a.cpu().numpy(), b, rtol=2e-5, atol=1e-9)
+        g = [None if x is None else (x * 0.9).astype(np.float32) for x in g]
+
+
+def test_optimizers_drive_weights_to_zero(cuda):
+    """AdamOptimizer.py / GradientDescentOptimizer.py of the reference tests: use the weights as gradients."""
+    for opt in (AdamOptimizer(learning_rate=0.05), GradientDescentOptimizer(learning_rate=0.05)):
+        torch.manual_seed(0)
+        weights = [None, torch.randn(5, 10, device="cuda"), torch.randn(2, 5, device="cuda")]
+        for _ in range(1000):
+            deltas = opt.step(weights)
+            for w, d in zip(weights, deltas):
+                if w is not None:
+                    w += d
+        for w in weights[1:]:
+            assert torch.allclose(w, torch.zeros_like(w), atol=1e-5 if isinstance(opt, AdamOptimizer) else 1e-8)
+
+
+def test_lif_training_known_answer(cuda):
+    """LIFLayer_tests.py:91-132: 200 epochs of first-spike-time MSE descent on a 7->5 layer put every first
+    spike within 5e-4 of its target."""
+    d = np.load(os.path.join(GOLDEN, "kat_lif_training.npz"))
+    inp = InputLayer(n_neurons=d["spike_per_neuron"].shape[1])
+    layer = LIFLayer(previous_layer=inp, n_neurons=int(d["n_post"]), tau_s=float(d["tau_s"]), theta=float(d["theta"]),
+                     delta_theta=float(d["delta_theta"]),
+                     weight_initializer=lambda a, b: cu(d["weights0"]), max_n_spike=int(d["max_n_spike"]))
+    inp.set_spike_trains(d["spike_per_neuron"], d["n_spike_per_neuron"])
+    targets = cu(d["targets"])
+    lr = float(d["learning_rate"])
+    for _ in range(int(d["n_epoch"])):
+        layer.reset()
+        layer.forward(float(d["max_simulation"]))
+        sp, _ = layer.spike_trains
+        err = torch.zeros_like(sp)
+        err[:, :, 0] = sp[:, :, 0] - targets
+        g, _ = layer.backward(err)
+        layer.add_deltas(-lr * g.mean(0))
+    sp, _ = layer.spike_trains
+    np.testing.assert_allclose(sp[:, :, 0].cpu().numpy(), d["targets"], atol=float(d["atol"]))
+
+
+def test_store_restore(cuda, tmp_path):
+    """LIFLayer_tests.py:134-161."""
+    inp = InputLayer(n_neurons=7)
+    w = torch.randn(5, 7, device="cuda")
+    layer = LIFLayer(previous_layer=inp, n_neurons=5, tau_s=0.01, theta=0.01, delta_theta=0.01,
+                     weight_initializer=lambda a, b: w, max_n_spike=8, name="test_layer")
+    net = Network()
+    net.add_layer(inp, input=True)
+    net.add_layer(layer)
+    net.store(Path(tmp_path))
+    layer2 = LIFLayer(previous_layer=inp, n_neurons=5, tau_s=0.01, theta=0.01, delta_theta=0.01, max_n_spike=8,
+                      name="test_layer")
+    layer2.restore(Path(tmp_path))
+    assert torch.allclose(layer2.weights, w)
+    assert os.path.exists(tmp_path / "test_layer_weights.npy")
