@@ -342,3 +342,71 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free variant of the batch-mean weight gradient.
+//
+// Some callers cannot allocate device memory on the path that calls this library: a runtime that
+// owns every device allocation up front (a fixed arena or pool it may not grow), a host whose
+// plugin interface hands the plugin only input and output buffers, or a caller in a language with
+// no CUDA allocator of its own. For them, bats_weights_gradient_mean_noalloc keeps its per-group
+// partial sums in this file-scope device array instead of a caller-provided workspace. The array is
+// part of the library image, so every GPU that loads the library holds it (32 MiB) until the process
+// exits. Every call shares it: two calls whose kernels overlap on the GPU (different streams, or
+// different host threads on one device) race on it and must be serialised by the caller. The kernel
+// writes every partial it later reads, so nothing has to be cleared between calls.
+constexpr long long NOALLOC_GRAD_SCRATCH_FLOATS = 8LL * 1024 * 1024;  // 32 MiB
+static __device__ __align__(256) float g_noalloc_grad_scratch[NOALLOC_GRAD_SCRATCH_FLOATS];
+
+#include <mutex>
+
+// Device address of the scratch array, looked up once per device (host code only sees a stand-in
+// for the symbol, so the address must come from cudaGetSymbolAddress with that device current).
+static int noalloc_scratch_ptr(float** out) {
+    static std::mutex mu;
+    static float* cache[128] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= 128) return (int)cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cache[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_grad_scratch);
+        if (e != cudaSuccess) return (int)e;
+        cache[dev] = reinterpret_cast<float*>(p);
+    }
+    *out = cache[dev];
+    return (int)cudaSuccess;
+}
+
+extern "C" long long bats_weights_gradient_noalloc_capacity(void) { return NOALLOC_GRAD_SCRATCH_FLOATS; }
+
+extern "C" int bats_weights_gradient_mean_noalloc(const void* events, const int* ev_count, long long ev_cap,
+                                                  const float* post_times, const void* tables, const int* nvalid,
+                                                  int batch, int n_post, int k_post, int n_pre, int group,
+                                                  float* grad, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 2, BATS_ERR_BAD_SHAPE,
+                 "weights_gradient_mean_noalloc: bad shape (group must be >= 2)");
+    if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
+    BATS_REQUIRE(events && ev_count && post_times && tables && nvalid && grad, BATS_ERR_NULL,
+                 "weights_gradient_mean_noalloc: null pointer");
+    const int groups = (batch + group - 1) / group;
+    const long long per = (long long)n_post * n_pre;
+    float* part = grad;
+    if (groups > 1) {
+        BATS_REQUIRE(per <= NOALLOC_GRAD_SCRATCH_FLOATS / groups, BATS_ERR_CAPACITY,
+                     "weights_gradient_mean_noalloc: ceil(batch/group) * n_post * n_pre exceeds the 8 Mi-float "
+                     "(32 MiB) static scratch; use a larger group or bats_weights_gradient with a workspace");
+        BATS_CUDA((cudaError_t)noalloc_scratch_ptr(&part));
+    }
+    dim3 grid((n_post + GRAD_TILE - 1) / GRAD_TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
+    bats::bwd_grad_kernel<GRAD_TILE, GRAD_JC><<<grid, GRAD_TILE, 0, stream>>>(
+        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
+        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, part);
+    BATS_CUDA(cudaGetLastError());
+    const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
+    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, (float)batch, grad);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}

@@ -104,6 +104,20 @@ int bats_weights_gradient(const void* events, const int* ev_count, long long ev_
                           int group, int mean, float* grad, void* workspace, size_t workspace_bytes,
                           cudaStream_t stream);
 
+/* Allocation-free batch mean of bats_weights_gradient (group >= 2), for callers that cannot allocate device
+ * memory (a runtime with a fixed arena, a plugin host that passes only input and output buffers). No
+ * counterpart in the reference. The per-group partial sums live in a 32 MiB static device array of the
+ * library (bats_weights_gradient_noalloc_capacity() floats, held on every GPU that loads the library until
+ * exit): ceil(batch/group) * n_post * n_pre must not exceed it (BATS_ERR_CAPACITY otherwise). The first call
+ * on a device looks the array's address up (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the array, so calls whose kernels overlap on the GPU race and must be serialised
+ * by the caller. */
+long long bats_weights_gradient_noalloc_capacity(void);
+int bats_weights_gradient_mean_noalloc(const void* events, const int* ev_count, long long ev_cap,
+                                       const float* post_times, const void* tables, const int* nvalid, int batch,
+                                       int n_post, int k_post, int n_pre, int group, float* grad,
+                                       cudaStream_t stream);
+
 /* Errors of the pre-synaptic spikes (B, N_pre, K_pre), zero where there is no spike. Replaces
  * propagate_errors_to_pre_spikes and its (B, N_pre, K_pre, N_post) temporary + sum
  * (bats/CudaKernels/Wrappers/Backpropagation/propagate_errors_to_pre_spikes.py:11-27). */
