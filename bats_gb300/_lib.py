@@ -25,10 +25,11 @@ SIGNATURES = {
     "bats_abi_version": (c_int, []),
     "bats_status_string": (ctypes.c_char_p, [c_int]),
     "bats_last_error": (ctypes.c_char_p, []),
+    "bats_read_device_status": (c_int, [c_vp, c_int]),
     "bats_compute_pre_exps": (c_int, [c_vp, c_ll, c_float, c_float, c_vp, c_vp, c_vp]),
     "bats_sort_events_workspace_bytes": (c_size, [c_int, c_int, c_int]),
     "bats_sort_events": (c_int, [c_vp, c_int, c_int, c_int, c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
-                                 c_size, c_vp]),
+                                 c_vp, c_int, c_vp, c_size, c_vp]),
     "bats_lif_forward_fc": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float, c_float,
                                     c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_conv_forward": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
@@ -37,8 +38,8 @@ SIGNATURES = {
     "bats_backward_prep": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                    c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_weights_gradient_workspace_bytes": (c_size, [c_int, c_int, c_int, c_int]),
-    "bats_weights_gradient": (c_int, [c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int,
-                                      c_vp, c_vp, c_size, c_vp]),
+    "bats_weights_gradient": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
+                                      c_int, c_int, c_vp, c_vp, c_size, c_vp]),
     "bats_weights_gradient_noalloc_capacity": (c_ll, []),
     "bats_weights_gradient_mean_noalloc": (c_int, [c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
                                                    c_int, c_vp, c_vp]),
@@ -97,6 +98,12 @@ def call(name: str, *args):
         msg = load().bats_last_error().decode(errors="replace")
         raise BatsError(status, f"{name} failed: {msg}")
     return status
+
+
+def check_device_status() -> None:
+    """Raise if a device-side bounded wait gave up since the last check (synchronising call)."""
+    out = ctypes.c_int(0)
+    call("bats_read_device_status", ctypes.byref(out), 1)
 
 
 def ptr(t) -> int | None:

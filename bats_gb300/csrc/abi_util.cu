@@ -1,6 +1,7 @@
 // Error reporting and per-device launch attributes shared by the C-ABI entry points.
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include "abi_util.h"
 
 namespace bats {
@@ -32,7 +33,43 @@ int max_dynamic_smem_set(const void* func, int bytes) {
     return (int)cudaSuccess;
 }
 
+// Status word of bounded device-side waits: a kernel that gives up waiting ORs BATS_STATUS_TIMEOUT
+// (1) into it and returns; bats_read_device_status reports and clears it.
+static __device__ int g_device_status;
+
+int device_status(int** out) {
+    static std::mutex mu;
+    static int* cache[128] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= 128) return (int)cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cache[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_device_status);
+        if (e != cudaSuccess) return (int)e;
+        cache[dev] = reinterpret_cast<int*>(p);
+    }
+    *out = cache[dev];
+    return (int)cudaSuccess;
+}
+
 }  // namespace bats
+
+extern "C" int bats_read_device_status(int* out, int clear) {
+    BATS_REQUIRE(out, BATS_ERR_NULL, "read_device_status: null pointer");
+    BATS_CUDA(cudaMemcpyFromSymbol(out, bats::g_device_status, sizeof(int)));
+    if (clear) {
+        const int zero = 0;
+        BATS_CUDA(cudaMemcpyToSymbol(bats::g_device_status, &zero, sizeof(int)));
+    }
+    if (*out != 0) {
+        bats::set_last_error(BATS_ERR_TIMEOUT, "read_device_status", "a device-side wait gave up (timeout)");
+        return BATS_ERR_TIMEOUT;
+    }
+    return BATS_OK;
+}
 
 extern "C" const char* bats_last_error(void) { return bats::g_last_error; }
 

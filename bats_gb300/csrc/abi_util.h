@@ -6,6 +6,10 @@
 namespace bats {
 void set_last_error(int status, const char* where, const char* what);
 int max_dynamic_smem_set(const void* func, int bytes);
+// Device address of this device's status word (bounded waits that gave up OR their flag into it).
+int device_status(int** out);
+struct SolveConst;
+SolveConst make_solve_const(float c, float dtt, float tau, float max_sim);
 }  // namespace bats
 
 #define BATS_REQUIRE(cond, status, msg)                        \

@@ -40,42 +40,79 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+// Constants of the crossing search of one layer.
+struct SolveConst {
+    float c;        // theta / tau
+    float dtt;      // delta_theta / tau
+    float tau;
+    float max_sim;
+    float e_max;    // exp(max_sim / tau), +inf when unbounded
+    bool fast;      // c > 0: the provable rejections below are valid
+};
+
+// True when the reference solver provably finds no crossing in the window (t_last, t_next] for the
+// state (a, b), so the exact evaluation can be skipped without changing any result:
+//   * a <= 0 or b < 0 (with b^2 a normal float): the reference's x = sqrt(tmp) satisfies x >= |b|
+//     (a <= 0) or x <= |b| (a > 0, b < 0), because sqrt(fl(b^2)) == |b| in binary floating point;
+//     then x + b == 0, or z = 2a/(x + b) <= 0, and the log of a non-positive z is rejected.
+//   * a > 0 and fl(b*b) < fl(4a*c): b^2 - 4ac < 0 in every evaluation order (double, float, fused).
+//   * otherwise an approximate root z_f = 2a/(b + sq), sq ~ sqrt(fl(b^2 - 4ac)), is compared with the
+//     window [exp(t_last/tau), min(exp(t_next/tau), exp(max_sim/tau))] in z = exp(t/tau) space with a
+//     relative margin m that bounds |z_f - z| for the reference's root z: with
+//     err_D = 2^-23 b^2 + 2^-24 |D_f| >= |D_f - D| (D = fl(b^2) - 4ac, a > 0, b > 0, 4ac <= fl(b^2)),
+//     |sq - sqrt(D)| <= d = min(err_D / sq, sqrt(err_D)) + 2^-21 sq, so z_f is within d / (b + sq - d) of
+//     the exact root; the reference's own rounding of x, x + b and 2a/(x + b), the approximate
+//     reciprocal and square roots used here, __expf of the window ends and __logf of the root are all
+//     below 2^-19 relative together, and m = d / (b + sq - d) + 2^-16 covers them. A root outside the
+//     widened window gives a spike time tau*ln(z) outside (t_last, min(t_next, max_sim)], which the
+//     reference rejects.
+__device__ __forceinline__ bool no_crossing(float a, float b, float e_last, float e_next, const SolveConst& k) {
+    if (!k.fast) return false;
+    const float ab = fabsf(b);
+    if (!(ab >= 0x1p-60f && ab <= 0x1p60f)) return false;
+    if (a <= 0.0f || b < 0.0f) return true;
+    if (!(a <= 0x1p60f)) return false;
+    const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), k.c);
+    const float B2 = __fmul_rn(b, b);
+    if (B2 < p_hi) return true;
+    const float Df = fmaf(b, b, -p_hi);
+    const float err_d = fmaf(0x1p-23f, B2, 0x1p-24f * fabsf(Df));
+    const float rs = Df > 0.0f ? rsqrtf(Df) : 0.0f;
+    const float sq = Df * rs;  // 0 when Df <= 0
+    const float d_sqrt = err_d * rsqrtf(err_d);
+    const float d = (Df > 0.0f ? fminf(err_d * rs, d_sqrt) : d_sqrt) + 0x1p-21f * sq;
+    const float den = b + sq;
+    if (!(den > 2.0f * d)) return false;
+    const float m = __fdividef(d, den - d) + 0x1p-16f;
+    const float zf = __fdividef(2.0f * a, den);
+    return zf > fminf(e_next, k.e_max) * (1.0f + m) || zf < e_last * (1.0f - m);
+}
+
 // Threshold-crossing solver of the current-based LIF neuron after an input event.
 //
 // The neuron state is a = sum w*exp(t_i/tau_s), b = sum w*exp(t_i/tau) - (dtheta/tau)*sum z_k,
 // c = theta/tau. The next crossing is z = 2a / (b + sqrt(b^2 - 4ac)), t = tau*ln z, accepted in
 // the window (last_t, min(next_t, max_sim)]. Each accepted spike applies the reset
 // b -= (dtheta/tau) * z and the search repeats until no crossing remains or k_post spikes
-// have been written. Returns true when the spike buffer is full.
+// have been written. Returns true when the spike buffer is full. e_last/e_next are exp(t/tau) of
+// the window ends (used only by no_crossing).
 //
-// The arithmetic of the slow path is kept operation for operation identical to the reference
-// solver (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 for the FC layer,
-// compute_spike_times_conv.cu:59-90 for the conv layer, whose discriminant is evaluated in
-// float instead of double), so that spike times agree bit for bit. The fast path in front of it
-// only returns false in cases where the reference provably returns false:
-//   * a <= 0 and b^2 a normal float: sqrt(fl(b^2)) == |b| in binary floating point, so
-//     x + b >= 0 and either x + b == 0 or 2a/(x+b) <= 0 (log(-0) = -inf is rejected too);
-//   * a > 0 and fl(b*b) < fl(4a*c): then b^2 - 4ac < 0 in every evaluation order (double,
-//     float, or either fused form), so the discriminant test fails.
+// The arithmetic after the no_crossing test is kept operation for operation identical to the
+// reference solver (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 for the FC layer,
+// compute_spike_times_conv.cu:59-90 for the conv layer, whose discriminant is evaluated in float
+// instead of double), so that spike times agree bit for bit.
 template <bool CONV>
-__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t,
-                                                float c, float dtt, float tau, float max_sim,
-                                                int& n, int k_post,
+__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_last,
+                                                float e_next, const SolveConst& k, int& n, int k_post,
                                                 float* __restrict__ a_out, float* __restrict__ x_out,
                                                 float* __restrict__ t_out, float* __restrict__ z_out) {
     while (true) {
-        const float B2 = __fmul_rn(b, b);
-        const float ab = fabsf(b);
-        if (c > 0.0f && ab >= 0x1p-60f && ab <= 0x1p60f) {
-            if (a <= 0.0f) return false;
-            const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), c);
-            if (B2 < p_hi) return false;
-        }
+        if (no_crossing(a, b, e_last, e_next, k)) return false;
         float tmp;
         if (CONV) {
-            tmp = b * b - 4 * a * c;
+            tmp = b * b - 4 * a * k.c;
         } else {
-            tmp = (float)((double)B2 - 4.0 * (double)a * (double)c);
+            tmp = (float)((double)__fmul_rn(b, b) - 4.0 * (double)a * (double)k.c);
         }
         if (tmp < 0) return false;
         const float x_tmp = sqrtf(tmp);
@@ -83,14 +120,15 @@ __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t,
         if (tmp == 0.0f) return false;
         const float inside_log = 2 * a / tmp;
         if (inside_log < 0) return false;
-        tmp = tau * __logf(inside_log);
-        if (tmp <= last_t || tmp > max_sim || tmp > next_t) return false;
+        tmp = k.tau * __logf(inside_log);
+        if (tmp <= last_t || tmp > k.max_sim || tmp > next_t) return false;
         a_out[n] = a;
         x_out[n] = x_tmp;
         t_out[n] = tmp;
         z_out[n] = inside_log;
         last_t = tmp;
-        b -= dtt * inside_log;
+        e_last = inside_log;
+        b -= k.dtt * inside_log;
         n++;
         if (n >= k_post) return true;
     }

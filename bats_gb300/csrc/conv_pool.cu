@@ -35,8 +35,8 @@ constexpr int CONV_CHUNK = 256;
 
 __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                                     const float* __restrict__ W, int X, int Y, int C, int fx, int fy, int C_out,
-                                    int Xo, int Yo, int TX, int TY, int tiles_y, int k_post, float c, float dtt,
-                                    float tau, float max_sim, int w_in_smem, int* __restrict__ n_spikes,
+                                    int Xo, int Yo, int TX, int TY, int tiles_y, int k_post, SolveConst sk,
+                                    int w_in_smem, int* __restrict__ n_spikes,
                                     float* __restrict__ a_out, float* __restrict__ x_out, float* __restrict__ t_out,
                                     float* __restrict__ z_out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -66,7 +66,7 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
     // Receptive field of the whole tile.
     const int rx0 = tx0, rx1 = min(X, tx0 + TX + fx - 1), ry0 = ty0, ry1 = min(Y, ty0 + TY + fy - 1);
 
-    float a = 0.0f, b = 0.0f, last_t = 0.0f;
+    float a = 0.0f, b = 0.0f, last_t = 0.0f, last_e = 1.0f;
     bool has_prev = false;
     int n = 0;
     bool done = !active;
@@ -110,18 +110,20 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
             const int dx = (e.xyc & 1023) - xo, dy = ((e.xyc >> 10) & 1023) - yo;
             if (dx < 0 || dx >= fx || dy < 0 || dy >= fy) continue;
             if (has_prev) {
-                done = solve_crossings<true>(a, b, last_t, e.t, c, dtt, tau, max_sim, n, k_post, ao, xo_, to, zo);
+                done = solve_crossings<true>(a, b, last_t, e.t, last_e, e.e, sk, n, k_post, ao, xo_, to, zo);
                 if (done) break;
             }
             const float w = Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)];
             a += w * e.es;
             b += w * e.e;
             last_t = e.t;
+            last_e = e.e;
             has_prev = true;
         }
     }
     if (active) {
-        if (has_prev && !done) solve_crossings<true>(a, b, last_t, BATS_INF, c, dtt, tau, max_sim, n, k_post, ao, xo_, to, zo);
+        if (has_prev && !done)
+            solve_crossings<true>(a, b, last_t, BATS_INF, last_e, BATS_INF, sk, n, k_post, ao, xo_, to, zo);
         n_spikes[(long long)s * n_post + post] = n;
         for (int k = n; k < k_post; ++k) {
             to[k] = BATS_INF;
@@ -282,7 +284,8 @@ extern "C" int bats_conv_forward(const void* events, const int* ev_count, long l
     dim3 grid(tiles_x * tiles_y, batch);
     bats::conv_forward_kernel<<<grid, threads, smem, stream>>>(
         reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, weights, X, Y, C, fx, fy, C_out, Xo, Yo, TX,
-        TY, tiles_y, k_post, c, delta_theta_tau, tau, max_simulation, w_in_smem, n_spikes, a, x, times, post_exp_tau);
+        TY, tiles_y, k_post, bats::make_solve_const(c, delta_theta_tau, tau, max_simulation), w_in_smem, n_spikes, a, x,
+        times, post_exp_tau);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -18,6 +18,7 @@
 // The suffix sums are accumulated in the reference's order (ascending k from p, fused
 // multiply-add), so SA_p equals the reference's cumul_f1 for the same pre spike bit for bit.
 #include "common.cuh"
+#include "pipeline.cuh"
 #include "abi_util.h"
 
 namespace bats {
@@ -141,6 +142,70 @@ bwd_grad_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, 
     }
 }
 
+// Weight gradient over bucketed events: blockIdx.y is a pre-neuron bucket of JC neurons and the CTA
+// reads only that bucket's events of each sample (bats_sort_events with bucket_width == JC), in time
+// order, instead of filtering the whole event list. Same ownership and write-out as bwd_grad_kernel.
+template <int TILE, int JC>
+__global__ void __launch_bounds__(TILE)
+bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__ boff, int n_buckets,
+                         long long ev_cap, const float* __restrict__ post_t, const float2* __restrict__ tab,
+                         const int* __restrict__ nvalid, int n_post, int k_post, int n_pre, int batch, int group,
+                         float* __restrict__ out) {
+    __shared__ float G[JC][TILE + 1];
+    __shared__ Event sev[BWD_CHUNK];
+    const int tid = threadIdx.x;
+    const int i = blockIdx.x * TILE + tid;
+    const bool active = i < n_post;
+    const int bucket = blockIdx.y;
+    const int J0 = bucket * JC;
+    const int g = blockIdx.z;
+    for (int q = tid; q < JC * (TILE + 1); q += TILE) (&G[0][0])[q] = 0.0f;
+
+    const int s_begin = g * group;
+    const int s_end = min(batch, s_begin + group);
+    for (int s = s_begin; s < s_end; ++s) {
+        const int* bo = boff + (long long)s * (n_buckets + 1);
+        const int beg = bo[bucket], end = bo[bucket + 1];
+        if (beg >= end) continue;
+        const long long pn = (long long)s * n_post + (active ? i : 0);
+        const int n = active ? nvalid[pn] : 0;
+        const float* tp = post_t + pn * k_post;
+        const float2* tb = tab + pn * (k_post + 1);
+        int p = 0;
+        float2 AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
+        float tn = n > 0 ? tp[0] : BATS_INF;
+        const Event* evs = ev_b + (long long)s * ev_cap;
+        for (int m0 = beg; m0 < end; m0 += BWD_CHUNK) {
+            const int cnt = min(BWD_CHUNK, end - m0);
+            __syncthreads();
+            for (int q = tid; q < cnt; q += TILE) sev[q] = evs[m0 + q];
+            __syncthreads();
+            if (n == 0) continue;
+            for (int m = 0; m < cnt; ++m) {
+                const Event e = sev[m];
+                while (tn <= e.t) {
+                    ++p;
+                    if (p < n) {
+                        AB = tb[p];
+                        tn = tp[p];
+                    } else {
+                        AB = make_float2(0.0f, 0.0f);
+                        tn = BATS_INF;
+                    }
+                }
+                if (p < n) G[e.j - J0][tid] += fmaf(e.es, AB.x, -(e.e * AB.y));
+            }
+        }
+    }
+    __syncthreads();
+    const long long obase = (long long)g * n_post * n_pre;
+    for (int q = tid; q < TILE * JC; q += TILE) {
+        const int ii = q / JC, jj = q % JC;
+        const int gi = blockIdx.x * TILE + ii, gj = J0 + jj;
+        if (gi < n_post && gj < n_pre) out[obase + (long long)gi * n_pre + gj] = G[jj][ii];
+    }
+}
+
 // Sum of per-group partial gradients in a fixed order, divided by `divisor` (1 or the batch).
 __global__ void reduce_groups_kernel(const float* __restrict__ partial, long long per_group, int groups,
                                      float divisor, float* __restrict__ out) {
@@ -152,88 +217,115 @@ __global__ void reduce_groups_kernel(const float* __restrict__ partial, long lon
     }
 }
 
-// Errors of the pre-synaptic spikes. Grid (post tiles, B). Per event, each thread forms the
-// reference's term w * (SA e_s / tau_s - SB e / tau) for its post neuron; the sum over the tile is
-// a fixed-order warp transpose-reduction (31 shuffles per 32 events) followed by a cross-warp sum.
-// Per-tile partial sums go to partial[(s, m, tile)] and are summed in tile order by
-// pre_err_scatter_kernel, which writes them to the event's (neuron, slot).
-template <int TILE>
-__global__ void __launch_bounds__(TILE)
+// Errors of the pre-synaptic spikes. Grid (post tiles, B), TILE consumer threads (one per post
+// neuron) + one producer warp. As in the forward kernel, the producer streams the sample's events and
+// their weight-row segments wt[j, tile] into shared-memory stages with bulk copies; a stage holds 32
+// events. The reference's per-(pre spike, post neuron) term is w * (SA e_s / tau_s - SB e / tau) with
+// SA, SB the suffix sums of the post neuron after the event; summed over post neurons this is
+// (sum w SA) e_s / tau_s - (sum w SB) e / tau, so each consumer only forms w*SA and w*SB for its neuron.
+// Both are summed over the warp by fixed-order transpose-reductions (31 shuffles per 32 events), then
+// over the tile's warps, into partial[(s, m, tile, 0..1)]; pre_err_scatter_kernel sums the tiles in
+// order, applies the event's factors and writes the result to the event's (neuron, slot).
+template <int TILE, int STAGES>
+__global__ void __launch_bounds__(TILE + 32)
 bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                    const float* __restrict__ wt, int ld, const float* __restrict__ post_t,
                    const float2* __restrict__ tab, const int* __restrict__ nvalid, int n_post, int k_post,
-                   float tau_s, float tau, float* __restrict__ partial, int n_tiles) {
+                   float2* __restrict__ partial, int n_tiles, int* __restrict__ status) {
+    constexpr int SEV = 32;
     constexpr int WARPS = TILE / 32;
-    __shared__ Event sev[BWD_CHUNK];
-    __shared__ float sred[WARPS][BWD_CHUNK];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    using Smem = StreamSmem<TILE, SEV, STAGES>;
+    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+    __shared__ float2 sred[2][WARPS][32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int s = blockIdx.y;
-    const int i = blockIdx.x * TILE + tid;
+    const int tile0 = blockIdx.x * TILE;
+    const int E = ev_count[s];
+    const int n_stages = (E + SEV - 1) / SEV;
+    const Event* evs = ev + (long long)s * ev_cap;
+    stream_init(sm, WARPS);
+    __syncthreads();
+    if (warp == WARPS) {
+        stream_produce(sm, evs, E, wt, ld, tile0, n_stages, lane, status);
+        return;
+    }
+    const int i = tile0 + tid;
     const bool active = i < n_post;
     const long long pn = (long long)s * n_post + (active ? i : 0);
     const int n = active ? nvalid[pn] : 0;
     const float* tp = post_t + pn * k_post;
     const float2* tb = tab + pn * (k_post + 1);
-    const float* wcol = wt + (active ? i : 0);
     int p = 0;
     float2 AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
     float tn = n > 0 ? tp[0] : BATS_INF;
-    const int E = ev_count[s];
-    const Event* evs = ev + (long long)s * ev_cap;
-    for (int m0 = 0; m0 < E; m0 += BWD_CHUNK) {
-        const int cnt = min(BWD_CHUNK, E - m0);
-        __syncthreads();
-        for (int q = tid; q < cnt; q += TILE) sev[q] = evs[m0 + q];
-        __syncthreads();
-        for (int r = 0; r < cnt; r += 32) {
-            float v[32];
+    for (int k = 0; k < n_stages; ++k) {
+        const int slot = k % STAGES;
+        if (!stream_acquire(sm, k, status)) return;
+        const int m0 = k * SEV;
+        const int cnt = min(SEV, E - m0);
+        float va[32], vb[32];
 #pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                const int mm = min(r + q, cnt - 1);
-                v[q] = __ldg(wcol + (long long)sev[mm].j * ld);
-            }
-#pragma unroll
-            for (int q = 0; q < 32; ++q) {
-                float term = 0.0f;
-                if (r + q < cnt) {
-                    const Event e = sev[r + q];
-                    while (tn <= e.t) {
-                        ++p;
-                        if (p < n) {
-                            AB = tb[p];
-                            tn = tp[p];
-                        } else {
-                            AB = make_float2(0.0f, 0.0f);
-                            tn = BATS_INF;
-                        }
+        for (int q = 0; q < 32; ++q) {
+            const float t = sm.evs[slot][q].t;
+            if (q < cnt) {
+                while (tn <= t) {
+                    ++p;
+                    if (p < n) {
+                        AB = tb[p];
+                        tn = tp[p];
+                    } else {
+                        AB = make_float2(0.0f, 0.0f);
+                        tn = BATS_INF;
                     }
-                    if (p < n) term = v[q] * (AB.x * e.es / tau_s - AB.y * e.e / tau);
                 }
-                v[q] = term;
             }
-            const float red = warp_transpose_reduce32(v);
-            sred[warp][r + lane] = red;
+            const float w = sm.rows[slot][q][tid];
+            const bool use = q < cnt && p < n;
+            va[q] = use ? w * AB.x : 0.0f;
+            vb[q] = use ? w * AB.y : 0.0f;
         }
-        __syncthreads();
-        for (int q = tid; q < cnt; q += TILE) {
-            float acc = 0.0f;
+        stream_release(sm, k);
+        const float ra = warp_transpose_reduce32(va);
+        const float rb = warp_transpose_reduce32(vb);
+        float2* dst = partial + ((long long)s * ev_cap + m0) * n_tiles + blockIdx.x;
+        if (WARPS == 1) {
+            if (lane < cnt) dst[(long long)lane * n_tiles] = make_float2(ra, rb);
+        } else {
+            sred[k & 1][warp][lane] = make_float2(ra, rb);
+            asm volatile("bar.sync 1, %0;" ::"r"(TILE) : "memory");
+            if (warp == 0 && lane < cnt) {
+                float sa = 0.0f, sb = 0.0f;
 #pragma unroll
-            for (int w = 0; w < WARPS; ++w) acc += sred[w][q];
-            partial[((long long)s * ev_cap + m0 + q) * n_tiles + blockIdx.x] = acc;
+                for (int w = 0; w < WARPS; ++w) {
+                    sa += sred[k & 1][w][lane].x;
+                    sb += sred[k & 1][w][lane].y;
+                }
+                dst[(long long)lane * n_tiles] = make_float2(sa, sb);
+            }
         }
     }
 }
 
-__global__ void pre_err_scatter_kernel(const float* __restrict__ partial, const int* __restrict__ ev_slot,
-                                       const int* __restrict__ ev_count, long long ev_cap, int n_tiles,
-                                       long long slots_per_sample, float* __restrict__ pre_err) {
+// Sums the per-tile partials of each event in tile order and writes
+// (sum w SA) * e_s / tau_s - (sum w SB) * e / tau to the event's slot.
+__global__ void pre_err_scatter_kernel(const float2* __restrict__ partial, const Event* __restrict__ ev,
+                                       const int* __restrict__ ev_slot, const int* __restrict__ ev_count,
+                                       long long ev_cap, int n_tiles, long long slots_per_sample, float tau_s,
+                                       float tau, float* __restrict__ pre_err) {
     const int s = blockIdx.y;
     const int E = ev_count[s];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < E; m += gridDim.x * blockDim.x) {
-        const float* pp = partial + ((long long)s * ev_cap + m) * n_tiles;
-        float acc = 0.0f;
-        for (int q = 0; q < n_tiles; ++q) acc += pp[q];
-        pre_err[(long long)s * slots_per_sample + ev_slot[(long long)s * ev_cap + m]] = acc;
+        const long long em = (long long)s * ev_cap + m;
+        const float2* pp = partial + em * n_tiles;
+        float sa = 0.0f, sb = 0.0f;
+        for (int q = 0; q < n_tiles; ++q) {
+            const float2 v = pp[q];
+            sa += v.x;
+            sb += v.y;
+        }
+        const Event e = ev[em];
+        pre_err[(long long)s * slots_per_sample + ev_slot[em]] = sa * e.es / tau_s - sb * e.e / tau;
     }
 }
 
@@ -243,7 +335,6 @@ __global__ void pre_err_scatter_kernel(const float* __restrict__ partial, const 
 // C-ABI
 constexpr int GRAD_TILE = 128;
 constexpr int GRAD_JC = 64;
-constexpr int PERR_TILE = 128;
 
 extern "C" int bats_backward_prep(const float* post_times, const float* a, const float* x, const float* post_exp_tau,
                                   float* errors, int batch, int n_post, int k_post, float c, float tau,
@@ -271,38 +362,51 @@ extern "C" size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, i
     return (size_t)groups * n_post * n_pre * sizeof(float);
 }
 
-extern "C" int bats_weights_gradient(const void* events, const int* ev_count, long long ev_cap, const float* post_times,
+template <int TILE>
+static void launch_grad(const void* events, const int* ev_count, const void* ev_b, const int* boff, int n_buckets,
+                        long long ev_cap, const float* post_times, const void* tables, const int* nvalid, int batch,
+                        int n_post, int k_post, int n_pre, int group, int groups, float* out, cudaStream_t stream) {
+    dim3 grid((n_post + TILE - 1) / TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
+    if (ev_b) {
+        bats::bwd_grad_bucketed_kernel<TILE, GRAD_JC><<<grid, TILE, 0, stream>>>(
+            reinterpret_cast<const bats::Event*>(ev_b), boff, n_buckets, ev_cap, post_times,
+            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out);
+    } else {
+        bats::bwd_grad_kernel<TILE, GRAD_JC><<<grid, TILE, 0, stream>>>(
+            reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
+            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out);
+    }
+}
+
+extern "C" int bats_weights_gradient(const void* events, const int* ev_count, const void* events_bucketed,
+                                     const int* bucket_offsets, long long ev_cap, const float* post_times,
                                      const void* tables, const int* nvalid, int batch, int n_post, int k_post,
                                      int n_pre, int group, int mean, float* grad, void* workspace,
                                      size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 1, BATS_ERR_BAD_SHAPE,
                  "weights_gradient: bad shape");
     if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
-    BATS_REQUIRE(events && ev_count && post_times && tables && nvalid && grad, BATS_ERR_NULL,
-                 "weights_gradient: null pointer");
-    dim3 block(GRAD_TILE);
-    if (group == 1) {
-        // Per-sample gradient (B, N_post, N_pre).
-        dim3 grid((n_post + GRAD_TILE - 1) / GRAD_TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, batch);
-        bats::bwd_grad_kernel<GRAD_TILE, GRAD_JC><<<grid, block, 0, stream>>>(
-            reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
-            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, 1, grad);
-        BATS_CUDA(cudaGetLastError());
-        return BATS_OK;
-    }
-    // Batch mean (N_post, N_pre).
-    const int groups = (batch + group - 1) / group;
+    BATS_REQUIRE(post_times && tables && nvalid && grad && ((events && ev_count) || (events_bucketed && bucket_offsets)),
+                 BATS_ERR_NULL, "weights_gradient: null pointer");
+    const int n_buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
+    const int groups = group == 1 ? batch : (batch + group - 1) / group;
     float* part = grad;
-    if (groups > 1) {
+    if (group > 1 && groups > 1) {
         BATS_REQUIRE(workspace && workspace_bytes >= bats_weights_gradient_workspace_bytes(batch, n_post, n_pre, group),
                      BATS_ERR_WORKSPACE, "weights_gradient: workspace too small");
         part = reinterpret_cast<float*>(workspace);
     }
-    dim3 grid((n_post + GRAD_TILE - 1) / GRAD_TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
-    bats::bwd_grad_kernel<GRAD_TILE, GRAD_JC><<<grid, block, 0, stream>>>(
-        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
-        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, part);
+    if (n_post <= 32)
+        launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables, nvalid,
+                        batch, n_post, k_post, n_pre, group, groups, part, stream);
+    else if (n_post <= 64)
+        launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables, nvalid,
+                        batch, n_post, k_post, n_pre, group, groups, part, stream);
+    else
+        launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables,
+                         nvalid, batch, n_post, k_post, n_pre, group, groups, part, stream);
     BATS_CUDA(cudaGetLastError());
+    if (group == 1) return BATS_OK;  // per-sample gradient (B, N_post, N_pre)
     const long long per = (long long)n_post * n_pre;
     const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
     bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, mean ? (float)batch : 1.0f, grad);
@@ -311,8 +415,25 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, lo
 }
 
 extern "C" size_t bats_pre_errors_workspace_bytes(int batch, long long ev_cap, int n_post) {
-    const long long tiles = (n_post + PERR_TILE - 1) / PERR_TILE;
-    return (size_t)batch * ev_cap * tiles * sizeof(float);
+    const int tile = n_post <= 32 ? 32 : (n_post <= 64 ? 64 : 128);
+    const long long tiles = (n_post + tile - 1) / tile;
+    return (size_t)batch * ev_cap * tiles * 2 * sizeof(float);
+}
+
+template <int TILE>
+static int launch_pre_err(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld,
+                          const float* post_times, const void* tables, const int* nvalid, int batch, int n_post,
+                          int k_post, float2* part, int* status, cudaStream_t stream) {
+    constexpr int STAGES = 4;
+    const int tiles = (n_post + TILE - 1) / TILE;
+    const size_t smem = sizeof(bats::StreamSmem<TILE, 32, STAGES>);
+    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_kernel<TILE, STAGES>, (int)smem));
+    dim3 grid(tiles, batch);
+    bats::bwd_pre_err_kernel<TILE, STAGES><<<grid, TILE + 32, smem, stream>>>(
+        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, wt, ld, post_times,
+        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, part, tiles, status);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
 }
 
 extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int* ev_count, long long ev_cap,
@@ -320,7 +441,7 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
                                const int* nvalid, int batch, int n_post, int k_post, int n_pre, int k_pre,
                                float tau_s, float tau, float* pre_errors, void* workspace, size_t workspace_bytes,
                                cudaStream_t stream) {
-    BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && k_pre > 0 && ld >= n_post,
+    BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && k_pre > 0 && ld >= n_post && ld % 4 == 0,
                  BATS_ERR_BAD_SHAPE, "pre_errors: bad shape");
     if (batch == 0 || n_pre == 0) return BATS_OK;
     BATS_REQUIRE(events && ev_slot && ev_count && pre_errors, BATS_ERR_NULL, "pre_errors: null pointer");
@@ -328,17 +449,32 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
     BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)batch * slots * sizeof(float), stream));
     if (n_post == 0) return BATS_OK;
     BATS_REQUIRE(weights_t && post_times && tables && nvalid, BATS_ERR_NULL, "pre_errors: null pointer");
+    BATS_REQUIRE(((uintptr_t)weights_t & 15) == 0 && ((uintptr_t)events & 15) == 0, BATS_ERR_BAD_SHAPE,
+                 "pre_errors: weights_t and events must be 16-byte aligned");
     BATS_REQUIRE(workspace && workspace_bytes >= bats_pre_errors_workspace_bytes(batch, ev_cap, n_post),
                  BATS_ERR_WORKSPACE, "pre_errors: workspace too small");
-    const int tiles = (n_post + PERR_TILE - 1) / PERR_TILE;
-    float* part = reinterpret_cast<float*>(workspace);
-    dim3 grid(tiles, batch);
-    bats::bwd_pre_err_kernel<PERR_TILE><<<grid, PERR_TILE, 0, stream>>>(
-        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, weights_t, ld, post_times,
-        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, tau_s, tau, part, tiles);
-    BATS_CUDA(cudaGetLastError());
+    float2* part = reinterpret_cast<float2*>(workspace);
+    int* status = nullptr;
+    BATS_CUDA((cudaError_t)bats::device_status(&status));
+    int rc;
+    int tiles;
+    if (n_post <= 32) {
+        rc = launch_pre_err<32>(events, ev_count, ev_cap, weights_t, ld, post_times, tables, nvalid, batch, n_post,
+                                k_post, part, status, stream);
+        tiles = (n_post + 31) / 32;
+    } else if (n_post <= 64) {
+        rc = launch_pre_err<64>(events, ev_count, ev_cap, weights_t, ld, post_times, tables, nvalid, batch, n_post,
+                                k_post, part, status, stream);
+        tiles = (n_post + 63) / 64;
+    } else {
+        rc = launch_pre_err<128>(events, ev_count, ev_cap, weights_t, ld, post_times, tables, nvalid, batch, n_post,
+                                 k_post, part, status, stream);
+        tiles = (n_post + 127) / 128;
+    }
+    if (rc != BATS_OK) return rc;
     dim3 g2((unsigned)std::min<long long>((ev_cap + 255) / 256, 64), batch);
-    bats::pre_err_scatter_kernel<<<g2, 256, 0, stream>>>(part, ev_slot, ev_count, ev_cap, tiles, slots, pre_errors);
+    bats::pre_err_scatter_kernel<<<g2, 256, 0, stream>>>(part, reinterpret_cast<const bats::Event*>(events), ev_slot,
+                                                          ev_count, ev_cap, tiles, slots, tau_s, tau, pre_errors);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -1,0 +1,145 @@
+// mbarrier + bulk-copy (TMA engine, non-tensor form) helpers in inline PTX for sm_90+/sm_103a.
+//
+// Every wait is bounded: after BATS_WAIT_LIMIT polls it gives up, raises the CTA abort flag and the
+// global status word, and returns false, so a lost copy or a missing arrival never hangs the GPU.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bats {
+
+constexpr long long BATS_WAIT_LIMIT = 1LL << 24;  // polls; each try_wait may also suspend briefly
+constexpr int BATS_STATUS_TIMEOUT = 1;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on one phase of an mbarrier. `abort` is a CTA-shared flag raised by any thread that
+// gives up; `status` (may be null) receives BATS_STATUS_TIMEOUT.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int* status) {
+    for (long long it = 0; it < BATS_WAIT_LIMIT; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255) == 255 && *abort) return false;
+    }
+    *abort = 1;
+    if (status) atomicOr(status, BATS_STATUS_TIMEOUT);
+    return false;
+}
+
+// Bulk copy global -> shared, completing `bytes` transactions on `bar`. src/dst 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+}  // namespace bats
+
+// ---------------------------------------------------------------------------------------------
+// Event stream: a producer warp copies, stage by stage, SEV time-sorted event records (plus the next
+// one, for the window end) and their weight-row segments wt[j, tile0 : tile0 + TILE] into a ring of
+// STAGES shared-memory stages; consumer warps acquire a stage (full barrier), read it, and release it
+// (empty barrier, one arrival per consumer warp). Used by the forward and error-propagation kernels.
+#include "common.cuh"
+
+namespace bats {
+
+template <int TILE, int SEV, int STAGES>
+struct StreamSmem {
+    float rows[STAGES][SEV][TILE];
+    Event evs[STAGES][SEV + 1];
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+    int abort;
+};
+
+template <int TILE, int SEV, int STAGES>
+__device__ __forceinline__ void stream_init(StreamSmem<TILE, SEV, STAGES>& sm, int consumer_warps) {
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < STAGES; ++q) {
+            mbar_init(&sm.full[q], 1);
+            mbar_init(&sm.empty[q], consumer_warps);
+        }
+        sm.abort = 0;
+        fence_barrier_init();
+    }
+}
+
+// Producer warp body. Never returns with copies in flight into shared memory.
+template <int TILE, int SEV, int STAGES>
+__device__ __forceinline__ void stream_produce(StreamSmem<TILE, SEV, STAGES>& sm, const Event* __restrict__ evs, int E,
+                                               const float* __restrict__ wt, int ld, int tile0, int n_stages,
+                                               int lane, int* status) {
+    const uint32_t row_bytes = (uint32_t)min(TILE, ld - tile0) * 4u;
+    int issued = 0;
+    for (int k = 0; k < n_stages; ++k) {
+        const int slot = k % STAGES;
+        const bool ok = mbar_wait(&sm.empty[slot], ((k / STAGES) & 1) ^ 1, &sm.abort, status);
+        if (!__all_sync(0xffffffffu, ok)) break;
+        const int m0 = k * SEV;
+        const int cnt = min(SEV, E - m0);
+        const int cnt_ev = min(SEV + 1, E - m0);
+        if (lane == 0) mbar_arrive_expect_tx(&sm.full[slot], (uint32_t)cnt_ev * 16u + (uint32_t)cnt * row_bytes);
+        __syncwarp();
+        if (lane == 0) bulk_copy_g2s(&sm.evs[slot][0], evs + m0, (uint32_t)cnt_ev * 16u, &sm.full[slot]);
+        for (int u = lane; u < cnt; u += 32) {
+            const int j = __ldg(&evs[m0 + u].j);
+            bulk_copy_g2s(&sm.rows[slot][u][0], wt + (long long)j * ld + tile0, row_bytes, &sm.full[slot]);
+        }
+        issued = k + 1;
+    }
+    if (sm.abort) {
+        for (int k = max(0, issued - STAGES); k < issued; ++k) {
+            volatile int dummy = 0;
+            mbar_wait(&sm.full[k % STAGES], (k / STAGES) & 1, &dummy, nullptr);
+        }
+    }
+}
+
+// Consumer side: wait for stage k (all lanes of the warp agree on the outcome).
+template <int TILE, int SEV, int STAGES>
+__device__ __forceinline__ bool stream_acquire(StreamSmem<TILE, SEV, STAGES>& sm, int k, int* status) {
+    const bool ok = mbar_wait(&sm.full[k % STAGES], (k / STAGES) & 1, &sm.abort, status);
+    return __all_sync(0xffffffffu, ok);
+}
+
+template <int TILE, int SEV, int STAGES>
+__device__ __forceinline__ void stream_release(StreamSmem<TILE, SEV, STAGES>& sm, int k) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&sm.empty[k % STAGES]);
+}
+
+}  // namespace bats

@@ -8,6 +8,10 @@
 // compacted and sorted by a stable LSD radix sort in shared memory (8-bit digits, warp ranks
 // from __match_any_sync ballots), so the event list needs no host sync and no padding to the
 // batch maximum. Ties keep slot order, which makes the order deterministic.
+//
+// For the backward pass the same kernel can also emit the events grouped by pre-neuron bucket
+// (neuron / bucket_width), each bucket still in time order (one more stable counting pass), with
+// the per-sample bucket offsets: the weight-gradient kernel then reads only its bucket's events.
 #include "common.cuh"
 
 namespace bats {
@@ -15,6 +19,7 @@ namespace bats {
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
 constexpr int SORT_SMEM_ITEMS = 4096;  // items sorted fully in shared memory
+constexpr int SORT_MAX_BUCKETS = 255;
 
 struct SortShared {
     int hist[256];
@@ -22,7 +27,6 @@ struct SortShared {
     int wcnt[SORT_WARPS][256];
     int wofs[SORT_WARPS][256];
     int warp_tot[SORT_WARPS];
-    int total;
 };
 
 __device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh, int& block_total) {
@@ -43,17 +47,105 @@ __device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh,
     return off + in_warp;
 }
 
+// Exclusive scan of sh.hist (256 bins, one per thread) into sh.base; clears sh.wcnt.
+__device__ __forceinline__ void scan_bins(SortShared& sh) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int v = sh.hist[tid];
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) sh.warp_tot[warp] = incl;
+    __syncthreads();
+    int woff = 0;
+    for (int w = 0; w < warp; ++w) woff += sh.warp_tot[w];
+    sh.base[tid] = woff + incl - v;
+#pragma unroll
+    for (int w = 0; w < SORT_WARPS; ++w) sh.wcnt[w][tid] = 0;
+    __syncthreads();
+}
+
+// One stable counting pass (digit < 256) of n (key, val) pairs from (ka, va) into (kb, vb), using the
+// bin bases already in sh.base. Items are ranked in rounds of SORT_THREADS in their current order;
+// inside a warp, items of equal digit are ranked by __match_any_sync, across warps by a per-digit scan.
+template <typename DigitFn>
+__device__ __forceinline__ void stable_pass(const uint32_t* ka, const uint32_t* va, uint32_t* kb, uint32_t* vb, int n,
+                                            SortShared& sh, DigitFn digit) {
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int r0 = 0; r0 < n; r0 += SORT_THREADS) {
+        const int i = r0 + tid;
+        const bool valid = i < n;
+        uint32_t key = 0, val = 0;
+        int d = 256;
+        if (valid) {
+            key = ka[i];
+            val = va[i];
+            d = digit(key, val);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & lanemask_lt());
+        if (valid && rank == 0) sh.wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            int off = sh.base[tid];
+#pragma unroll
+            for (int w = 0; w < SORT_WARPS; ++w) {
+                sh.wofs[w][tid] = off;
+                off += sh.wcnt[w][tid];
+                sh.wcnt[w][tid] = 0;
+            }
+            sh.base[tid] = off;
+        }
+        __syncthreads();
+        if (valid) {
+            const int pos = sh.wofs[warp][d] + rank;
+            kb[pos] = key;
+            vb[pos] = val;
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ Event make_event(uint32_t key, uint32_t slot, int k_pre, long long sample_off,
+                                            const float* exp_s_in, const float* exp_in, float tau_s, float tau) {
+    Event e;
+    e.t = key_to_float(key);
+    e.j = (int)slot / k_pre;
+    if (exp_s_in) {
+        e.es = exp_s_in[sample_off + slot];
+        e.e = exp_in[sample_off + slot];
+    } else {
+        e.es = __expf(e.t / tau_s);
+        e.e = __expf(e.t / tau);
+    }
+    return e;
+}
+
+struct TimeDigit {
+    int shift;
+    __device__ int operator()(uint32_t key, uint32_t) const { return (int)((key >> shift) & 255u); }
+};
+struct BucketDigit {
+    int div;
+    __device__ int operator()(uint32_t, uint32_t slot) const { return (int)slot / div; }
+};
+
 __global__ void __launch_bounds__(SORT_THREADS)
 sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, float tau_s, float tau,
-                   const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out, int* __restrict__ slot_out, int* __restrict__ ev_count,
-                   long long cap, uint32_t* __restrict__ scratch) {
+                   const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out,
+                   int* __restrict__ slot_out, int* __restrict__ ev_count, Event* __restrict__ ev_bucketed,
+                   int* __restrict__ bucket_off, int bucket_width, int n_buckets, long long cap,
+                   uint32_t* __restrict__ scratch) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortShared& sh = *reinterpret_cast<SortShared*>(smem_raw);
     uint32_t* smem_items = reinterpret_cast<uint32_t*>(smem_raw + sizeof(SortShared));
 
     const int s = blockIdx.x;
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const float* tsrc = times + (long long)s * n_slots;
+    const int tid = threadIdx.x;
+    const long long sample_off = (long long)s * n_slots;
+    const float* tsrc = times + sample_off;
 
     // Count valid slots first so that the buffers can be chosen.
     int n = 0;
@@ -95,65 +187,15 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     }
     __syncthreads();
 
-    // LSD radix sort, 4 passes of 8 bits; passes whose digit is uniform are skipped.
+    // LSD radix sort on the time key, 4 passes of 8 bits; passes whose digit is uniform are skipped.
     for (int shift = 0; shift < 32; shift += 8) {
         sh.hist[tid] = 0;
         __syncthreads();
         for (int i = tid; i < n; i += SORT_THREADS) atomicAdd(&sh.hist[(ka[i] >> shift) & 255u], 1);
         __syncthreads();
-        const bool uniform = __syncthreads_or(sh.hist[tid] == n);
-        if (uniform) continue;
-        // Exclusive scan of the 256 bins (one bin per thread).
-        {
-            const int lane = tid & 31;
-            int v = sh.hist[tid];
-            int incl = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            if (lane == 31) sh.warp_tot[warp] = incl;
-            __syncthreads();
-            int woff = 0;
-            for (int w = 0; w < warp; ++w) woff += sh.warp_tot[w];
-            sh.base[tid] = woff + incl - v;
-#pragma unroll
-            for (int w = 0; w < SORT_WARPS; ++w) sh.wcnt[w][tid] = 0;
-            __syncthreads();
-        }
-        for (int r0 = 0; r0 < n; r0 += SORT_THREADS) {
-            const int i = r0 + tid;
-            const bool valid = i < n;
-            uint32_t key = 0, val = 0;
-            int d = 256;
-            if (valid) {
-                key = ka[i];
-                val = va[i];
-                d = (key >> shift) & 255u;
-            }
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            const int rank = __popc(peers & lanemask_lt());
-            if (valid && rank == 0) sh.wcnt[warp][d] = __popc(peers);
-            __syncthreads();
-            {
-                int off = sh.base[tid];
-#pragma unroll
-                for (int w = 0; w < SORT_WARPS; ++w) {
-                    sh.wofs[w][tid] = off;
-                    off += sh.wcnt[w][tid];
-                    sh.wcnt[w][tid] = 0;
-                }
-                sh.base[tid] = off;
-            }
-            __syncthreads();
-            if (valid) {
-                const int pos = sh.wofs[warp][d] + rank;
-                kb[pos] = key;
-                vb[pos] = val;
-            }
-        }
-        __syncthreads();
+        if (__syncthreads_or(sh.hist[tid] == n)) continue;
+        scan_bins(sh);
+        stable_pass(ka, va, kb, vb, n, sh, TimeDigit{shift});
         uint32_t* t0 = ka; ka = kb; kb = t0;
         t0 = va; va = vb; vb = t0;
     }
@@ -161,22 +203,28 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     Event* eo = ev_out + (long long)s * cap;
     int* so = slot_out ? slot_out + (long long)s * cap : nullptr;
     for (int m = tid; m < n; m += SORT_THREADS) {
-        const float t = key_to_float(ka[m]);
-        const int slot = (int)va[m];
-        Event e;
-        e.t = t;
-        e.j = slot / k_pre;
-        if (exp_s_in) {
-            e.es = exp_s_in[(long long)s * n_slots + slot];
-            e.e = exp_in[(long long)s * n_slots + slot];
-        } else {
-            e.es = __expf(t / tau_s);
-            e.e = __expf(t / tau);
-        }
-        eo[m] = e;
-        if (so) so[m] = slot;
+        eo[m] = make_event(ka[m], va[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
+        if (so) so[m] = (int)va[m];
     }
     if (tid == 0) ev_count[s] = n;
+
+    if (ev_bucketed) {
+        // Stable counting pass by pre-neuron bucket over the time-sorted items.
+        const int div = k_pre * bucket_width;
+        sh.hist[tid] = 0;
+        __syncthreads();
+        for (int i = tid; i < n; i += SORT_THREADS) atomicAdd(&sh.hist[(int)va[i] / div], 1);
+        __syncthreads();
+        scan_bins(sh);
+        int* bo = bucket_off + (long long)s * (n_buckets + 1);
+        if (tid < n_buckets) bo[tid] = sh.base[tid];
+        if (tid == 0) bo[n_buckets] = n;
+        __syncthreads();
+        stable_pass(ka, va, kb, vb, n, sh, BucketDigit{div});
+        Event* be = ev_bucketed + (long long)s * cap;
+        for (int m = tid; m < n; m += SORT_THREADS)
+            be[m] = make_event(kb[m], vb[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
+    }
 }
 
 }  // namespace bats
@@ -192,21 +240,30 @@ extern "C" size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_p
 }
 
 extern "C" int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, float tau_s,
-                                float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out, int* slot_out, int* ev_count, void* workspace,
-                                size_t workspace_bytes, cudaStream_t stream) {
+                                float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out, int* slot_out,
+                                int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
+                                void* workspace, size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_pre >= 0 && k_pre > 0, BATS_ERR_BAD_SHAPE, "sort_events: bad shape");
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(pre_times && ev_out && ev_count, BATS_ERR_NULL, "sort_events: null pointer");
     BATS_REQUIRE((exp_tau_s == nullptr) == (exp_tau == nullptr), BATS_ERR_NULL, "sort_events: give both exps or none");
     const long long cap = (long long)n_pre * k_pre;
     BATS_REQUIRE(cap < (1LL << 30), BATS_ERR_CAPACITY, "sort_events: n_pre*k_pre too large");
+    int n_buckets = 0;
+    if (ev_bucketed) {
+        BATS_REQUIRE(bucket_offsets && bucket_width > 0, BATS_ERR_NULL, "sort_events: bucket outputs");
+        n_buckets = (n_pre + bucket_width - 1) / bucket_width;
+        BATS_REQUIRE(n_buckets <= bats::SORT_MAX_BUCKETS, BATS_ERR_CAPACITY,
+                     "sort_events: more than 255 pre-neuron buckets (n_pre > 255 * bucket_width)");
+    }
     const size_t need = bats_sort_events_workspace_bytes(batch, n_pre, k_pre);
     BATS_REQUIRE(workspace_bytes >= need && (need == 0 || workspace), BATS_ERR_WORKSPACE,
                  "sort_events: workspace too small");
     const size_t smem = sizeof(bats::SortShared) + 4 * bats::SORT_SMEM_ITEMS * sizeof(uint32_t);
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel, (int)smem));
     bats::sort_events_kernel<<<batch, bats::SORT_THREADS, smem, stream>>>(
-        pre_times, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out, ev_count, cap,
+        pre_times, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out,
+        ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets, cap,
         reinterpret_cast<uint32_t*>(workspace));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;

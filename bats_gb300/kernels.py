@@ -53,15 +53,22 @@ def transpose_weights(weights, out=None):
     return out
 
 
+BUCKET_WIDTH = 64  # pre neurons per bucket of the weight-gradient kernel
+
+
 @dataclass
 class Events:
     """Time-sorted pre-synaptic spikes of a batch: events (B, cap, 4) 16-byte records, the source slot
-    of each event (B, cap), and the number of events per sample (B)."""
+    of each event (B, cap), and the number of events per sample (B); for the backward pass also the
+    same events grouped in buckets of BUCKET_WIDTH pre neurons (time order kept inside a bucket) with
+    the bucket offsets (B, n_buckets + 1)."""
     events: torch.Tensor
     slots: torch.Tensor
     counts: torch.Tensor
     n_neurons: int
     k: int
+    bucketed: torch.Tensor | None = None
+    bucket_offsets: torch.Tensor | None = None
 
     @property
     def cap(self) -> int:
@@ -72,26 +79,34 @@ class Events:
         return self.events.shape[0]
 
 
-def alloc_events(batch: int, n_neurons: int, k: int, device="cuda") -> Events:
+def alloc_events(batch: int, n_neurons: int, k: int, device="cuda", bucketed: bool = True) -> Events:
     cap = n_neurons * k
-    return Events(torch.empty((batch, cap, 4), dtype=F32, device=device),
-                  torch.empty((batch, cap), dtype=I32, device=device),
-                  torch.empty((batch,), dtype=I32, device=device), n_neurons, k)
+    ev = Events(torch.empty((batch, cap, 4), dtype=F32, device=device),
+                torch.empty((batch, cap), dtype=I32, device=device),
+                torch.empty((batch,), dtype=I32, device=device), n_neurons, k)
+    n_buckets = (n_neurons + BUCKET_WIDTH - 1) // BUCKET_WIDTH
+    if bucketed and n_buckets <= 255:
+        ev.bucketed = torch.empty((batch, cap, 4), dtype=F32, device=device)
+        ev.bucket_offsets = torch.empty((batch, n_buckets + 1), dtype=I32, device=device)
+    return ev
 
 
-def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=None, out: Events | None = None):
+def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=None, out: Events | None = None,
+                bucketed: bool = True):
     """Per-sample time sort of all valid pre-spikes (replaces get_sorted_spikes_indices, the
-    take_along_axis gathers and compute_pre_exps; bats/Layers/LIFLayer.py:66-84)."""
+    take_along_axis gathers and compute_pre_exps; bats/Layers/LIFLayer.py:66-84). With `bucketed`, also
+    the bucketed copy used by the weight gradient."""
     t = _c(spike_times)
     B, N, K = t.shape
     if out is None:
-        out = alloc_events(B, N, K, t.device)
+        out = alloc_events(B, N, K, t.device, bucketed=bucketed)
     ws_bytes = call_size("bats_sort_events_workspace_bytes", B, N, K)
     ws = workspace(ws_bytes, t.device) if ws_bytes else None
     es = _c(exp_tau_s) if exp_tau_s is not None else None
     ee = _c(exp_tau) if exp_tau is not None else None
     call("bats_sort_events", ptr(t), B, N, K, float(tau_s), float(tau), ptr(es), ptr(ee), ptr(out.events),
-         ptr(out.slots), ptr(out.counts), ptr(ws), ws_bytes, stream_ptr())
+         ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets), BUCKET_WIDTH, ptr(ws),
+         ws_bytes, stream_ptr())
     return out
 
 
@@ -115,7 +130,7 @@ def get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron):
     of the batch (one host read) and sorted_indices pointing at inf slots past a sample's spikes."""
     t = _c(spike_times_per_neuron)
     B, N, K = t.shape
-    ev = sort_events(t, 1.0, 1.0)
+    ev = sort_events(t, 1.0, 1.0, bucketed=False)
     S = int(ev.counts.max().item()) if B > 0 else 0
     reshaped = t.reshape(B, N * K)
     idx = ev.slots[:, :S].to(torch.int64)
@@ -259,16 +274,29 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
         g = 1
         shape = (B, n_post, n_pre)
     else:
-        g = max(2, int(group or 16))  # group >= 2 selects the batch-mean path
+        g = max(2, int(group or default_group(B, n_post, n_pre)))  # group >= 2 selects the batch-reduced path
         shape = (n_post, n_pre)
     if out is None:
         out = torch.empty(shape, dtype=F32, device=dev)
     ws_bytes = call_size("bats_weights_gradient_workspace_bytes", B, n_post, n_pre, g)
     ws = workspace(ws_bytes, dev) if ws_bytes else None
-    call("bats_weights_gradient", ptr(events.events), ptr(events.counts), events.cap, ptr(post_times),
-         ptr(tabs.tables), ptr(tabs.nvalid), B, n_post, k_post, n_pre, g, int(reduce == "mean"), ptr(out), ptr(ws),
-         ws_bytes, stream_ptr())
+    call("bats_weights_gradient", ptr(events.events), ptr(events.counts), ptr(events.bucketed),
+         ptr(events.bucket_offsets), events.cap, ptr(post_times), ptr(tabs.tables), ptr(tabs.nvalid), B, n_post,
+         k_post, n_pre, g, int(reduce == "mean"), ptr(out), ptr(ws), ws_bytes, stream_ptr())
     return out
+
+
+def grad_tile(n_post: int) -> int:
+    return 32 if n_post <= 32 else (64 if n_post <= 64 else 128)
+
+
+def default_group(batch: int, n_post: int, n_pre: int, target_ctas: int = 1216) -> int:
+    """Samples per group of the batch-reduced weight gradient: enough groups for ~8 CTAs per SM of a
+    152-SM GB300, but at most 32 partial gradients."""
+    tiles = (n_post + grad_tile(n_post) - 1) // grad_tile(n_post)
+    buckets = (n_pre + BUCKET_WIDTH - 1) // BUCKET_WIDTH
+    groups = max(1, min(batch, -(-target_ctas // (tiles * buckets)), 32))
+    return max(1, -(-batch // groups))
 
 
 def pre_errors(events: Events, weights_t, post_times, tabs: BackwardTables, tau_s: float, tau: float, out=None):

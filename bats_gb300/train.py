@@ -32,7 +32,7 @@ class FCTrainStep:
     def __init__(self, batch: int, n_inputs: int, k_input: int, layers: Sequence[FCLayerSpec],
                  weights: Sequence[torch.Tensor], target_true: float, target_false: float,
                  learning_rate: float = 3e-3, beta_1: float = 0.9, beta_2: float = 0.999, epsilon: float = 1e-8,
-                 max_simulation: float = np.inf, grad_group: int = 16, device="cuda"):
+                 max_simulation: float = np.inf, grad_group: int = 0, device="cuda"):
         self.B = int(batch)
         self.dev = torch.device(device)
         self.specs = list(layers)
@@ -69,13 +69,15 @@ class FCTrainStep:
             n_prev, k_prev = N, Kp
         self.loss = torch.empty((B,), dtype=f32, device=dev)
         self.errors = torch.empty((B, n_prev, k_prev), dtype=f32, device=dev)
-        # Scratch sized for the largest user.
+        # Samples per gradient group (>= 2 selects the batch-mean path) and scratch for the largest user.
+        self.groups = []
         ws = 0
         n_prev, k_prev = n_inputs, k_input
         for spec in self.specs:
+            grp = max(2, self.grad_group or K.default_group(B, spec.n_neurons, n_prev))
+            self.groups.append(grp)
             ws = max(ws, K.call_size("bats_sort_events_workspace_bytes", B, n_prev, k_prev),
-                     K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev,
-                                 max(2, self.grad_group)),
+                     K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev, grp),
                      K.call_size("bats_pre_errors_workspace_bytes", B, n_prev * k_prev, spec.n_neurons))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
         self.ws = torch.empty(max(ws, 256), dtype=torch.uint8, device=dev)
@@ -103,7 +105,8 @@ class FCTrainStep:
             tag = f"L{li + 1}"
             L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), ev=ev, spec=spec, tau32=tau32: call(
                 "bats_sort_events", pt, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32), None,
-                None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ws, wsb, s)))
+                None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
+                K.BUCKET_WIDTH, ws, wsb, s)))
             n, a, x, t, z = self.out[li]
             L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
                       call("bats_lif_forward_fc", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
@@ -126,10 +129,11 @@ class FCTrainStep:
                       call("bats_backward_prep", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]), ptr(e), B,
                            spec.n_neurons, spec.max_n_spike, float(c), float(tau32), float(dtt), 1, 1, ptr(tb.f1),
                            ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
-            L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
-                "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(t), ptr(tb.tables),
-                ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons, max(2, self.grad_group), 1,
-                ptr(self.grad[li]), ws, wsb, s)))
+            grp = self.groups[li]
+            L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, grp=grp: call(
+                "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
+                ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,
+                grp, 1, ptr(self.grad[li]), ws, wsb, s)))
             if li > 0:
                 pe = self.pre_err[li]
                 L.append((f"{tag}.pre_err", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, pe=pe, tau32=tau32: call(

@@ -10,8 +10,8 @@
  *     failure of the calling thread. Launches are asynchronous on `stream`.
  *   - Spike trains are (B, N, K) float32 row-major, +inf after the neuron's spikes, with counts
  *     (B, N) int32. Weights of a fully-connected layer are (N_post, N_pre); the forward and
- *     error-propagation kernels read the transposed copy wt (N_pre, ld), ld >= N_post and
- *     ld % 4 == 0 (bats_transpose builds it). Conv filters are (C_out, fx, fy, C_in).
+ *     error-propagation kernels read the transposed copy wt (N_pre, ld), ld >= N_post,
+ *     ld % 4 == 0 and wt 16-byte aligned (bats_transpose builds it). Conv filters are (C_out, fx, fy, C_in).
  *   - `events` is an array of 16-byte records {float t; int j; float exp(t/tau_s); float exp(t/tau)}
  *     of shape (B, ev_cap), ev_cap = N_pre * K_pre, filled by bats_sort_events.
  *
@@ -40,6 +40,11 @@ extern "C" {
 #define BATS_ERR_TIMEOUT 6
 
 int bats_abi_version(void);
+
+/* Device-side waits (the mbarrier pipelines of the forward kernels) are bounded: a wait that gives up
+ * sets this device's status word and the kernel returns early. Reads it into *out (synchronous), clears
+ * it if `clear`, and returns BATS_ERR_TIMEOUT when it was set. */
+int bats_read_device_status(int* out, int clear);
 const char* bats_status_string(int status);
 const char* bats_last_error(void);
 
@@ -53,12 +58,16 @@ int bats_compute_pre_exps(const float* times, long long count, float tau_s, floa
 /* Per-sample time sort of the valid (time < +inf) pre-synaptic spike slots into `events`
  * (B, N_pre*K_pre) plus the slot index n*K_pre+k of each event (slot_out, may be NULL) and the
  * per-sample count. The events' exponentials are __expf(t/tau_s), __expf(t/tau), or gathered from
- * exp_tau_s / exp_tau (B, N_pre, K_pre) when those are given. Replaces get_sorted_spikes_indices + take_along_axis + compute_pre_exps
+ * exp_tau_s / exp_tau (B, N_pre, K_pre) when those are given. When events_bucketed is given, the same
+ * events are also written grouped by pre-neuron bucket (neuron / bucket_width, at most 255 buckets), time
+ * order kept inside each bucket, with bucket_offsets (B, n_buckets + 1) delimiting the buckets.
+ * Replaces get_sorted_spikes_indices + take_along_axis + compute_pre_exps
  * (bats/CudaKernels/Wrappers/Inference/get_sorted_spikes_indices.py:7-17; bats/Layers/LIFLayer.py:66-84). */
 size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_pre);
 int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, float tau_s, float tau,
-                     const float* exp_tau_s, const float* exp_tau, void* events,
-                     int* slot_out, int* ev_count, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+                     const float* exp_tau_s, const float* exp_tau, void* events, int* slot_out, int* ev_count,
+                     void* events_bucketed, int* bucket_offsets, int bucket_width, void* workspace,
+                     size_t workspace_bytes, cudaStream_t stream);
 
 /* Fully-connected LIF forward: spike counts (B, N_post) and a, x, times, post_exp_tau (B, N_post, K_post);
  * times/post_exp_tau are +inf after the spikes, a/x are undefined there. c = theta/tau,
@@ -96,13 +105,15 @@ int bats_backward_prep(const float* post_times, const float* a, const float* x, 
 
 /* Weight gradient of a fully-connected layer. group == 1: per-sample gradient (B, N_post, N_pre) like the
  * reference; group > 1: the batch mean (mean != 0) or sum (N_post, N_pre), accumulated per group of samples
- * and reduced in a fixed order (deterministic). Replaces compute_weights_gradient (+ the caller's mean over the batch)
- * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24). */
+ * and reduced in a fixed order (deterministic). Reads the events grouped in pre-neuron buckets of 64
+ * (events_bucketed + bucket_offsets from bats_sort_events with bucket_width 64) when given, else filters the
+ * time-sorted events (events + ev_count). Replaces compute_weights_gradient (+ the caller's mean over the
+ * batch) (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24). */
 size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, int n_pre, int group);
-int bats_weights_gradient(const void* events, const int* ev_count, long long ev_cap, const float* post_times,
-                          const void* tables, const int* nvalid, int batch, int n_post, int k_post, int n_pre,
-                          int group, int mean, float* grad, void* workspace, size_t workspace_bytes,
-                          cudaStream_t stream);
+int bats_weights_gradient(const void* events, const int* ev_count, const void* events_bucketed,
+                          const int* bucket_offsets, long long ev_cap, const float* post_times, const void* tables,
+                          const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, int mean,
+                          float* grad, void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
 /* Allocation-free batch mean of bats_weights_gradient (group >= 2), for callers that cannot allocate device
  * memory (a runtime with a fixed arena, a plugin host that passes only input and output buffers). No

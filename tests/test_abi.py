@@ -57,7 +57,7 @@ def test_shape_validation_without_a_gpu(lib):
     st = L.bats_lif_forward_fc(None, None, 0, None, 1, 2, 4, 3, 1.0, 1.0, 1.0, 1.0, None, None, None, None, None,
                                None, None)
     assert st == 1  # BATS_ERR_BAD_SHAPE: ld < n_post
-    st = L.bats_sort_events(None, 2, 3, 0, 1.0, 1.0, None, None, None, None, None, None, 0, None)
+    st = L.bats_sort_events(None, 2, 3, 0, 1.0, 1.0, None, None, None, None, None, None, None, 0, None, 0, None)
     assert st == 1
     assert b"sort_events" in L.bats_last_error()
     # batch 0 is a no-op
@@ -72,4 +72,4 @@ def test_workspace_queries(lib):
     assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 4 * 30000 * 4
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == 16 * 800 * 784 * 4
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 1) == 0
-    assert L.bats_pre_errors_workspace_bytes(2, 100, 300) == 2 * 100 * 3 * 4
+    assert L.bats_pre_errors_workspace_bytes(2, 100, 300) == 2 * 100 * 3 * 2 * 4
