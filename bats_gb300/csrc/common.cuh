@@ -47,45 +47,41 @@ struct SolveConst {
     float tau;
     float max_sim;
     float e_max;    // exp(max_sim / tau), +inf when unbounded
+    float inv_c;    // 1 / c
     bool fast;      // c > 0: the provable rejections below are valid
 };
 
-// True when the reference solver provably finds no crossing in the window (t_last, t_next] for the
-// state (a, b), so the exact evaluation can be skipped without changing any result:
-//   * a <= 0 or b < 0 (with b^2 a normal float): the reference's x = sqrt(tmp) satisfies x >= |b|
-//     (a <= 0) or x <= |b| (a > 0, b < 0), because sqrt(fl(b^2)) == |b| in binary floating point;
-//     then x + b == 0, or z = 2a/(x + b) <= 0, and the log of a non-positive z is rejected.
-//   * a > 0 and fl(b*b) < fl(4a*c): b^2 - 4ac < 0 in every evaluation order (double, float, fused).
-//   * otherwise an approximate root z_f = 2a/(b + sq), sq ~ sqrt(fl(b^2 - 4ac)), is compared with the
-//     window [exp(t_last/tau), min(exp(t_next/tau), exp(max_sim/tau))] in z = exp(t/tau) space with a
-//     relative margin m that bounds |z_f - z| for the reference's root z: with
-//     err_D = 2^-23 b^2 + 2^-24 |D_f| >= |D_f - D| (D = fl(b^2) - 4ac, a > 0, b > 0, 4ac <= fl(b^2)),
-//     |sq - sqrt(D)| <= d = min(err_D / sq, sqrt(err_D)) + 2^-21 sq, so z_f is within d / (b + sq - d) of
-//     the exact root; the reference's own rounding of x, x + b and 2a/(x + b), the approximate
-//     reciprocal and square roots used here, __expf of the window ends and __logf of the root are all
-//     below 2^-19 relative together, and m = d / (b + sq - d) + 2^-16 covers them. A root outside the
-//     widened window gives a spike time tau*ln(z) outside (t_last, min(t_next, max_sim)], which the
-//     reference rejects.
-__device__ __forceinline__ bool no_crossing(float a, float b, float e_last, float e_next, const SolveConst& k) {
-    if (!k.fast) return false;
+// True when the reference solver provably accepts no crossing in the window (t_last, t_next] for the
+// state (a, b), so that its exact evaluation can be skipped without changing any result. With
+// B2 = fl(b*b), D = B2 - 4ac and (|b| a normal float, a <= 2^60, c > 0):
+//   * a <= 0 or b < 0: the reference's x = sqrt(tmp) satisfies x >= |b| (a <= 0) or x <= |b|
+//     (a > 0, b < 0), because sqrt(fl(b^2)) == |b| in binary floating point; then x + b == 0, or
+//     z = 2a/(x + b) <= 0, and the log of a non-positive z is rejected.
+//   * a > 0 and B2 < fl(4a*c): D < 0 in every evaluation order (double, float, fused), so the
+//     discriminant test fails.
+//   * otherwise (a, b > 0) the reference's root z = 2a/(x + b) lies within 2^-21 (relative) of the
+//     smaller root z1 of Q(z) = c z^2 - sqrt(B2) z + a (the FC discriminant is formed in double, so tmp
+//     is D to 2^-24 relative; the conv discriminant, formed in float, is D to 2^-22 B2 absolute, which
+//     bounds z by the root of Q with a lowered by 2^-24 B2 / c). Z_hi = min(exp(t_next/tau),
+//     exp(max_sim/tau)) is widened by 2^-19 + 2^-20 for the errors of __expf, of __logf and of the root.
+//     If Z_hi lies left of the vertex of Q (2c Z_hi < sqrt(B2)) and Q(Z_hi) is positive beyond its
+//     rounding error (2^-21 of the sum of its terms's magnitudes; plus 2^-23 B2 / c for conv), then
+//     Z_hi < z1: the spike time tau ln z exceeds t_next or max_sim, and the reference rejects it. The
+//     window test is used for t_next < 8 tau only (Z_hi < 2981), where those error bounds hold.
+//     No square root or division is needed.
+template <bool CONV>
+__device__ __forceinline__ bool no_crossing(float a, float b, float e_next, const SolveConst& k) {
     const float ab = fabsf(b);
-    if (!(ab >= 0x1p-60f && ab <= 0x1p60f)) return false;
-    if (a <= 0.0f || b < 0.0f) return true;
-    if (!(a <= 0x1p60f)) return false;
+    const bool usable = k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && a <= 0x1p60f;
     const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), k.c);
     const float B2 = __fmul_rn(b, b);
-    if (B2 < p_hi) return true;
-    const float Df = fmaf(b, b, -p_hi);
-    const float err_d = fmaf(0x1p-23f, B2, 0x1p-24f * fabsf(Df));
-    const float rs = Df > 0.0f ? rsqrtf(Df) : 0.0f;
-    const float sq = Df * rs;  // 0 when Df <= 0
-    const float d_sqrt = err_d * rsqrtf(err_d);
-    const float d = (Df > 0.0f ? fminf(err_d * rs, d_sqrt) : d_sqrt) + 0x1p-21f * sq;
-    const float den = b + sq;
-    if (!(den > 2.0f * d)) return false;
-    const float m = __fdividef(d, den - d) + 0x1p-16f;
-    const float zf = __fdividef(2.0f * a, den);
-    return zf > fminf(e_next, k.e_max) * (1.0f + m) || zf < e_last * (1.0f - m);
+    const bool level1 = a <= 0.0f || b < 0.0f || B2 < p_hi;
+    const float Z = fminf(e_next, k.e_max) * (1.0f + 0x1.8p-19f);
+    const float q = fmaf(fmaf(k.c, Z, -b), Z, a);                 // (cZ - b) Z + a
+    float err = 0x1p-21f * fmaf(fmaf(k.c, Z, b), Z, a);           // |rounding| + |sqrt(B2) - b| Z
+    if (CONV) err = fmaf(0x1p-23f * B2, k.inv_c, err);
+    const bool right_of_window = Z < 2981.0f && (2.0f * k.c) * Z < b * (1.0f - 0x1p-21f) && q > err;
+    return usable && (level1 || right_of_window);
 }
 
 // Threshold-crossing solver of the current-based LIF neuron after an input event.
@@ -94,20 +90,20 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_last, floa
 // c = theta/tau. The next crossing is z = 2a / (b + sqrt(b^2 - 4ac)), t = tau*ln z, accepted in
 // the window (last_t, min(next_t, max_sim)]. Each accepted spike applies the reset
 // b -= (dtheta/tau) * z and the search repeats until no crossing remains or k_post spikes
-// have been written. Returns true when the spike buffer is full. e_last/e_next are exp(t/tau) of
-// the window ends (used only by no_crossing).
+// have been written. Returns true when the spike buffer is full. e_next is exp(t_next/tau), used only
+// by no_crossing.
 //
 // The arithmetic after the no_crossing test is kept operation for operation identical to the
 // reference solver (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 for the FC layer,
 // compute_spike_times_conv.cu:59-90 for the conv layer, whose discriminant is evaluated in float
 // instead of double), so that spike times agree bit for bit.
 template <bool CONV>
-__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_last,
-                                                float e_next, const SolveConst& k, int& n, int k_post,
+__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_next,
+                                                const SolveConst& k, int& n, int k_post,
                                                 float* __restrict__ a_out, float* __restrict__ x_out,
                                                 float* __restrict__ t_out, float* __restrict__ z_out) {
     while (true) {
-        if (no_crossing(a, b, e_last, e_next, k)) return false;
+        if (no_crossing<CONV>(a, b, e_next, k)) return false;
         float tmp;
         if (CONV) {
             tmp = b * b - 4 * a * k.c;
@@ -127,7 +123,6 @@ __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t,
         t_out[n] = tmp;
         z_out[n] = inside_log;
         last_t = tmp;
-        e_last = inside_log;
         b -= k.dtt * inside_log;
         n++;
         if (n >= k_post) return true;

@@ -66,7 +66,7 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
     // Receptive field of the whole tile.
     const int rx0 = tx0, rx1 = min(X, tx0 + TX + fx - 1), ry0 = ty0, ry1 = min(Y, ty0 + TY + fy - 1);
 
-    float a = 0.0f, b = 0.0f, last_t = 0.0f, last_e = 1.0f;
+    float a = 0.0f, b = 0.0f, last_t = 0.0f;
     bool has_prev = false;
     int n = 0;
     bool done = !active;
@@ -110,20 +110,19 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
             const int dx = (e.xyc & 1023) - xo, dy = ((e.xyc >> 10) & 1023) - yo;
             if (dx < 0 || dx >= fx || dy < 0 || dy >= fy) continue;
             if (has_prev) {
-                done = solve_crossings<true>(a, b, last_t, e.t, last_e, e.e, sk, n, k_post, ao, xo_, to, zo);
+                done = solve_crossings<true>(a, b, last_t, e.t, e.e, sk, n, k_post, ao, xo_, to, zo);
                 if (done) break;
             }
             const float w = Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)];
             a += w * e.es;
             b += w * e.e;
             last_t = e.t;
-            last_e = e.e;
             has_prev = true;
         }
     }
     if (active) {
         if (has_prev && !done)
-            solve_crossings<true>(a, b, last_t, BATS_INF, last_e, BATS_INF, sk, n, k_post, ao, xo_, to, zo);
+            solve_crossings<true>(a, b, last_t, BATS_INF, BATS_INF, sk, n, k_post, ao, xo_, to, zo);
         n_spikes[(long long)s * n_post + post] = n;
         for (int k = n; k < k_post; ++k) {
             to[k] = BATS_INF;

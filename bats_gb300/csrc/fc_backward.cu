@@ -77,6 +77,119 @@ __global__ void bwd_prep_kernel(const float* __restrict__ t, const float* __rest
     }
 }
 
+// Layer-path variant of bwd_prep_kernel for K <= 32, for spike trains produced by the forward kernels
+// (times and post_exp_tau finite exactly on a neuron's leading spikes). Each warp handles 32 neurons:
+// their K-slot rows are contiguous in memory, so they are staged through shared memory with
+// coalesced loads and stores; a warp whose neurons are all silent only reads the spike times. The
+// arithmetic per neuron is that of bwd_prep_kernel (the reference's order). f1/f2 are written only
+// when requested.
+constexpr int PREP_WARPS = 2;
+constexpr int PREP_KS = 33;  // padded row stride (conflict-free)
+
+__global__ void __launch_bounds__(PREP_WARPS * 32)
+bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, const float* __restrict__ x,
+                      const float* __restrict__ z, float* __restrict__ err, long long total, int K, float c, float tau,
+                      float dtt, float* __restrict__ f1, float* __restrict__ f2, float2* __restrict__ tab,
+                      int* __restrict__ nvalid) {
+    extern __shared__ float prep_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* sT = prep_smem + warp * 5 * 32 * PREP_KS;
+    float* sZ = sT + 32 * PREP_KS;
+    float* sX = sZ + 32 * PREP_KS;
+    float* sA = sX + 32 * PREP_KS;
+    float* sE = sA + 32 * PREP_KS;
+    const long long nb = ((long long)blockIdx.x * PREP_WARPS + warp) * 32;
+    if (nb >= total) return;
+    const int cnt = (int)min(32LL, total - nb);
+    const long long base = nb * K;
+    const int nk = cnt * K;
+    for (int q = lane; q < nk; q += 32) sT[(q / K) * PREP_KS + q % K] = t[base + q];
+    __syncwarp();
+    int n = 0;
+    if (lane < cnt) {
+        n = K;
+        for (int k = 0; k < K; ++k)
+            if (isinf(sT[lane * PREP_KS + k])) {
+                n = k;
+                break;
+            }
+        nvalid[nb + lane] = n;
+    }
+    const int K1 = K + 1;
+    if (!__any_sync(0xffffffffu, n > 0)) {
+        // Silent neurons: empty tables, zero factors, errors unchanged.
+        if (lane < cnt) tab[(nb + lane) * K1] = make_float2(0.0f, 0.0f);
+        if (f1)
+            for (int q = lane; q < nk; q += 32) {
+                f1[base + q] = 0.0f;
+                f2[base + q] = 0.0f;
+            }
+        return;
+    }
+    for (int q = lane; q < nk; q += 32) {
+        const int o = (q / K) * PREP_KS + q % K;
+        sZ[o] = z[base + q];
+        sX[o] = x[base + q];
+        sA[o] = a[base + q];
+        sE[o] = err[base + q];
+    }
+    __syncwarp();
+    if (lane < cnt) {
+        float* rt = sT + lane * PREP_KS;
+        float* rz = sZ + lane * PREP_KS;
+        float* rx = sX + lane * PREP_KS;
+        float* ra = sA + lane * PREP_KS;
+        float* re = sE + lane * PREP_KS;
+        // Reset errors, last spike first (propagate_recurrent_errors.cu:17-22).
+        float cum = 0.0f;
+        for (int k = n - 1; k >= 0; --k) {
+            const float ek = re[k] + cum * rz[k];
+            re[k] = ek;
+            cum += ek * dtt / rx[k];
+        }
+        // Factors (compute_factors.cu:27-30); f1 replaces a, f2 replaces z.
+        for (int k = 0; k < K; ++k) {
+            float v1 = 0.0f, v2 = 0.0f;
+            if (k < n) {
+                const float xk = rx[k];
+                v1 = tau / ra[k] * (1 + rz[k] * c / xk);
+                v2 = tau / xk;
+            }
+            ra[k] = v1;
+            rz[k] = v2;
+        }
+        // Suffix tables in the reference's accumulation order; (SA_p, SB_p) into (t, x) rows.
+        for (int p = 0; p < n; ++p) {
+            float sa = 0.0f, sb = 0.0f;
+            for (int k = p; k < n; ++k) {
+                const float ek = re[k];
+                sa += ek * ra[k];
+                sb += ek * rz[k];
+            }
+            rt[p] = sa;
+            rx[p] = sb;
+        }
+        for (int p = n; p <= K && p < PREP_KS; ++p) {
+            rt[p] = 0.0f;
+            rx[p] = 0.0f;
+        }
+    }
+    __syncwarp();
+    for (int q = lane; q < nk; q += 32) {
+        const int o = (q / K) * PREP_KS + q % K;
+        err[base + q] = sE[o];
+        if (f1) {
+            f1[base + q] = sA[o];
+            f2[base + q] = sZ[o];
+        }
+    }
+    const int nt = cnt * K1;
+    for (int q = lane; q < nt; q += 32) {
+        const int o = (q / K1) * PREP_KS + q % K1;
+        tab[nb * K1 + q] = make_float2(sT[o], sX[o]);
+    }
+}
+
 constexpr int BWD_CHUNK = 128;
 
 // Weight gradient. Grid (post tiles, pre chunks, sample groups); each thread owns one post
@@ -352,6 +465,31 @@ extern "C" int bats_backward_prep(const float* post_times, const float* a, const
     bats::bwd_prep_kernel<<<blocks, threads, 0, stream>>>(post_times, a, x, post_exp_tau, errors, total, k_post, c,
                                                          tau, delta_theta_tau, do_recurrent, do_factors, f1, f2,
                                                          reinterpret_cast<float2*>(tables), nvalid);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_backward_prep_layer(const float* post_times, const float* a, const float* x,
+                                        const float* post_exp_tau, float* errors, int batch, int n_post, int k_post,
+                                        float c, float tau, float delta_theta_tau, float* f1, float* f2, void* tables,
+                                        int* nvalid, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0, BATS_ERR_BAD_SHAPE, "backward_prep_layer: bad shape");
+    const long long total = (long long)batch * n_post;
+    if (total == 0) return BATS_OK;
+    BATS_REQUIRE(post_times && a && x && post_exp_tau && errors && tables && nvalid && ((f1 == nullptr) == (f2 == nullptr)),
+                 BATS_ERR_NULL, "backward_prep_layer: null pointer");
+    if (k_post > 32) {
+        BATS_REQUIRE(f1 && f2, BATS_ERR_NULL, "backward_prep_layer: f1/f2 buffers are required when k_post > 32");
+        return bats_backward_prep(post_times, a, x, post_exp_tau, errors, batch, n_post, k_post, c, tau,
+                                  delta_theta_tau, 1, 1, f1, f2, tables, nvalid, stream);
+    }
+    const long long warps = (total + 31) / 32;
+    const int blocks = (int)((warps + bats::PREP_WARPS - 1) / bats::PREP_WARPS);
+    const size_t smem = (size_t)bats::PREP_WARPS * 5 * 32 * bats::PREP_KS * sizeof(float);
+    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_prep_layer_kernel, (int)smem));
+    bats::bwd_prep_layer_kernel<<<blocks, bats::PREP_WARPS * 32, smem, stream>>>(
+        post_times, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau, f1, f2,
+        reinterpret_cast<float2*>(tables), nvalid);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -82,7 +82,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
                 aa = in ? a2 : aa;
                 bb = in ? b2 : bb;
                 const float e_next = (m0 + u + 1 < E) ? e_nx : BATS_INF;
-                const bool maybe = !no_crossing(aa, bb, e4.w, e_next, sk);
+                const bool maybe = !no_crossing<false>(aa, bb, e_next, sk);
                 cand |= (in && maybe) ? (1u << u) : 0u;
             }
             if (cand == 0u) {
@@ -105,7 +105,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
                     const bool has_next = m0 + u + 1 < E;
                     const float t_next = has_next ? se[u + 1].t : BATS_INF;
                     const float e_next = has_next ? se[u + 1].e : BATS_INF;
-                    done = solve_crossings<false>(a, b, e.t, t_next, e.e, e_next, sk, n, k_post, ao, xo, to, zo);
+                    done = solve_crossings<false>(a, b, e.t, t_next, e_next, sk, n, k_post, ao, xo, to, zo);
                     if (done) break;
                 }
             }
@@ -143,6 +143,7 @@ SolveConst make_solve_const(float c, float dtt, float tau, float max_sim) {
     k.max_sim = max_sim;
     const double em = std::exp((double)max_sim / (double)tau);
     k.e_max = std::isfinite(em) && em < 3.0e38 ? (float)em : std::numeric_limits<float>::infinity();
+    k.inv_c = c > 0.0f ? 1.0f / c : 0.0f;
     k.fast = c > 0.0f && tau > 0.0f;
     return k;
 }

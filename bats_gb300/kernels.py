@@ -217,19 +217,27 @@ class BackwardTables:
 
 
 def backward_prep(post_times, a, x, post_exp_tau, errors, c: float, tau: float, delta_theta_tau: float,
-                  recurrent: bool = True, out: BackwardTables | None = None) -> BackwardTables:
+                  recurrent: bool = True, out: BackwardTables | None = None, want_factors: bool = False
+                  ) -> BackwardTables:
     """Reset errors in place + factors + suffix tables (replaces propagate_recurrent_errors and
-    compute_factors, Wrappers/Backpropagation/propagate_recurrent_errors.py:9-16, compute_factors.py:11-22)."""
+    compute_factors, Wrappers/Backpropagation/propagate_recurrent_errors.py:9-16, compute_factors.py:11-22).
+    For the forward kernels' outputs (the layer path); f1/f2 are only materialised if want_factors."""
     B, N, K = post_times.shape
     dev = post_times.device
+    need_f = want_factors or K > 32 or not recurrent
     if out is None:
-        out = BackwardTables(torch.empty((B, N, K), dtype=F32, device=dev),
-                             torch.empty((B, N, K), dtype=F32, device=dev),
+        out = BackwardTables(torch.empty((B, N, K), dtype=F32, device=dev) if need_f else None,
+                             torch.empty((B, N, K), dtype=F32, device=dev) if need_f else None,
                              torch.empty((B, N, K + 1, 2), dtype=F32, device=dev),
                              torch.empty((B, N), dtype=I32, device=dev))
-    call("bats_backward_prep", ptr(post_times), ptr(a), ptr(x), ptr(post_exp_tau), ptr(errors), B, N, K,
-         float(c), float(tau), float(delta_theta_tau), int(recurrent), 1, ptr(out.f1), ptr(out.f2), ptr(out.tables),
-         ptr(out.nvalid), stream_ptr())
+    if recurrent:
+        call("bats_backward_prep_layer", ptr(post_times), ptr(a), ptr(x), ptr(post_exp_tau), ptr(errors), B, N, K,
+             float(c), float(tau), float(delta_theta_tau), ptr(out.f1), ptr(out.f2), ptr(out.tables),
+             ptr(out.nvalid), stream_ptr())
+    else:
+        call("bats_backward_prep", ptr(post_times), ptr(a), ptr(x), ptr(post_exp_tau), ptr(errors), B, N, K,
+             float(c), float(tau), float(delta_theta_tau), 0, 1, ptr(out.f1), ptr(out.f2), ptr(out.tables),
+             ptr(out.nvalid), stream_ptr())
     return out
 
 

@@ -60,8 +60,9 @@ class FCTrainStep:
             N, Kp = spec.n_neurons, spec.max_n_spike
             self.out.append((torch.empty((B, N), dtype=i32, device=dev),
                              *(torch.empty((B, N, Kp), dtype=f32, device=dev) for _ in range(4))))
-            self.tabs.append(K.BackwardTables(torch.empty((B, N, Kp), dtype=f32, device=dev),
-                                              torch.empty((B, N, Kp), dtype=f32, device=dev),
+            need_f = Kp > 32
+            self.tabs.append(K.BackwardTables(torch.empty((B, N, Kp), dtype=f32, device=dev) if need_f else None,
+                                              torch.empty((B, N, Kp), dtype=f32, device=dev) if need_f else None,
                                               torch.empty((B, N, Kp + 1, 2), dtype=f32, device=dev),
                                               torch.empty((B, N), dtype=i32, device=dev)))
             self.grad.append(torch.empty((N, n_prev), dtype=f32, device=dev))
@@ -126,8 +127,8 @@ class FCTrainStep:
             tb = self.tabs[li]
             tag = f"L{li + 1}"
             L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt, tb=tb:
-                      call("bats_backward_prep", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]), ptr(e), B,
-                           spec.n_neurons, spec.max_n_spike, float(c), float(tau32), float(dtt), 1, 1, ptr(tb.f1),
+                      call("bats_backward_prep_layer", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]), ptr(e), B,
+                           spec.n_neurons, spec.max_n_spike, float(c), float(tau32), float(dtt), ptr(tb.f1),
                            ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
             grp = self.groups[li]
             L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, grp=grp: call(

@@ -103,6 +103,14 @@ int bats_backward_prep(const float* post_times, const float* a, const float* x, 
                        int do_recurrent, int do_factors, float* f1, float* f2, void* tables, int* nvalid,
                        cudaStream_t stream);
 
+/* bats_backward_prep (recurrent + factors + tables) for spike trains produced by the forward entry points
+ * (post_times and post_exp_tau finite exactly on each neuron's leading spikes): rows staged through shared
+ * memory, silent neurons skipped, f1/f2 written only if given (required when k_post > 32). */
+int bats_backward_prep_layer(const float* post_times, const float* a, const float* x, const float* post_exp_tau,
+                             float* errors, int batch, int n_post, int k_post, float c, float tau,
+                             float delta_theta_tau, float* f1, float* f2, void* tables, int* nvalid,
+                             cudaStream_t stream);
+
 /* Weight gradient of a fully-connected layer. group == 1: per-sample gradient (B, N_post, N_pre) like the
  * reference; group > 1: the batch mean (mean != 0) or sum (N_post, N_pre), accumulated per group of samples
  * and reduced in a fixed order (deterministic). Reads the events grouped in pre-neuron buckets of 64

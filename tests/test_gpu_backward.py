@@ -128,12 +128,12 @@ def test_two_layer_backward_vs_reference_kernels(cuda, variant):
     _, err2 = K.spike_count_loss(n2, labels=cu(labels, torch.int32), target_true=15, target_false=3, k=K_post)
     err2_ref = err2.clone()
     tau32, c2, dtt2 = K.lif_constants(tau_s, th2, th2)
-    tab2 = K.backward_prep(t2, a2, x2, z2, err2, c2, tau32, dtt2)
+    tab2 = K.backward_prep(t2, a2, x2, z2, err2, c2, tau32, dtt2, want_factors=True)
     g2 = K.weights_gradient(ev2, t2, tab2, 120, per_sample=True)
     pe2 = K.pre_errors(ev2, wt2, t2, tab2, tau_s, tau32)
     _, c1, dtt1 = K.lif_constants(tau_s, th1, th1)
     e1 = pe2.clone()
-    tab1 = K.backward_prep(t1, a1, x1, z1, e1, c1, tau32, dtt1)
+    tab1 = K.backward_prep(t1, a1, x1, z1, e1, c1, tau32, dtt1, want_factors=True)
     g1 = K.weights_gradient(ev1, t1, tab1, 784, per_sample=True)
     g1_mean = K.weights_gradient(ev1, t1, tab1, 784, per_sample=False, group=4)
     # Reference kernels on the same inputs.
