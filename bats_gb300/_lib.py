@@ -34,6 +34,8 @@ SIGNATURES = {
                                     c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_conv_forward": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                   c_float, c_float, c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "bats_events_to_trains": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
+    "bats_events_max_per_neuron": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_vp, c_vp]),
     "bats_pool_forward": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
     "bats_backward_prep": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                    c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#include "disc.cuh"
 
 #define BATS_INF __int_as_float(0x7f800000)
 
@@ -93,10 +94,11 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_next, cons
 // have been written. Returns true when the spike buffer is full. e_next is exp(t_next/tau), used only
 // by no_crossing.
 //
-// The arithmetic after the no_crossing test is kept operation for operation identical to the
-// reference solver (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 for the FC layer,
+// The arithmetic after the no_crossing test gives results bit-identical to the reference solver
+// (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 for the FC layer,
 // compute_spike_times_conv.cu:59-90 for the conv layer, whose discriminant is evaluated in float
-// instead of double), so that spike times agree bit for bit.
+// instead of double): the FC discriminant through fc_discriminant, which reproduces the reference's
+// double expression without FP64 on its common path, everything else operation for operation.
 template <bool CONV>
 __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_next,
                                                 const SolveConst& k, int& n, int k_post,
@@ -108,7 +110,7 @@ __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t,
         if (CONV) {
             tmp = b * b - 4 * a * k.c;
         } else {
-            tmp = (float)((double)__fmul_rn(b, b) - 4.0 * (double)a * (double)k.c);
+            tmp = fc_discriminant(__fmul_rn(b, b), a, k.c);  // == (float)((double)fl(b*b) - 4.0*a*c)
         }
         if (tmp < 0) return false;
         const float x_tmp = sqrtf(tmp);

@@ -1,0 +1,125 @@
+// Event-list input format: (neuron index, time) per spike, in order of appearance, index < 0 ending a
+// sample -> per-neuron spike trains (B, N, K) + counts (B, N), the layout every layer reads.
+//
+// Replaces convert_to_spike_per_neuron (bats/CudaKernels/CuFiles/Inference/convert_to_spike_per_neuron.cu:2-26,
+// Wrappers/Inference/convert_to_spike_per_neuron.py:20-33): the reference runs one thread per sample
+// over its events; here one warp per sample takes 32 events at a time and ranks events of the same
+// neuron by __match_any_sync, so every spike lands in the slot of its order of appearance, as in the
+// reference. Slots past a neuron's count hold +inf. Spikes beyond k_cap slots are dropped and counted in
+// *overflow (the reference sizes K to the batch maximum with a host-side cp.unique loop; callers that
+// need the same do so from the counts of a first pass).
+#include "common.cuh"
+#include "abi_util.h"
+
+namespace bats {
+
+constexpr int CONV_WARPS = 4;
+
+__global__ void __launch_bounds__(CONV_WARPS * 32)
+events_to_trains_kernel(const int* __restrict__ indices, const float* __restrict__ times, int batch, int max_events,
+                        int n_neurons, int k_cap, float* __restrict__ out_times, int* __restrict__ out_counts,
+                        int* __restrict__ overflow) {
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);
+    if (s >= batch) return;
+    const long long tb = (long long)s * n_neurons * k_cap;
+    int* cnt = out_counts + (long long)s * n_neurons;
+    for (long long q = lane; q < (long long)n_neurons * k_cap; q += 32) out_times[tb + q] = BATS_INF;
+    for (int q = lane; q < n_neurons; q += 32) cnt[q] = 0;
+    __syncwarp();
+    const int* idx = indices + (long long)s * max_events;
+    const float* tm = times + (long long)s * max_events;
+    int dropped = 0;
+    for (int m0 = 0; m0 < max_events; m0 += 32) {
+        const int m = m0 + lane;
+        int j = m < max_events ? idx[m] : -1;
+        // The sample ends at its first negative index.
+        const unsigned neg = __ballot_sync(0xffffffffu, j < 0 || j >= n_neurons);
+        const int stop = neg ? __ffs(neg) - 1 : 32;
+        const bool valid = lane < stop;
+        if (!valid) j = -1 - lane;  // distinct keys so that invalid lanes never match
+        const unsigned peers = __match_any_sync(0xffffffffu, j);
+        const int rank = __popc(peers & lanemask_lt());
+        int base = 0;
+        if (valid && rank == 0) base = cnt[j];
+        base = __shfl_sync(0xffffffffu, base, __ffs(peers) - 1);
+        if (valid) {
+            const int slot = base + rank;
+            if (slot < k_cap)
+                out_times[tb + (long long)j * k_cap + slot] = tm[m];
+            else
+                ++dropped;
+            if (rank == 0) cnt[j] = min(base + __popc(peers), k_cap);
+        }
+        __syncwarp();
+        if (stop < 32) break;
+    }
+    for (int o = 16; o >= 1; o >>= 1) dropped += __shfl_xor_sync(0xffffffffu, dropped, o);
+    if (lane == 0 && dropped && overflow) atomicAdd(overflow, dropped);
+}
+
+// Largest per-neuron spike count of each sample (the K the reference derives on the host).
+__global__ void __launch_bounds__(CONV_WARPS * 32)
+max_per_neuron_kernel(const int* __restrict__ indices, int batch, int max_events, int n_neurons,
+                      int* __restrict__ scratch_counts, int* __restrict__ out_max) {
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);
+    if (s >= batch) return;
+    int* cnt = scratch_counts + (long long)s * n_neurons;
+    for (int q = lane; q < n_neurons; q += 32) cnt[q] = 0;
+    __syncwarp();
+    const int* idx = indices + (long long)s * max_events;
+    int best = 0;
+    for (int m0 = 0; m0 < max_events; m0 += 32) {
+        const int m = m0 + lane;
+        int j = m < max_events ? idx[m] : -1;
+        const unsigned neg = __ballot_sync(0xffffffffu, j < 0 || j >= n_neurons);
+        const int stop = neg ? __ffs(neg) - 1 : 32;
+        const bool valid = lane < stop;
+        if (!valid) j = -1 - lane;
+        const unsigned peers = __match_any_sync(0xffffffffu, j);
+        const int rank = __popc(peers & lanemask_lt());
+        int base = 0;
+        if (valid && rank == 0) base = cnt[j];
+        base = __shfl_sync(0xffffffffu, base, __ffs(peers) - 1);
+        if (valid && rank == 0) {
+            cnt[j] = base + __popc(peers);
+            best = max(best, base + __popc(peers));
+        }
+        __syncwarp();
+        if (stop < 32) break;
+    }
+    for (int o = 16; o >= 1; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (lane == 0) out_max[s] = best;
+}
+
+}  // namespace bats
+
+extern "C" int bats_events_to_trains(const int* indices, const float* times, int batch, int max_events, int n_neurons,
+                                     int k_cap, float* out_times, int* out_counts, int* overflow,
+                                     cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && max_events >= 0 && n_neurons > 0 && k_cap > 0, BATS_ERR_BAD_SHAPE,
+                 "events_to_trains: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(out_times && out_counts && (max_events == 0 || (indices && times)), BATS_ERR_NULL,
+                 "events_to_trains: null pointer");
+    const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
+    bats::events_to_trains_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
+        indices, times, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_events_max_per_neuron(const int* indices, int batch, int max_events, int n_neurons,
+                                          int* scratch_counts, int* out_max, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && max_events >= 0 && n_neurons > 0, BATS_ERR_BAD_SHAPE,
+                 "events_max_per_neuron: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(scratch_counts && out_max && (max_events == 0 || indices), BATS_ERR_NULL,
+                 "events_max_per_neuron: null pointer");
+    const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
+    bats::max_per_neuron_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(indices, batch, max_events, n_neurons,
+                                                                              scratch_counts, out_max);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}

@@ -98,15 +98,22 @@ __device__ __forceinline__ void stream_init(StreamSmem<TILE, SEV, STAGES>& sm, i
     }
 }
 
-// Producer warp body. Never returns with copies in flight into shared memory.
+// Producer warp body. Never returns with copies in flight into shared memory. Lane u issues the row
+// copy of the stage's event u (SEV <= 32); the event indices of the next stage are loaded while the
+// producer waits for a free slot, so that no global-load latency sits between two stages.
 template <int TILE, int SEV, int STAGES>
 __device__ __forceinline__ void stream_produce(StreamSmem<TILE, SEV, STAGES>& sm, const Event* __restrict__ evs, int E,
                                                const float* __restrict__ wt, int ld, int tile0, int n_stages,
                                                int lane, int* status) {
+    static_assert(SEV <= 32, "one event per producer lane");
     const uint32_t row_bytes = (uint32_t)min(TILE, ld - tile0) * 4u;
     int issued = 0;
+    int j_next = (lane < SEV && lane < E) ? __ldg(&evs[lane].j) : 0;
     for (int k = 0; k < n_stages; ++k) {
         const int slot = k % STAGES;
+        const int j = j_next;
+        const int m1 = (k + 1) * SEV + lane;
+        j_next = (lane < SEV && m1 < E) ? __ldg(&evs[m1].j) : 0;
         const bool ok = mbar_wait(&sm.empty[slot], ((k / STAGES) & 1) ^ 1, &sm.abort, status);
         if (!__all_sync(0xffffffffu, ok)) break;
         const int m0 = k * SEV;
@@ -115,10 +122,7 @@ __device__ __forceinline__ void stream_produce(StreamSmem<TILE, SEV, STAGES>& sm
         if (lane == 0) mbar_arrive_expect_tx(&sm.full[slot], (uint32_t)cnt_ev * 16u + (uint32_t)cnt * row_bytes);
         __syncwarp();
         if (lane == 0) bulk_copy_g2s(&sm.evs[slot][0], evs + m0, (uint32_t)cnt_ev * 16u, &sm.full[slot]);
-        for (int u = lane; u < cnt; u += 32) {
-            const int j = __ldg(&evs[m0 + u].j);
-            bulk_copy_g2s(&sm.rows[slot][u][0], wt + (long long)j * ld + tile0, row_bytes, &sm.full[slot]);
-        }
+        if (lane < cnt) bulk_copy_g2s(&sm.rows[slot][lane][0], wt + (long long)j * ld + tile0, row_bytes, &sm.full[slot]);
         issued = k + 1;
     }
     if (sm.abort) {

@@ -184,6 +184,27 @@ def conv_forward(events: Events, filters, pre_shape, k_post: int, tau_s: float, 
     return n, a, x, t, z
 
 
+def convert_to_spike_per_neuron(indices, times, n_neurons: int, k_cap: int | None = None, overflow=None):
+    """Event list (B, S) of (neuron index, time), index < 0 ending a sample, into per-neuron spike trains
+    (B, N, K) + counts (B, N) (Wrappers/Inference/convert_to_spike_per_neuron.py:20-33). With k_cap None,
+    K is the batch's largest per-neuron count, as in the reference (one host read); otherwise K = k_cap and
+    spikes beyond it are dropped (counted in `overflow`, an int32 CUDA tensor of one element)."""
+    idx = _c(indices, I32)
+    tm = _c(times)
+    B, S = idx.shape
+    dev = idx.device
+    if k_cap is None:
+        scratch = torch.empty((B, int(n_neurons)), dtype=I32, device=dev)
+        mx = torch.empty((B,), dtype=I32, device=dev)
+        call("bats_events_max_per_neuron", ptr(idx), B, S, int(n_neurons), ptr(scratch), ptr(mx), stream_ptr())
+        k_cap = max(1, int(mx.max().item())) if B > 0 else 1
+    out_t = torch.empty((B, int(n_neurons), int(k_cap)), dtype=F32, device=dev)
+    out_n = torch.empty((B, int(n_neurons)), dtype=I32, device=dev)
+    call("bats_events_to_trains", ptr(idx), ptr(tm), B, S, int(n_neurons), int(k_cap), ptr(out_t), ptr(out_n),
+         ptr(overflow), stream_ptr())
+    return out_t, out_n
+
+
 def aggregate_spikes_conv(n_spikes, spike_times, pre_shape):
     """2x2 pooling (replaces aggregate_spikes_conv + argsort, Wrappers/Inference/aggregate_spikes_conv.py:10-28).
     Returns (n_spikes (B, N_out), times (B, N_out, 4K), indices (B, N_out, 4K) int32)."""

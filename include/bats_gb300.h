@@ -91,6 +91,18 @@ int bats_conv_forward(const void* events, const int* ev_count, long long ev_cap,
 int bats_pool_forward(const int* n_spikes, const float* times, int batch, int X, int Y, int C, int K,
                       int* out_n_spikes, float* out_times, int* out_indices, cudaStream_t stream);
 
+/* Event list -> spike trains: indices/times (B, max_events), index < 0 ends a sample; writes times (B, N, k_cap)
+ * (+inf padded, spikes of a neuron in order of appearance) and counts (B, N); spikes beyond k_cap are dropped
+ * and added to *overflow (may be NULL). Replaces convert_to_spike_per_neuron
+ * (bats/CudaKernels/Wrappers/Inference/convert_to_spike_per_neuron.py:20-33). */
+int bats_events_to_trains(const int* indices, const float* times, int batch, int max_events, int n_neurons,
+                          int k_cap, float* out_times, int* out_counts, int* overflow, cudaStream_t stream);
+
+/* Largest per-neuron spike count of each sample of an event list (the K of convert_to_spike_per_neuron,
+ * Wrappers/Inference/convert_to_spike_per_neuron.py:11-18), using scratch_counts (B, N). */
+int bats_events_max_per_neuron(const int* indices, int batch, int max_events, int n_neurons, int* scratch_counts,
+                               int* out_max, cudaStream_t stream);
+
 /* ---- Backpropagation ------------------------------------------------------------------------ */
 
 /* Per (sample, post neuron): reset errors in place on `errors` (if do_recurrent), factors f1/f2

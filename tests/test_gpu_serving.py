@@ -1,0 +1,90 @@
+"""The serving pattern: continuous batching of variable-length spike-event requests on device-resident
+FC networks (bats_gb300.serving). Each request's result is the same alone and in a mixed batch (bit for
+bit: samples are independent in every kernel), equal to the layer API's forward on the same input, and
+the event-list conversion matches the reference test's known answer."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from bats_gb300 import kernels as K
+from bats_gb300.serving import InferenceServer, make_network, make_requests, run_poisson, latency_stats
+from oracle import bats_ref64 as R
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def net(seed=0):
+    return make_network(seed=seed)
+
+
+def test_event_list_conversion_known_answer(cuda):
+    d = np.load(os.path.join(GOLDEN, "kat_convert.npz"))
+    t, n = K.convert_to_spike_per_neuron(torch.tensor(d["indices"], dtype=torch.int32, device="cuda"),
+                                         torch.tensor(d["times"], dtype=torch.float32, device="cuda"),
+                                         int(d["n_neurons"]))
+    np.testing.assert_array_equal(n.cpu().numpy(), d["n_spike_per_neuron"])
+    np.testing.assert_array_equal(t.cpu().numpy(), d["spike_per_neuron"])
+    # Random lists against the oracle, with a capacity smaller than the largest count (dropped, counted).
+    rng = np.random.default_rng(0)
+    idx = rng.integers(0, 40, (5, 300)).astype(np.int32)
+    idx[2, 100:] = -1
+    tm = np.sort(rng.uniform(0, 1, (5, 300)), axis=1).astype(np.float32)
+    t, n = K.convert_to_spike_per_neuron(torch.tensor(idx, device="cuda"), torch.tensor(tm, device="cuda"), 40)
+    et, en = R.convert_to_spike_per_neuron(idx, tm, 40)
+    np.testing.assert_array_equal(n.cpu().numpy(), en)
+    np.testing.assert_array_equal(t.cpu().numpy(), et.astype(np.float32))
+    ovf = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.convert_to_spike_per_neuron(torch.tensor(idx, device="cuda"), torch.tensor(tm, device="cuda"), 40, k_cap=4,
+                                  overflow=ovf)
+    assert int(ovf) == int(np.maximum(en - 4, 0).sum())
+
+
+def test_same_result_alone_and_in_the_mix(cuda):
+    ws, specs = net()
+    server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=32, max_lanes=3)
+    reqs = make_requests(40, seed=1)
+    mixed = server.infer(reqs)
+    assert sum(int(r.counts.sum()) > 0 for r in mixed) >= 10, "the network should produce output spikes"
+    alone_server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=1, max_lanes=1)
+    for r, m in zip(make_requests(40, seed=1, rid0=1000)[:12], mixed[:12]):
+        a = alone_server.infer([r])[0]
+        np.testing.assert_array_equal(a.counts, m.counts)
+        np.testing.assert_array_equal(a.spike_times, m.spike_times)
+
+
+def test_serving_matches_layer_forward(cuda):
+    """The server's batched path gives the same output as converting + running the layers directly."""
+    ws, specs = net()
+    reqs = make_requests(6, seed=3)
+    server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=8, max_lanes=2)
+    res = server.infer(reqs)
+    L = max(len(r.indices) for r in reqs)
+    idx = np.full((6, L), -1, np.int32)
+    tm = np.zeros((6, L), np.float32)
+    for q, r in enumerate(reqs):
+        idx[q, :len(r.indices)] = r.indices
+        tm[q, :len(r.times)] = r.times
+    x, _ = K.convert_to_spike_per_neuron(torch.tensor(idx, device="cuda"), torch.tensor(tm, device="cuda"), 700,
+                                         k_cap=32)
+    for w, sp in zip(ws, specs):
+        ev = K.sort_events(x, np.float32(sp.tau_s), np.float32(2 * sp.tau_s), bucketed=False)
+        n, a, xx, t, z = K.lif_forward_fc(ev, K.transpose_weights(torch.tensor(w, device="cuda")), sp.n_neurons,
+                                          sp.max_n_spike, sp.tau_s, sp.theta, sp.delta_theta)
+        x = t
+    for q, r in enumerate(res):
+        np.testing.assert_array_equal(r.counts, n[q].cpu().numpy())
+        np.testing.assert_array_equal(r.spike_times, x[q].cpu().numpy())
+
+
+def test_poisson_arrivals_complete_with_latency_stats(cuda):
+    ws, specs = net()
+    server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=16, max_lanes=3)
+    reqs = make_requests(200, seed=2)
+    res = run_poisson(server, reqs, rate=2000.0)
+    assert len(res) == 200 and not server.rejected
+    st = latency_stats(res)
+    assert st["p99_ms"] >= st["p50_ms"] > 0
+    assert server.batches_launched > 1
