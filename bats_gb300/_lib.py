@@ -32,6 +32,9 @@ SIGNATURES = {
                                  c_vp, c_int, c_vp, c_size, c_vp]),
     "bats_lif_forward_fc": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float, c_float,
                                     c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "bats_lif_forward_fc_default_algo": (c_int, [c_int, c_int, c_int]),
+    "bats_lif_forward_fc_algo": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float,
+                                         c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp]),
     "bats_conv_forward": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                   c_float, c_float, c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_events_to_trains": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),

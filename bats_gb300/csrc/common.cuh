@@ -63,15 +63,24 @@ struct SolveConst {
 //   * otherwise (a, b > 0) the reference's root z = 2a/(x + b) lies within 2^-21 (relative) of the
 //     smaller root z1 of Q(z) = c z^2 - sqrt(B2) z + a (the FC discriminant is formed in double, so tmp
 //     is D to 2^-24 relative; the conv discriminant, formed in float, is D to 2^-22 B2 absolute, which
-//     bounds z by the root of Q with a lowered by 2^-24 B2 / c). Z_hi = min(exp(t_next/tau),
-//     exp(max_sim/tau)) is widened by 2^-19 + 2^-20 for the errors of __expf, of __logf and of the root.
-//     If Z_hi lies left of the vertex of Q (2c Z_hi < sqrt(B2)) and Q(Z_hi) is positive beyond its
-//     rounding error (2^-21 of the sum of its terms's magnitudes; plus 2^-23 B2 / c for conv), then
-//     Z_hi < z1: the spike time tau ln z exceeds t_next or max_sim, and the reference rejects it. The
-//     window test is used for t_next < 8 tau only (Z_hi < 2981), where those error bounds hold.
+//     bounds z by the root of Q with a lowered by 2^-24 B2 / c). The sign of Q at a point Z is known
+//     when the evaluated Q(Z) exceeds its rounding error (2^-21 of the sum of its terms' magnitudes;
+//     plus 2^-23 B2 / c for conv) in magnitude.
+//     - Right of the window: Z_hi = min(exp(t_next/tau), exp(max_sim/tau)), widened by 2^-19 + 2^-20
+//       for the errors of __expf, of __logf and of the root. If Z_hi lies left of the vertex of Q
+//       (2c Z_hi < sqrt(B2)) and Q(Z_hi) > 0, then Z_hi < z1: the spike time tau ln z exceeds t_next or
+//       max_sim, and the reference rejects it.
+//     - Left of the window (FC only; e_start = exp(t_event/tau) of the window's first event, 0 to skip):
+//       Z_lo = e_start (1 - 2^-17). If Q(Z_lo) < 0 (Z_lo between the roots), or Q(Z_lo) > 0 with Z_lo
+//       right of the vertex (both roots below it), then z1 < Z_lo: the spike time tau ln z lies before
+//       the event (the margin 2^-17 covers __expf, __logf and the root), and the reference rejects it
+//       as not after the last spike or event. Strongly driven neurons that were reset meet this after
+//       most events.
+//     Both tests are used for windows ending before 8 tau (Z < 2981), where those error bounds hold.
+//     LEFT = false leaves the left test out (a cheaper first screen; the solver applies it).
 //     No square root or division is needed.
-template <bool CONV>
-__device__ __forceinline__ bool no_crossing(float a, float b, float e_next, const SolveConst& k) {
+template <bool CONV, bool LEFT = !CONV>
+__device__ __forceinline__ bool no_crossing(float a, float b, float e_start, float e_next, const SolveConst& k) {
     const float ab = fabsf(b);
     const bool usable = k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && a <= 0x1p60f;
     const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), k.c);
@@ -82,7 +91,15 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_next, cons
     float err = 0x1p-21f * fmaf(fmaf(k.c, Z, b), Z, a);           // |rounding| + |sqrt(B2) - b| Z
     if (CONV) err = fmaf(0x1p-23f * B2, k.inv_c, err);
     const bool right_of_window = Z < 2981.0f && (2.0f * k.c) * Z < b * (1.0f - 0x1p-21f) && q > err;
-    return usable && (level1 || right_of_window);
+    bool left_of_window = false;
+    if (LEFT && !CONV) {
+        const float Zl = e_start * (1.0f - 0x1p-17f);
+        const float ql = fmaf(fmaf(k.c, Zl, -b), Zl, a);
+        const float errl = 0x1p-21f * fmaf(fmaf(k.c, Zl, b), Zl, a);
+        left_of_window = Zl > 0.0f && Zl < 2981.0f &&
+                         (ql < -errl || (ql > errl && (2.0f * k.c) * Zl > b * (1.0f + 0x1p-21f)));
+    }
+    return usable && (level1 || right_of_window || left_of_window);
 }
 
 // Threshold-crossing solver of the current-based LIF neuron after an input event.
@@ -91,8 +108,8 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_next, cons
 // c = theta/tau. The next crossing is z = 2a / (b + sqrt(b^2 - 4ac)), t = tau*ln z, accepted in
 // the window (last_t, min(next_t, max_sim)]. Each accepted spike applies the reset
 // b -= (dtheta/tau) * z and the search repeats until no crossing remains or k_post spikes
-// have been written. Returns true when the spike buffer is full. e_next is exp(t_next/tau), used only
-// by no_crossing.
+// have been written. Returns true when the spike buffer is full. e_start and e_next are exp(t/tau) of
+// the window's first event and of the next event, used only by no_crossing (e_start 0: not known).
 //
 // The arithmetic after the no_crossing test gives results bit-identical to the reference solver
 // (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 for the FC layer,
@@ -100,12 +117,12 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_next, cons
 // instead of double): the FC discriminant through fc_discriminant, which reproduces the reference's
 // double expression without FP64 on its common path, everything else operation for operation.
 template <bool CONV>
-__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_next,
+__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_start, float e_next,
                                                 const SolveConst& k, int& n, int k_post,
                                                 float* __restrict__ a_out, float* __restrict__ x_out,
                                                 float* __restrict__ t_out, float* __restrict__ z_out) {
     while (true) {
-        if (no_crossing<CONV>(a, b, e_next, k)) return false;
+        if (no_crossing<CONV>(a, b, e_start, e_next, k)) return false;
         float tmp;
         if (CONV) {
             tmp = b * b - 4 * a * k.c;

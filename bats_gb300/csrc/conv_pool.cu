@@ -110,7 +110,7 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
             const int dx = (e.xyc & 1023) - xo, dy = ((e.xyc >> 10) & 1023) - yo;
             if (dx < 0 || dx >= fx || dy < 0 || dy >= fy) continue;
             if (has_prev) {
-                done = solve_crossings<true>(a, b, last_t, e.t, e.e, sk, n, k_post, ao, xo_, to, zo);
+                done = solve_crossings<true>(a, b, last_t, e.t, 0.0f, e.e, sk, n, k_post, ao, xo_, to, zo);
                 if (done) break;
             }
             const float w = Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)];
@@ -122,7 +122,7 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
     }
     if (active) {
         if (has_prev && !done)
-            solve_crossings<true>(a, b, last_t, BATS_INF, BATS_INF, sk, n, k_post, ao, xo_, to, zo);
+            solve_crossings<true>(a, b, last_t, BATS_INF, 0.0f, BATS_INF, sk, n, k_post, ao, xo_, to, zo);
         n_spikes[(long long)s * n_post + post] = n;
         for (int k = n; k < k_post; ++k) {
             to[k] = BATS_INF;

@@ -82,7 +82,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
                 aa = in ? a2 : aa;
                 bb = in ? b2 : bb;
                 const float e_next = (m0 + u + 1 < E) ? e_nx : BATS_INF;
-                const bool maybe = !no_crossing<false>(aa, bb, e_next, sk);
+                const bool maybe = !no_crossing<false, false>(aa, bb, e4.w, e_next, sk);
                 cand |= (in && maybe) ? (1u << u) : 0u;
             }
             if (cand == 0u) {
@@ -105,7 +105,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
                     const bool has_next = m0 + u + 1 < E;
                     const float t_next = has_next ? se[u + 1].t : BATS_INF;
                     const float e_next = has_next ? se[u + 1].e : BATS_INF;
-                    done = solve_crossings<false>(a, b, e.t, t_next, e_next, sk, n, k_post, ao, xo, to, zo);
+                    done = solve_crossings<false>(a, b, e.t, t_next, e.e, e_next, sk, n, k_post, ao, xo, to, zo);
                     if (done) break;
                 }
             }
@@ -119,6 +119,130 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
             zo[q] = BATS_INF;
         }
     }
+}
+
+// Event-parallel variant for layers with little neuron parallelism (few post neurons, or a small
+// batch with long event streams): one warp per (sample, post neuron), the 32 lanes taking 32
+// consecutive events. Per block of 32 events:
+//   1. the states after each event are formed by the reference's sequential FMA chain
+//      (a = fma(w, e^{t/tau_s}, a), b = fma(w, e^{t/tau}, b), event order), every lane running the
+//      same chain over the block's (w, exponentials) in warp-private shared memory and keeping the
+//      state after its own event;
+//   2. every lane evaluates the provable no-crossing test on its own state at once (one ballot);
+//   3. candidates are taken in event order by their lane with the exact solver; a spike's reset
+//      changes b for the later events of the block, whose b chain is then re-run from the spiking
+//      event (a is unaffected by resets) and whose tests are re-evaluated.
+// The arithmetic per event is that of the reference's loop, so results are bit-identical to the
+// tile kernel's. The warp is latency-bound rather than issue-bound: a 32-event block costs about 230
+// instructions for one neuron, against the tile kernel's ~100 per 32 neurons and event, so the
+// variant pays off when B * N_post is small against the GPU's ~5000 resident warps.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32)
+lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
+                            const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
+                            int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
+                            float* __restrict__ t_out, float* __restrict__ z_out) {
+    __shared__ float4 blk[WARPS][32];  // (w, es, e, -) of the block's events
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int s = blockIdx.y;
+    const int i = blockIdx.x * WARPS + warp;
+    if (i >= n_post) return;  // whole warp
+    const int E = ev_count[s];
+    const Event* evs = ev + (long long)s * ev_cap;
+    const long long obase = ((long long)s * n_post + i) * k_post;
+    float* ao = a_out + obase;
+    float* xo = x_out + obase;
+    float* to = t_out + obase;
+    float* zo = z_out + obase;
+    float4* my = blk[warp];
+    float a = 0.0f, b = 0.0f;
+    int n = 0;
+    bool done = false;
+    for (int m0 = 0; m0 < E && !done; m0 += 32) {
+        const int m = m0 + lane;
+        const int cnt = min(32, E - m0);
+        const bool in = lane < cnt;
+        float4 e4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // (t, j, es, e)
+        float w = 0.0f;
+        if (in) {
+            e4 = __ldg(reinterpret_cast<const float4*>(evs + m));
+            w = __ldg(wt + (long long)__float_as_int(e4.y) * ld + i);
+        }
+        // Window end: the next event's time and exponential (+inf after the last event).
+        float t_nx = __shfl_down_sync(0xffffffffu, e4.x, 1);
+        float e_nx = __shfl_down_sync(0xffffffffu, e4.w, 1);
+        if (lane == 31 && m0 + 32 < E) {
+            const float4 nx = __ldg(reinterpret_cast<const float4*>(evs + m0 + 32));
+            t_nx = nx.x;
+            e_nx = nx.w;
+        }
+        if (m + 1 >= E) {
+            t_nx = BATS_INF;
+            e_nx = BATS_INF;
+        }
+        // 1. sequential chain; lanes past the block's end carry w = 0, which leaves a and b unchanged.
+        my[lane] = make_float4(w, e4.z, e4.w, 0.0f);
+        __syncwarp();
+        float am = 0.0f, bm = 0.0f, ca = a, cb = b;
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            const float4 q = my[k];
+            ca = fmaf(q.x, q.y, ca);
+            cb = fmaf(q.x, q.z, cb);
+            am = (lane == k) ? ca : am;
+            bm = (lane == k) ? cb : bm;
+        }
+        // 2. provable no-crossing tests of all lanes at once.
+        unsigned cand = __ballot_sync(0xffffffffu, in && !no_crossing<false>(am, bm, e4.w, e_nx, sk));
+        // 3. candidates in event order.
+        while (cand) {
+            const int u = __ffs(cand) - 1;
+            int spiked = 0;
+            int full = 0;
+            if (lane == u) {
+                const int n0 = n;
+                full = solve_crossings<false>(am, bm, e4.x, t_nx, e4.w, e_nx, sk, n, k_post, ao, xo, to, zo) ? 1 : 0;
+                spiked = n - n0;
+            }
+            n = __shfl_sync(0xffffffffu, n, u);
+            spiked = __shfl_sync(0xffffffffu, spiked, u);
+            if (__shfl_sync(0xffffffffu, full, u)) {
+                done = true;
+                break;
+            }
+            if (spiked) {
+                float cb2 = __shfl_sync(0xffffffffu, bm, u);
+                for (int k = u + 1; k < cnt; ++k) {
+                    const float4 q = my[k];
+                    cb2 = fmaf(q.x, q.z, cb2);
+                    bm = (lane == k) ? cb2 : bm;
+                }
+                cand = __ballot_sync(0xffffffffu, in && lane > u && !no_crossing<false>(am, bm, e4.w, e_nx, sk));
+            } else {
+                cand &= cand - 1u;
+            }
+        }
+        a = __shfl_sync(0xffffffffu, am, cnt - 1);
+        b = __shfl_sync(0xffffffffu, bm, cnt - 1);
+        __syncwarp();
+    }
+    if (lane == 0) n_spikes[(long long)s * n_post + i] = n;
+    for (int q = n + lane; q < k_post; q += 32) {
+        to[q] = BATS_INF;
+        zo[q] = BATS_INF;
+    }
+}
+
+template <int WARPS>
+static int launch_forward_lanes(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld,
+                                int batch, int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a,
+                                float* x, float* times, float* post_exp_tau, cudaStream_t stream) {
+    dim3 grid((n_post + WARPS - 1) / WARPS, batch);
+    lif_fc_forward_lanes_kernel<WARPS><<<grid, WARPS * 32, 0, stream>>>(
+        reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
+        post_exp_tau);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
 }
 
 template <int TILE, int SEV, int STAGES>
@@ -150,18 +274,23 @@ SolveConst make_solve_const(float c, float dtt, float tau, float max_sim) {
 
 }  // namespace bats
 
-extern "C" int bats_lif_forward_fc(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
-                                   int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau,
-                                   float tau, float max_simulation, int* n_spikes, float* a, float* x, float* times,
-                                   float* post_exp_tau, cudaStream_t stream) {
+static int forward_fc_impl(const void* events, const int* ev_count, long long ev_cap, const float* weights_t, int ld,
+                           int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,
+                           float max_simulation, int* n_spikes, float* a, float* x, float* times, float* post_exp_tau,
+                           int algo, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0 && ld >= n_post && ld % 4 == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc: bad shape (ld must be >= n_post and a multiple of 4)");
+    BATS_REQUIRE(algo >= BATS_FWD_AUTO && algo <= BATS_FWD_LANES, BATS_ERR_BAD_SHAPE, "lif_forward_fc: unknown algo");
     if (batch == 0 || n_post == 0) return BATS_OK;
     BATS_REQUIRE(events && ev_count && weights_t && n_spikes && a && x && times && post_exp_tau, BATS_ERR_NULL,
                  "lif_forward_fc: null pointer");
     BATS_REQUIRE(((uintptr_t)weights_t & 15) == 0 && ((uintptr_t)events & 15) == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc: weights_t and events must be 16-byte aligned");
     const bats::SolveConst sk = bats::make_solve_const(c, delta_theta_tau, tau, max_simulation);
+    if (algo == BATS_FWD_AUTO) algo = bats_lif_forward_fc_default_algo(batch, n_post, (int)(ev_cap < (1LL << 30) ? ev_cap : (1LL << 30)));
+    if (algo == BATS_FWD_LANES)
+        return bats::launch_forward_lanes<4>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+                                             n_spikes, a, x, times, post_exp_tau, stream);
     int* status = nullptr;
     BATS_CUDA((cudaError_t)bats::device_status(&status));
     if (n_post <= 32)
@@ -172,4 +301,29 @@ extern "C" int bats_lif_forward_fc(const void* events, const int* ev_count, long
                                               n_spikes, a, x, times, post_exp_tau, status, stream);
     return bats::launch_forward<128, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                            n_spikes, a, x, times, post_exp_tau, status, stream);
+}
+
+extern "C" int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap) {
+    (void)ev_cap;
+    // Warp per (sample, neuron) when that gives fewer warps than about four per SM sub-partition of a
+    // 152-SM GPU, or the layer has so few neurons that the tile kernel would idle most of its lanes.
+    const long long warps = (long long)batch * n_post;
+    return (n_post <= 16 || warps <= 152LL * 4 * 4) ? BATS_FWD_LANES : BATS_FWD_TILE;
+}
+
+extern "C" int bats_lif_forward_fc(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
+                                   int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau,
+                                   float tau, float max_simulation, int* n_spikes, float* a, float* x, float* times,
+                                   float* post_exp_tau, cudaStream_t stream) {
+    return forward_fc_impl(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, c, delta_theta_tau, tau,
+                           max_simulation, n_spikes, a, x, times, post_exp_tau, BATS_FWD_AUTO, stream);
+}
+
+extern "C" int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long ev_cap,
+                                        const float* weights_t, int ld, int batch, int n_post, int k_post, float c,
+                                        float delta_theta_tau, float tau, float max_simulation, int* n_spikes,
+                                        float* a, float* x, float* times, float* post_exp_tau, int algo,
+                                        cudaStream_t stream) {
+    return forward_fc_impl(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, c, delta_theta_tau, tau,
+                           max_simulation, n_spikes, a, x, times, post_exp_tau, algo, stream);
 }

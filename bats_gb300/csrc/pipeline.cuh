@@ -1,18 +1,26 @@
 // mbarrier + bulk-copy (TMA engine, non-tensor form) helpers in inline PTX for sm_90+/sm_103a.
 //
-// Every wait is bounded: after BATS_WAIT_LIMIT polls it gives up, raises the CTA abort flag and the
-// global status word, and returns false, so a lost copy or a missing arrival never hangs the GPU.
+// Every wait is bounded: after BATS_WAIT_NS of global time it gives up, raises the CTA abort flag and
+// the global status word, and returns false, so a lost copy or a missing arrival never hangs the GPU.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace bats {
 
-constexpr long long BATS_WAIT_LIMIT = 1LL << 24;  // polls; each try_wait may also suspend briefly
+constexpr unsigned long long BATS_WAIT_NS = 2000000000ull;  // give up after 2 s of waiting
+constexpr uint32_t BATS_SUSPEND_NS = 2000;                   // per try_wait: sleep until the phase completes,
+                                                             // at most this long
 constexpr int BATS_STATUS_TIMEOUT = 1;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -32,24 +40,31 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
+// One test of the phase; the thread may be suspended (not issuing) until the phase completes or the
+// hint expires, so that waiting warps leave the issue slots to the working ones.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(BATS_SUSPEND_NS)
         : "memory");
     return ok != 0;
 }
 
 // Bounded wait on one phase of an mbarrier. `abort` is a CTA-shared flag raised by any thread that
-// gives up; `status` (may be null) receives BATS_STATUS_TIMEOUT.
+// gives up; `status` (may be null) receives BATS_STATUS_TIMEOUT. Ends after BATS_WAIT_NS of global time.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, int* status) {
-    for (long long it = 0; it < BATS_WAIT_LIMIT; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255) == 255 && *abort) return false;
+        if ((it & 15) == 0) {
+            if (*abort) return false;
+            if (global_ns() - t0 > BATS_WAIT_NS) break;
+        }
     }
     *abort = 1;
     if (status) atomicOr(status, BATS_STATUS_TIMEOUT);

@@ -145,10 +145,15 @@ def get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron):
     return (B, N * K), idx, reshaped
 
 
+FWD_AUTO, FWD_TILE, FWD_LANES = 0, 1, 2
+
+
 def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: float, theta: float,
-                   delta_theta: float, max_simulation: float = float("inf"), outs=None):
+                   delta_theta: float, max_simulation: float = float("inf"), outs=None, algo: int = FWD_AUTO):
     """FC LIF forward (replaces get_spike_weights + compute_spike_times,
-    bats/CudaKernels/Wrappers/Inference/compute_spike_times.py:11-32). Returns n, a, x, times, post_exp_tau."""
+    bats/CudaKernels/Wrappers/Inference/compute_spike_times.py:11-32). Returns n, a, x, times, post_exp_tau.
+    algo: FWD_TILE (CTA per neuron tile and sample), FWD_LANES (warp per neuron and sample, 32 events in
+    parallel) or FWD_AUTO; all give identical results."""
     B = events.batch
     tau32, c, dtt = lif_constants(tau_s, theta, delta_theta)
     dev = events.events.device
@@ -156,9 +161,9 @@ def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: f
         outs = (torch.empty((B, n_post), dtype=I32, device=dev),
                 *(torch.empty((B, n_post, k_post), dtype=F32, device=dev) for _ in range(4)))
     n, a, x, t, z = outs
-    call("bats_lif_forward_fc", ptr(events.events), ptr(events.counts), events.cap, ptr(weights_t),
+    call("bats_lif_forward_fc_algo", ptr(events.events), ptr(events.counts), events.cap, ptr(weights_t),
          weights_t.shape[1], B, n_post, k_post, float(c), float(dtt), float(tau32), float(np.float32(max_simulation)),
-         ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), stream_ptr())
+         ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), int(algo), stream_ptr())
     return n, a, x, t, z
 
 

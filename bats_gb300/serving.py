@@ -7,10 +7,13 @@ transposed weights are uploaded once. Whenever a lane is free and requests are w
 requests (up to max_batch, oldest first) are packed and launched on that lane: host -> device copy,
 event-list -> spike-train conversion, and per layer the event sort and the LIF forward, then the output
 spike counts and times are copied back. Several lanes are in flight at once, so requests that arrive while
-others are on the GPU start as soon as a lane frees up and their work overlaps on the device. The number
-of lanes is set from the free HBM reported by the driver (cudaMemGetInfo) at start-up, and every
-admission re-checks it. A request's result does not depend on which other requests share its batch (the
-kernels treat samples independently), which tests/test_gpu_serving.py checks bit for bit.
+others are on the GPU start as soon as a lane frees up and their work overlaps on the device. The lane
+pool starts with one lane and grows, while every lane is busy and requests wait, up to max_lanes, each new
+lane only if the free HBM reported by the driver (cudaMemGetInfo) leaves room for it; admission refuses
+requests when free HBM (re-read at most every 5 ms) falls below a floor or the queue is full. The forward
+kernel variant of every layer is chosen per batch-size bucket by autotune(). A request's result does not
+depend on which other requests share its batch (the kernels treat samples independently), which
+tests/test_gpu_serving.py checks bit for bit.
 """
 from __future__ import annotations
 
@@ -24,6 +27,7 @@ import torch
 
 from . import kernels as K
 from ._lib import call, ptr
+from .autotune import Autotuner, get_tuner
 
 
 @dataclass
@@ -83,6 +87,12 @@ class _Lane:
         self.h_overflow = torch.empty((1,), dtype=i32, pin_memory=True)
         self.done = torch.cuda.Event()
         self.batch: List[Request] = []
+        # numpy views of the pinned buffers (no per-request torch calls on the host path)
+        self.np_idx = self.h_idx.numpy().reshape(-1)
+        self.np_t = self.h_t.numpy().reshape(-1)
+        self.np_counts = self.h_counts.numpy()
+        self.np_times = self.h_times.numpy()
+        self.np_overflow = self.h_overflow.numpy()
 
     def busy(self) -> bool:
         return bool(self.batch) and not self.done.query()
@@ -103,7 +113,7 @@ class _Lane:
 class InferenceServer:
     def __init__(self, weights: Sequence, specs: Sequence[LayerSpec], n_inputs: int, max_events: int,
                  k_in: int = 32, max_batch: int = 64, max_lanes: int = 4, hbm_fraction: float = 0.5,
-                 max_simulation: float = float("inf"), device="cuda"):
+                 max_simulation: float = float("inf"), max_pending: int = 1 << 16, device="cuda"):
         self.dev = torch.device(device)
         self.specs = list(specs)
         self.n_inputs, self.max_events, self.k_in = int(n_inputs), int(max_events), int(k_in)
@@ -121,35 +131,57 @@ class InferenceServer:
                                                          n_prev, k_prev))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
         self.lane_bytes = _Lane.bytes_needed(self)
-        free, _ = torch.cuda.mem_get_info(self.dev)
-        n_lanes = int(min(max_lanes, max(1, (free * self.hbm_fraction) // self.lane_bytes)))
-        self.lanes = [_Lane(self, self.dev) for _ in range(n_lanes)]
+        self.max_lanes = int(max_lanes)
+        self.max_pending = int(max_pending)
+        self._free_hbm, self._free_t = 0, -1.0
+        if self._free_hbm_now(force=True) * self.hbm_fraction < self.lane_bytes:
+            raise RuntimeError(f"not enough free HBM for one lane ({self.lane_bytes} bytes)")
+        self.lanes = [_Lane(self, self.dev)]
         self.pending: Deque[Request] = collections.deque()
         self.results: Dict[int, Result] = {}
         self.rejected: List[int] = []
         self.batches_launched = 0
+        self.algo_table: Dict[int, List[int]] = {}
 
     # -- admission --------------------------------------------------------------------------------------
+    HBM_FLOOR = 64 * 1024 * 1024  # free HBM kept for the rest of the process
+
+    def _free_hbm_now(self, force: bool = False) -> int:
+        """Free device memory from the driver, re-read at most every 5 ms."""
+        now = time.perf_counter()
+        if force or now - self._free_t > 0.005:
+            self._free_hbm, _ = torch.cuda.mem_get_info(self.dev)
+            self._free_t = now
+        return self._free_hbm
+
     def submit(self, req: Request, now: Optional[float] = None) -> bool:
-        """Queue a request; refused (False) if it exceeds the lane capacity or free HBM is exhausted."""
+        """Queue a request; refused (False) if it exceeds the lane capacity, the queue is full, or free HBM
+        is below the floor."""
         req.t_arrival = time.perf_counter() if now is None else now
-        if len(req.indices) > self.max_events or len(req.indices) != len(req.times):
-            self.rejected.append(req.rid)
-            return False
-        free, _ = torch.cuda.mem_get_info(self.dev)
-        if free < 64 * 1024 * 1024:  # keep a floor of free HBM for the rest of the process
+        if (len(req.indices) > self.max_events or len(req.indices) != len(req.times)
+                or len(self.pending) >= self.max_pending or self._free_hbm_now() < self.HBM_FLOOR):
             self.rejected.append(req.rid)
             return False
         self.pending.append(req)
         return True
+
+    def _grow(self) -> Optional[_Lane]:
+        """A new lane when every lane is busy, requests wait and free HBM allows it."""
+        if len(self.lanes) >= self.max_lanes:
+            return None
+        if self._free_hbm_now(force=True) * self.hbm_fraction < self.lane_bytes + self.HBM_FLOOR:
+            return None
+        lane = _Lane(self, self.dev)
+        self.lanes.append(lane)
+        return lane
 
     # -- device work ------------------------------------------------------------------------------------
     def _launch(self, lane: _Lane, batch: List[Request]) -> None:
         B = len(batch)
         L = max(1, max(len(r.indices) for r in batch))
         # Pack the batch contiguously as (B, L); a sample ends at its first negative index.
-        hi = lane.h_idx.view(-1)[:B * L].view(B, L).numpy()
-        ht = lane.h_t.view(-1)[:B * L].view(B, L).numpy()
+        hi = lane.np_idx[:B * L].reshape(B, L)
+        ht = lane.np_t[:B * L].reshape(B, L)
         for q, r in enumerate(batch):
             n = len(r.indices)
             hi[q, :n] = r.indices
@@ -166,38 +198,89 @@ class InferenceServer:
             lane.overflow.zero_()
             call("bats_events_to_trains", ptr(d_idx), ptr(d_t), B, L, self.n_inputs, self.k_in,
                  ptr(lane.trains), ptr(lane.train_counts), ptr(lane.overflow), s)
-            pre = lane.trains
-            for li, spec in enumerate(self.specs):
-                ev = lane.ev[li]
-                tau32, c, dtt = self.consts[li]
-                call("bats_sort_events", ptr(pre), B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)),
-                     float(tau32), None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), None, None, 0,
-                     ptr(lane.ws), lane.ws.numel(), s)
-                n, a, x, t, z = lane.out[li]
-                call("bats_lif_forward_fc", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.wt[li]),
-                     self.wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt), float(tau32),
-                     float(np.float32(self.max_sim)), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), s)
-                pre = t
+            self._layers(lane, B, self._algos_for(B), s)
             lane.h_counts[:B].copy_(lane.out[-1][0][:B], non_blocking=True)
             lane.h_times[:B].copy_(lane.out[-1][3][:B], non_blocking=True)
             lane.h_overflow.copy_(lane.overflow, non_blocking=True)
             lane.done.record(lane.stream)
         self.batches_launched += 1
 
+    def _layers(self, lane: _Lane, B: int, algos: Sequence[int], s: int, only: Optional[int] = None) -> None:
+        """Per layer: event sort of the previous layer's spike trains, then the LIF forward with the given
+        kernel variant. With `only`, just that layer's forward (used by the autotuner)."""
+        pre = lane.trains
+        for li, spec in enumerate(self.specs):
+            ev = lane.ev[li]
+            tau32, c, dtt = self.consts[li]
+            if only is None:
+                call("bats_sort_events", ptr(pre), B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)),
+                     float(tau32), None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), None, None, 0,
+                     ptr(lane.ws), lane.ws.numel(), s)
+            n, a, x, t, z = lane.out[li]
+            if only is None or only == li:
+                call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.wt[li]),
+                     self.wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt), float(tau32),
+                     float(np.float32(self.max_sim)), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), int(algos[li]), s)
+            pre = t
+
+    @staticmethod
+    def _bucket(B: int) -> int:
+        return 1 << max(0, int(B - 1).bit_length())
+
+    def _algos_for(self, B: int) -> List[int]:
+        return self.algo_table.get(self._bucket(B), [K.FWD_AUTO] * len(self.specs))
+
+    def autotune(self, requests: Sequence[Request], tuner: Optional[Autotuner] = None) -> Dict[int, List[str]]:
+        """Per batch-size bucket (powers of two up to max_batch) and layer, the faster forward kernel variant,
+        timed on batches drawn from `requests` (cycled) on the first lane."""
+        tuner = tuner or get_tuner()
+        lane = self.lanes[0]
+        s = lane.stream.cuda_stream
+        out = {}
+        b = 1
+        while b <= self.max_batch:
+            batch = [requests[q % len(requests)] for q in range(b)]
+            self._launch(lane, batch)
+            lane.done.synchronize()
+            self._collect(lane)
+            names = []
+            algos = list(self._algos_for(b))
+            with torch.cuda.stream(lane.stream):
+                for li, spec in enumerate(self.specs):
+                    ev_mean = max(1, int(lane.ev[li].counts[:b].float().mean().item()))
+                    shape = (b, lane.ev[li].n_neurons, lane.ev[li].k, spec.n_neurons, spec.max_n_spike,
+                             int(np.log2(ev_mean)))
+
+                    def run(algo, li=li):
+                        trial = list(algos)
+                        trial[li] = algo
+                        self._layers(lane, b, trial, s, only=li)
+
+                    best = tuner.pick("fc_forward", shape, {"tile": lambda: run(K.FWD_TILE),
+                                                             "lanes": lambda: run(K.FWD_LANES)})
+                    algos[li] = K.FWD_TILE if best == "tile" else K.FWD_LANES
+                    names.append(best)
+            torch.cuda.synchronize()
+            self.algo_table[b] = algos
+            out[b] = names
+            b *= 2
+        return out
+
     def _collect(self, lane: _Lane) -> List[Result]:
         now = time.perf_counter()
         out = []
-        if int(lane.h_overflow[0]) != 0:
+        if int(lane.np_overflow[0]) != 0:
             raise RuntimeError("a request has more spikes on one input neuron than the server's k_in")
         for q, r in enumerate(lane.batch):
-            res = Result(r.rid, lane.h_counts[q].numpy().copy(), lane.h_times[q].numpy().copy(), r.t_arrival, now)
+            res = Result(r.rid, lane.np_counts[q].copy(), lane.np_times[q].copy(), r.t_arrival, now)
             self.results[r.rid] = res
             out.append(res)
         lane.batch = []
         return out
 
     def pump(self) -> List[Result]:
-        """Collect finished lanes and launch pending requests on free lanes. Non-blocking."""
+        """Collect finished lanes and launch pending requests on free lanes (growing the lane pool while
+        free HBM allows). Non-blocking."""
         done = []
         for lane in self.lanes:
             if lane.batch and lane.done.query():
@@ -207,8 +290,12 @@ class InferenceServer:
                 break
             if lane.batch:
                 continue
-            batch = [self.pending.popleft() for _ in range(min(self.max_batch, len(self.pending)))]
-            self._launch(lane, batch)
+            self._launch(lane, [self.pending.popleft() for _ in range(min(self.max_batch, len(self.pending)))])
+        while self.pending:
+            lane = self._grow()
+            if lane is None:
+                break
+            self._launch(lane, [self.pending.popleft() for _ in range(min(self.max_batch, len(self.pending)))])
         return done
 
     def drain(self) -> List[Result]:

@@ -17,6 +17,7 @@ import torch
 
 from . import kernels as K
 from ._lib import call, ptr, stream_ptr
+from .autotune import Autotuner, get_tuner
 
 
 @dataclass
@@ -90,6 +91,7 @@ class FCTrainStep:
         self.h_times = torch.empty(self.in_times.shape, dtype=f32, pin_memory=True)
         self.h_labels = torch.empty((B,), dtype=i32, pin_memory=True)
         self.h_loss = torch.empty((B,), dtype=f32, pin_memory=True)
+        self.fwd_algo = [K.FWD_AUTO] * len(self.specs)
         self.launches = self._build_launches()
         self.launches_per_step = self._count_launches()
 
@@ -110,9 +112,10 @@ class FCTrainStep:
                 K.BUCKET_WIDTH, ws, wsb, s)))
             n, a, x, t, z = self.out[li]
             L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
-                      call("bats_lif_forward_fc", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
+                      call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
                            self.Wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt),
-                           float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o), s)))
+                           float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o), self.fwd_algo[li],
+                           s)))
             pre_times = t
         n_out = self.out[-1][0]
         L.append(("loss", lambda s: call("bats_spike_count_loss", ptr(n_out), 0, None, ptr(self.labels),
@@ -130,11 +133,10 @@ class FCTrainStep:
                       call("bats_backward_prep_layer", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]), ptr(e), B,
                            spec.n_neurons, spec.max_n_spike, float(c), float(tau32), float(dtt), ptr(tb.f1),
                            ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
-            grp = self.groups[li]
-            L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, grp=grp: call(
+            L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
                 "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
                 ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,
-                grp, 1, ptr(self.grad[li]), ws, wsb, s)))
+                self.groups[li], 1, ptr(self.grad[li]), ws, wsb, s)))
             if li > 0:
                 pe = self.pre_err[li]
                 L.append((f"{tag}.pre_err", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, pe=pe, tau32=tau32: call(
@@ -166,6 +168,59 @@ class FCTrainStep:
         for _, fn in self.launches:
             fn(s)
         self.t += 1
+
+    def autotune(self, tuner: Optional[Autotuner] = None, force: bool = False) -> dict:
+        """Pick, per layer, the forward kernel variant and the samples per partial gradient by timing the
+        candidates on this step's own buffers (after one forward/backward pass without the optimizer, so
+        the weights are unchanged). Call before try_capture. Returns the choices."""
+        tuner = tuner or get_tuner()
+        s = stream_ptr()
+        for name, fn in self.launches:
+            if not name.endswith("adam") and name != "adam.powers":
+                fn(s)
+        torch.cuda.synchronize()
+        B = self.B
+        choice = {}
+        n_prev = self.in_times.shape[1]
+        k_prev = self.in_times.shape[2]
+        fwd = {nm: fn for nm, fn in self.launches if nm.endswith(".forward")}
+        grad = {nm: fn for nm, fn in self.launches if nm.endswith(".grad")}
+        wsb = self.ws.numel()
+        for li, spec in enumerate(self.specs):
+            tag = f"L{li + 1}"
+            ev_mean = max(1, int(self.ev[li].counts.float().mean().item()))
+            bucket = int(np.log2(ev_mean))
+            shape = (B, n_prev, k_prev, spec.n_neurons, spec.max_n_spike, bucket)
+
+            def run_fwd(algo, li=li):
+                saved = self.fwd_algo[li]
+                self.fwd_algo[li] = algo
+                fwd[f"{tag}.forward"](s)
+                self.fwd_algo[li] = saved
+
+            best = tuner.pick("fc_forward", shape, {"tile": lambda: run_fwd(K.FWD_TILE),
+                                                     "lanes": lambda: run_fwd(K.FWD_LANES)}, force=force)
+            self.fwd_algo[li] = K.FWD_TILE if best == "tile" else K.FWD_LANES
+            cands = {}
+            for parts in (4, 8, 16, 32):
+                g = max(2, -(-B // parts))
+                if K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev, g) <= wsb:
+                    cands[str(g)] = g
+            if len(cands) > 1:
+                def run_grad(g, li=li):
+                    saved = self.groups[li]
+                    self.groups[li] = g
+                    grad[f"{tag}.grad"](s)
+                    self.groups[li] = saved
+
+                bg = tuner.pick("fc_grad_group", shape, {k: (lambda g=g: run_grad(g)) for k, g in cands.items()},
+                                force=force)
+                self.groups[li] = cands[bg]
+            choice[tag] = {"forward": best, "grad_group": self.groups[li]}
+            n_prev, k_prev = spec.n_neurons, spec.max_n_spike
+        torch.cuda.synchronize()
+        self.tuned = choice
+        return choice
 
     def try_capture(self) -> bool:
         """Record one step as a CUDA graph (after an eager warm-up step); False if capture fails."""

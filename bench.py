@@ -246,8 +246,11 @@ def run_ours(args, dist, rank, world):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
     result = {}
-    for variant in ("literal", "active"):
+    variants = ("literal", "active") if args.workload == "all" else (
+        (args.workload,) if args.workload in ("literal", "active") else ())
+    for variant in variants:
         ts = build_train_step(variant)
+        tuned = ts.autotune()
         graphed = ts.try_capture()
         fn = ts.replay if graphed else ts.step
         with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
@@ -277,7 +280,8 @@ def run_ours(args, dist, rank, world):
             e2e = {"value": world * B * args.steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": ts.h2d_bytes,
                    "d2h_bytes_per_step": ts.d2h_bytes}
         result[variant] = {
-            "value": sps, "ms_per_step": ms / args.steps, "graph": graphed, "clocks": clocks, "e2e": e2e,
+            "value": sps, "ms_per_step": ms / args.steps, "graph": graphed, "autotuned": tuned, "clocks": clocks,
+            "e2e": e2e,
             "spikes_per_layer_last_step": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
@@ -288,8 +292,9 @@ def run_ours(args, dist, rank, world):
         del ts
         torch.cuda.empty_cache()
     # Plain (layer-by-layer) drop-in API and the reference kernels, active regime (few steps).
-    result["active"]["plain_api"] = plain_api_rate("active", max(2, args.steps // 4), flush)
-    result["active"]["refkern"] = refkern_rate("active", 2, flush)
+    if args.workload == "all":
+        result["active"]["plain_api"] = plain_api_rate("active", max(2, args.steps // 4), flush)
+        result["active"]["refkern"] = refkern_rate("active", 2, flush)
     return result
 
 
@@ -378,6 +383,7 @@ def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float =
     ws, specs = make_network()
     server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=64, max_lanes=4)
     pool = make_requests(1000, seed=7)
+    tuned = server.autotune(pool[:64])
 
     def batch_of(n, rid0):
         return [dataclasses.replace(pool[q % len(pool)], rid=rid0 + q) for q in range(n)]
@@ -400,6 +406,7 @@ def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float =
             "peak_throughput_rps": peak, "load_rps": rate, "load_fraction": load, "n_requests": n_p,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
             "lanes": len(server.lanes), "max_batch": server.max_batch, "rejected": len(server.rejected),
+            "forward_variant_per_batch_bucket": tuned,
             "batches": server.batches_launched}
 
 
@@ -410,6 +417,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--workload", default="all", choices=["all", "literal", "active", "serving"],
+                    help="all (default): every measurement; otherwise only that one (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -429,7 +439,7 @@ def main():
         return
 
     # CPU baseline first (spawned workers, before any GPU context exists in this process).
-    cb = cpu_baseline("active", budget_s=args.cpu_budget) if rank == 0 else None
+    cb = cpu_baseline("active", budget_s=args.cpu_budget) if rank == 0 and not args.no_cpu else None
 
     dist = None
     if world > 1:
@@ -437,8 +447,14 @@ def main():
         dist_mod.init_process_group("nccl")
         dist = dist_mod
     res = run_ours(args, dist, rank, world)
-    serving = serving_bench()
+    serving = serving_bench() if args.workload in ("all", "serving") else None
     if rank != 0:
+        return
+    if args.workload != "all":
+        head = res.get(args.workload, {})
+        print(json.dumps({"metric": METRIC, "workload": args.workload, "value": head.get("value"),
+                          "unit": "samples/s", "steps": args.steps, "warmup": args.warmup, "detail": head,
+                          "serving": serving}))
         return
     lit, act = res["literal"], res["active"]
     line = {

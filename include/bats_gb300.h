@@ -78,6 +78,20 @@ int bats_lif_forward_fc(const void* events, const int* ev_count, long long ev_ca
                         float max_simulation, int* n_spikes, float* a, float* x, float* times, float* post_exp_tau,
                         cudaStream_t stream);
 
+/* Kernel choice of the FC forward: BATS_FWD_TILE runs one CTA per (post-neuron tile, sample) with a
+ * producer warp streaming weight rows (throughput-oriented, large B * N_post); BATS_FWD_LANES runs one warp
+ * per (sample, post neuron) with 32 events evaluated in parallel (latency-oriented: few neurons, small
+ * batches, long event streams). Both give bit-identical results. BATS_FWD_AUTO picks by
+ * bats_lif_forward_fc_default_algo. No counterpart in the reference (it has one kernel shape). */
+#define BATS_FWD_AUTO 0
+#define BATS_FWD_TILE 1
+#define BATS_FWD_LANES 2
+int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap);
+int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
+                             int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,
+                             float max_simulation, int* n_spikes, float* a, float* x, float* times,
+                             float* post_exp_tau, int algo, cudaStream_t stream);
+
 /* Convolutional LIF forward on a (X, Y, C) input with (C_out, fx, fy, C) filters, valid, stride 1.
  * Replaces compute_spike_times_conv (bats/CudaKernels/Wrappers/Inference/compute_spike_times_conv.py:11-35). */
 int bats_conv_forward(const void* events, const int* ev_count, long long ev_cap, const float* weights, int batch,

@@ -156,3 +156,55 @@ def test_edge_cases(cuda):
     assert np.nanmax(np.where(np.isinf(ours[3]), np.nan, ours[3])) <= np.float32(0.1)
     ref = run_ref(t, n_in, W2, 0.1, 0.05, 0.05, 40, 0.1)
     check_against(ours, ref, None, what="max_simulation")
+
+
+def _both_algos(t, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
+    tt = torch.tensor(t, device="cuda")
+    ev = K.sort_events(tt, np.float32(tau_s), np.float32(2 * tau_s))
+    wt = K.transpose_weights(torch.tensor(W, device="cuda"))
+    outs = []
+    for algo in (K.FWD_TILE, K.FWD_LANES):
+        o = K.lif_forward_fc(ev, wt, W.shape[0], K_post, tau_s, theta, dtheta, max_sim, algo=algo)
+        outs.append([v.cpu().numpy() for v in o])
+    return outs
+
+
+def _assert_identical(p, q, what):
+    n = p[0]
+    assert np.array_equal(n, q[0]), what
+    valid = leading_mask(n, p[3].shape[2])
+    for name, i in (("a", 1), ("x", 2)):
+        assert np.array_equal(p[i][valid].view(np.uint32), q[i][valid].view(np.uint32)), f"{what}: {name}"
+    for name, i in (("t", 3), ("z", 4)):
+        assert np.array_equal(p[i].view(np.uint32), q[i].view(np.uint32)), f"{what}: {name}"
+
+
+@pytest.mark.parametrize("case", ["small", "mnist_active", "long_narrow", "long_wide", "cap_and_cut"])
+def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
+    """The warp-per-neuron forward (32 events per step, FWD_LANES) is bit-identical to the tile kernel on
+    short and long event streams, narrow and wide layers, a full spike buffer and a max_simulation cut; on
+    a long stream it also matches the reference kernels."""
+    rng = np.random.default_rng(5)
+    if case == "small":
+        t, n_in = multi_spike_input(4, 40, 3, 0.3, seed=2)
+        W = rng.normal(0, 1, (16, 40)).astype(np.float32)
+        args = (0.1, 0.1, 0.2, 16, 0.5)
+    elif case == "mnist_active":
+        t, n_in = mnist_like_input(16, seed=3)
+        W = rng.uniform(-1, 1, (800, 784)).astype(np.float32)
+        args = (0.13, 0.2, 0.2, 30, 0.2)
+    elif case in ("long_narrow", "long_wide"):
+        n_post = 20 if case == "long_narrow" else 512
+        t, n_in = multi_spike_input(2, 700, 20, 0.2, seed=4, p_silent=0.1)
+        W = ((rng.normal(0, 1, (n_post, 700)) + 1.5) / np.sqrt(700)).astype(np.float32)
+        args = (0.13, 1.0, 1.0, 30, np.inf)
+    else:
+        t, n_in = multi_spike_input(3, 50, 6, 0.2, seed=6, p_silent=0.0)
+        W = np.abs(rng.normal(0, 1, (40, 50))).astype(np.float32)
+        args = (0.1, 0.05, 0.05, 4, 0.12)
+    tile, lanes = _both_algos(t, W, *args)
+    assert tile[0].sum() > 0, "the case should spike"
+    _assert_identical(tile, lanes, case)
+    if case == "long_narrow":
+        ref = run_ref(t, n_in, W, *args)
+        check_against(lanes, ref, None, what="lanes vs reference kernels")

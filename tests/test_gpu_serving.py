@@ -79,6 +79,20 @@ def test_serving_matches_layer_forward(cuda):
         np.testing.assert_array_equal(r.spike_times, x[q].cpu().numpy())
 
 
+def test_autotuned_variants_give_the_same_results(cuda):
+    """Per-bucket kernel choices change speed only: results equal those of the untuned server."""
+    ws, specs = net()
+    reqs = make_requests(24, seed=5)
+    plain = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=8, max_lanes=2).infer(reqs)
+    tuned_server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=8, max_lanes=2)
+    table = tuned_server.autotune(reqs)
+    assert set(table) == {1, 2, 4, 8}
+    tuned = tuned_server.infer(make_requests(24, seed=5, rid0=500))
+    for p, q in zip(plain, tuned):
+        np.testing.assert_array_equal(p.counts, q.counts)
+        np.testing.assert_array_equal(p.spike_times, q.spike_times)
+
+
 def test_poisson_arrivals_complete_with_latency_stats(cuda):
     ws, specs = net()
     server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=16, max_lanes=3)
