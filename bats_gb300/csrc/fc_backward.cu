@@ -23,6 +23,50 @@
 
 namespace bats {
 
+// Asynchronous 4- and 8-byte global -> shared copies (cp.async): every copy of a staging loop is in
+// flight at once, with no register round trip; cp_async_wait_all() waits for the thread's copies.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+
+// Position of one post neuron's spike train relative to a time-ordered scan of pre spikes: p = first
+// post spike with t_p > the current pre-spike time, with its suffix-table entry AB = (SA_p, SB_p)
+// ((0, 0) once p reaches the neuron's n valid spikes). The entry after the current one is loaded ahead,
+// so an advance does not wait on a global load.
+struct PostCursor {
+    const float* tp;
+    const float2* tb;
+    int n, p;
+    float tn, tn1;
+    float2 AB, AB1;
+    __device__ __forceinline__ void init(const float* tp_, const float2* tb_, int n_) {
+        tp = tp_;
+        tb = tb_;
+        n = n_;
+        p = 0;
+        tn = n > 0 ? tp[0] : BATS_INF;
+        AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
+        tn1 = n > 1 ? tp[1] : BATS_INF;
+        AB1 = n > 1 ? tb[1] : make_float2(0.0f, 0.0f);
+    }
+    __device__ __forceinline__ void advance_past(float t) {
+        while (tn <= t) {
+            ++p;
+            tn = tn1;
+            AB = AB1;
+            const bool more = p + 1 < n;
+            tn1 = more ? tp[p + 1] : BATS_INF;
+            AB1 = more ? tb[p + 1] : make_float2(0.0f, 0.0f);
+        }
+    }
+    __device__ __forceinline__ bool valid() const { return p < n; }
+};
+
 // One thread per (sample, post neuron): recurrent (reset) errors in place, factors, suffix tables.
 //   recurrent: propagate_recurrent_errors.cu:17-22   factors: compute_factors.cu:20-30
 __global__ void bwd_prep_kernel(const float* __restrict__ t, const float* __restrict__ a, const float* __restrict__ x,
@@ -103,7 +147,8 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
     const int cnt = (int)min(32LL, total - nb);
     const long long base = nb * K;
     const int nk = cnt * K;
-    for (int q = lane; q < nk; q += 32) sT[(q / K) * PREP_KS + q % K] = t[base + q];
+    for (int q = lane; q < nk; q += 32) cp_async4(sT + (q / K) * PREP_KS + q % K, t + base + q);
+    cp_async_wait_all();
     __syncwarp();
     int n = 0;
     if (lane < cnt) {
@@ -128,11 +173,12 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
     }
     for (int q = lane; q < nk; q += 32) {
         const int o = (q / K) * PREP_KS + q % K;
-        sZ[o] = z[base + q];
-        sX[o] = x[base + q];
-        sA[o] = a[base + q];
-        sE[o] = err[base + q];
+        cp_async4(sZ + o, z + base + q);
+        cp_async4(sX + o, x + base + q);
+        cp_async4(sA + o, a + base + q);
+        cp_async4(sE + o, err + base + q);
     }
+    cp_async_wait_all();
     __syncwarp();
     if (lane < cnt) {
         float* rt = sT + lane * PREP_KS;
@@ -217,9 +263,8 @@ bwd_grad_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, 
         const int n = active ? nvalid[pn] : 0;
         const float* tp = post_t + pn * k_post;
         const float2* tb = tab + pn * (k_post + 1);
-        int p = 0;
-        float2 AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
-        float tn = n > 0 ? tp[0] : BATS_INF;
+        PostCursor cur;
+        cur.init(tp, tb, n);
         const int E = ev_count[s];
         const Event* evs = ev + (long long)s * ev_cap;
         for (int m0 = 0; m0 < E; m0 += BWD_CHUNK) {
@@ -231,17 +276,8 @@ bwd_grad_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, 
                 const Event e = sev[m];
                 const int jj = e.j - J0;
                 if (jj < 0 || jj >= JC) continue;
-                while (tn <= e.t) {
-                    ++p;
-                    if (p < n) {
-                        AB = tb[p];
-                        tn = tp[p];
-                    } else {
-                        AB = make_float2(0.0f, 0.0f);
-                        tn = BATS_INF;
-                    }
-                }
-                if (p < n) G[jj][tid] += fmaf(e.es, AB.x, -(e.e * AB.y));
+                cur.advance_past(e.t);
+                if (cur.valid()) G[jj][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
             }
         }
     }
@@ -284,9 +320,8 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
         const int n = active ? nvalid[pn] : 0;
         const float* tp = post_t + pn * k_post;
         const float2* tb = tab + pn * (k_post + 1);
-        int p = 0;
-        float2 AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
-        float tn = n > 0 ? tp[0] : BATS_INF;
+        PostCursor cur;
+        cur.init(tp, tb, n);
         const Event* evs = ev_b + (long long)s * ev_cap;
         for (int m0 = beg; m0 < end; m0 += BWD_CHUNK) {
             const int cnt = min(BWD_CHUNK, end - m0);
@@ -296,17 +331,8 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
             if (n == 0) continue;
             for (int m = 0; m < cnt; ++m) {
                 const Event e = sev[m];
-                while (tn <= e.t) {
-                    ++p;
-                    if (p < n) {
-                        AB = tb[p];
-                        tn = tp[p];
-                    } else {
-                        AB = make_float2(0.0f, 0.0f);
-                        tn = BATS_INF;
-                    }
-                }
-                if (p < n) G[e.j - J0][tid] += fmaf(e.es, AB.x, -(e.e * AB.y));
+                cur.advance_past(e.t);
+                if (cur.valid()) G[e.j - J0][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
             }
         }
     }
@@ -369,9 +395,8 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
     const int n = active ? nvalid[pn] : 0;
     const float* tp = post_t + pn * k_post;
     const float2* tb = tab + pn * (k_post + 1);
-    int p = 0;
-    float2 AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
-    float tn = n > 0 ? tp[0] : BATS_INF;
+    PostCursor cur;
+    cur.init(tp, tb, n);
     for (int k = 0; k < n_stages; ++k) {
         const int slot = k % STAGES;
         if (!stream_acquire(sm, k, status)) return;
@@ -381,22 +406,11 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
 #pragma unroll
         for (int q = 0; q < 32; ++q) {
             const float t = sm.evs[slot][q].t;
-            if (q < cnt) {
-                while (tn <= t) {
-                    ++p;
-                    if (p < n) {
-                        AB = tb[p];
-                        tn = tp[p];
-                    } else {
-                        AB = make_float2(0.0f, 0.0f);
-                        tn = BATS_INF;
-                    }
-                }
-            }
+            if (q < cnt) cur.advance_past(t);
             const float w = sm.rows[slot][q][tid];
-            const bool use = q < cnt && p < n;
-            va[q] = use ? w * AB.x : 0.0f;
-            vb[q] = use ? w * AB.y : 0.0f;
+            const bool use = q < cnt && cur.valid();
+            va[q] = use ? w * cur.AB.x : 0.0f;
+            vb[q] = use ? w * cur.AB.y : 0.0f;
         }
         stream_release(sm, k);
         const float ra = warp_transpose_reduce32(va);
@@ -418,6 +432,75 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
             }
         }
     }
+}
+
+// ---- Narrow layers (N_post <= 32): event-parallel pre-spike errors ----------------------------------
+// With few post neurons, one thread per post neuron leaves most lanes idle and the per-sample CTA
+// serial over all events; here lanes take events instead, and every lane runs over the (few) post
+// neurons. The sample's post-spike times, suffix tables and counts are staged in shared memory.
+// (The weight gradient of narrow layers keeps the thread-per-neuron merge of bwd_grad_bucketed_kernel,
+// which costs a few instructions per event for all neurons at once, with more sample groups instead.)
+
+// Post-spike position of every post neuron for a pre spike at time t: p = number of valid post spikes
+// with t_k <= t (the first k with t_k > t), by binary search over the neuron's leading valid spikes.
+__device__ __forceinline__ int post_position(const float* __restrict__ tk, int n, float t) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (tk[mid] <= t) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Shared-memory copy of one sample's post-neuron data: times (N_post, K), tables (N_post, K + 1),
+// counts (N_post), issued as asynchronous copies (cp.async, no register round trip, all in flight at
+// once); the caller waits with cp_async_wait_all() and a barrier.
+__device__ __forceinline__ void stage_post(const float* __restrict__ post_t, const float2* __restrict__ tab,
+                                           const int* __restrict__ nvalid, int s, int n_post, int k_post,
+                                           float* st, float2* stab, int* snv) {
+    const long long pn0 = (long long)s * n_post;
+    for (int q = threadIdx.x; q < n_post * k_post; q += blockDim.x) cp_async4(st + q, post_t + pn0 * k_post + q);
+    for (int q = threadIdx.x; q < n_post * (k_post + 1); q += blockDim.x)
+        cp_async8(stab + q, tab + pn0 * (k_post + 1) + q);
+    for (int q = threadIdx.x; q < n_post; q += blockDim.x) cp_async4(snv + q, nvalid + pn0 + q);
+}
+
+// Pre-spike errors, thread per event: sum over post neurons i (in order) of w_ij * SA_i(p) and
+// w_ij * SB_i(p), then * e^{t/tau_s}/tau_s and * e^{t/tau}/tau, written to the event's slot.
+__global__ void __launch_bounds__(128)
+bwd_pre_err_narrow_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_slot,
+                          const int* __restrict__ ev_count, long long ev_cap, const float* __restrict__ wt, int ld,
+                          const float* __restrict__ post_t, const float2* __restrict__ tab,
+                          const int* __restrict__ nvalid, int n_post, int k_post, long long slots_per_sample,
+                          float tau_s, float tau, float* __restrict__ pre_err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* stab = reinterpret_cast<float2*>(smem_raw);
+    float* st = reinterpret_cast<float*>(stab + n_post * (k_post + 1));
+    int* snv = reinterpret_cast<int*>(st + n_post * k_post);
+    const int s = blockIdx.y;
+    const int E = ev_count[s];
+    if ((long long)blockIdx.x * blockDim.x >= E) return;  // whole CTA
+    stage_post(post_t, tab, nvalid, s, n_post, k_post, st, stab, snv);
+    cp_async_wait_all();
+    __syncthreads();
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= E) return;
+    const long long em = (long long)s * ev_cap + m;
+    const Event e = ev[em];
+    const float* wrow = wt + (long long)e.j * ld;
+    float sa = 0.0f, sb = 0.0f;
+    for (int i = 0; i < n_post; ++i) {
+        const int n = snv[i];
+        const int p = post_position(st + i * k_post, n, e.t);
+        if (p < n) {
+            const float w = __ldg(wrow + i);
+            const float2 AB = stab[i * (k_post + 1) + p];
+            sa += w * AB.x;
+            sb += w * AB.y;
+        }
+    }
+    pre_err[(long long)s * slots_per_sample + ev_slot[em]] = sa * e.es / tau_s - sb * e.e / tau;
 }
 
 // Sums the per-tile partials of each event in tile order and writes
@@ -553,6 +636,7 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
 }
 
 extern "C" size_t bats_pre_errors_workspace_bytes(int batch, long long ev_cap, int n_post) {
+    if (n_post <= 32) return 0;  // narrow layers: event-parallel kernel, no partials
     const int tile = n_post <= 32 ? 32 : (n_post <= 64 ? 64 : 128);
     const long long tiles = (n_post + tile - 1) / tile;
     return (size_t)batch * ev_cap * tiles * 2 * sizeof(float);
@@ -589,6 +673,18 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
     BATS_REQUIRE(weights_t && post_times && tables && nvalid, BATS_ERR_NULL, "pre_errors: null pointer");
     BATS_REQUIRE(((uintptr_t)weights_t & 15) == 0 && ((uintptr_t)events & 15) == 0, BATS_ERR_BAD_SHAPE,
                  "pre_errors: weights_t and events must be 16-byte aligned");
+    if (n_post <= 32) {
+        const size_t smem = (size_t)n_post * (k_post + 1) * sizeof(float2) + (size_t)n_post * k_post * sizeof(float) +
+                            (size_t)n_post * sizeof(int);
+        BATS_REQUIRE(smem <= 160 * 1024, BATS_ERR_BAD_SHAPE, "pre_errors: k_post too large for a narrow layer");
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_narrow_kernel, (int)smem));
+        dim3 grid((unsigned)((ev_cap + 127) / 128), batch);
+        bats::bwd_pre_err_narrow_kernel<<<grid, 128, smem, stream>>>(
+            reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights_t, ld, post_times,
+            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, slots, tau_s, tau, pre_errors);
+        BATS_CUDA(cudaGetLastError());
+        return BATS_OK;
+    }
     BATS_REQUIRE(workspace && workspace_bytes >= bats_pre_errors_workspace_bytes(batch, ev_cap, n_post),
                  BATS_ERR_WORKSPACE, "pre_errors: workspace too small");
     float2* part = reinterpret_cast<float2*>(workspace);

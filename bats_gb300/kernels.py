@@ -326,7 +326,12 @@ def grad_tile(n_post: int) -> int:
 
 def default_group(batch: int, n_post: int, n_pre: int, target_ctas: int = 1216) -> int:
     """Samples per group of the batch-reduced weight gradient: enough groups for ~8 CTAs per SM of a
-    152-SM GB300, but at most 32 partial gradients."""
+    152-SM GB300, but at most 32 partial gradients (narrow layers, N_post <= 32, whose partials are small
+    and whose kernel runs one warp per bucket and group: up to 4 warps per SM, any number of partials)."""
+    if n_post <= 32:
+        buckets = (n_pre + BUCKET_WIDTH - 1) // BUCKET_WIDTH
+        groups = max(1, min(batch, -(-4 * 152 // buckets)))
+        return max(1, -(-batch // groups))
     tiles = (n_post + grad_tile(n_post) - 1) // grad_tile(n_post)
     buckets = (n_pre + BUCKET_WIDTH - 1) // BUCKET_WIDTH
     groups = max(1, min(batch, -(-target_ctas // (tiles * buckets)), 32))

@@ -202,7 +202,7 @@ class FCTrainStep:
                                                      "lanes": lambda: run_fwd(K.FWD_LANES)}, force=force)
             self.fwd_algo[li] = K.FWD_TILE if best == "tile" else K.FWD_LANES
             cands = {}
-            for parts in (4, 8, 16, 32):
+            for parts in ((4, 8, 16, 32) if spec.n_neurons > 32 else (16, 32, 64, 128, 256)):
                 g = max(2, -(-B // parts))
                 if K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev, g) <= wsb:
                     cands[str(g)] = g

@@ -182,3 +182,41 @@ def test_backward_is_deterministic(cuda):
         pe = K.pre_errors(ev, wt, ts, tab, 0.1, tau32)
         outs.append((g.cpu(), pe.cpu()))
     assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("n_post", [10, 20, 32])
+def test_narrow_layer_kernels(cuda, n_post):
+    """Narrow layers (N_post <= 32): the weight gradient over bucketed events is bit-identical to the
+    one over the full event list (same order of every sum), per sample and batch-summed, and
+    deterministic; the event-parallel pre errors are deterministic and agree with the float64 oracle on
+    the same forward state."""
+    import dataclasses
+    t, n_in = multi_spike_input(16, 150, 4, 0.1, seed=7)
+    rng = np.random.default_rng(7)
+    W = (rng.uniform(-0.5, 1.0, (n_post, 150)) * 2).astype(np.float32)
+    tau_s, th = 0.1, 0.5
+    ev = K.sort_events(cu(t), tau_s, 2 * tau_s)
+    wt = K.transpose_weights(cu(W))
+    n, a, x, ts, z = K.lif_forward_fc(ev, wt, n_post, 8, tau_s, th, th)
+    assert int(n.sum()) > 50
+    err = cu(rng.normal(size=ts.shape).astype(np.float32))
+    tau32, c, dtt = K.lif_constants(tau_s, th, th)
+    tab = K.backward_prep(ts, a, x, z, err, c, tau32, dtt, want_factors=True)
+    plain = dataclasses.replace(ev, bucketed=None, bucket_offsets=None)
+    for per_sample, group in ((True, None), (False, 4), (False, 16)):
+        g_b = K.weights_gradient(ev, ts, tab, 150, per_sample=per_sample, group=group)
+        g_again = K.weights_gradient(ev, ts, tab, 150, per_sample=per_sample, group=group)
+        g_full = K.weights_gradient(plain, ts, tab, 150, per_sample=per_sample, group=group)
+        assert torch.equal(g_b, g_again), "gradient not deterministic"
+        assert torch.equal(g_b, g_full), f"bucketed vs full event list (per_sample={per_sample}, group={group})"
+    pe = K.pre_errors(ev, wt, ts, tab, tau_s, tau32)
+    pe2 = K.pre_errors(ev, wt, ts, tab, tau_s, tau32)
+    assert torch.equal(pe, pe2)
+    f1, f2 = tab.f1.cpu().numpy(), tab.f2.cpu().numpy()
+    e = err.cpu().numpy()
+    post = ts.cpu().numpy()
+    pre = (t.astype(np.float64),) + R.compute_pre_exps(t, float(np.float32(tau_s)), float(tau32))
+    ref = R.propagate_errors_to_pre_spikes(f1, f2, post, pre, W, e, float(np.float32(tau_s)), float(tau32))
+    scale = R.propagate_errors_to_pre_spikes(np.abs(f1), np.abs(f2), post, pre, np.abs(W), np.abs(e),
+                                             float(np.float32(tau_s)), -float(tau32))
+    assert_sum_close(pe.cpu().numpy(), ref, scale, what="narrow pre errors vs oracle")
