@@ -372,6 +372,113 @@ def refkern_rate(variant, steps, flush):
             "what": "reference CUDA kernels (unmodified, oracle/_ref) with the reference wrappers' launch shapes"}
 
 
+def batching_inputs(batch=4096, n_in=1024, seed=11, median=200, lo=20, hi=4000, t_max=0.1):
+    """Per-sample input spike count clip(round(lognormal(ln median, 1)), lo, hi), channels uniform over
+    n_in, times U(0, t_max): spike trains (B, n_in, K_in) with K_in the largest per-channel count, and
+    labels."""
+    rng = np.random.default_rng(seed)
+    counts = np.clip(np.round(rng.lognormal(np.log(median), 1.0, batch)), lo, hi).astype(np.int64)
+    chans = [rng.integers(0, n_in, c) for c in counts]
+    times = [np.sort(rng.uniform(0, t_max, c)).astype(np.float32) for c in counts]
+    k_in = max(int(np.bincount(ch, minlength=n_in).max()) for ch in chans)
+    t = np.full((batch, n_in, k_in), np.inf, dtype=np.float32)
+    for q, (ch, tm) in enumerate(zip(chans, times)):
+        order = np.argsort(ch, kind="stable")
+        ch_s, tm_s = ch[order], tm[order]
+        first = np.searchsorted(ch_s, ch_s, side="left")
+        slot = np.arange(len(ch_s)) - first
+        t[q, ch_s, slot] = tm_s
+    labels = rng.integers(0, 20, batch).astype(np.int32)
+    return t, labels, counts
+
+
+def batching_bench(steps: int = 5, warmup: int = 3):
+    """Uneven batches: 4096 samples over 1024 input channels with lognormal spike counts (median 200,
+    20-4000), times U(0, 0.1) s, network 1024-1024-20, max_n_spike 30, in the reference's MNIST regime
+    (weights U(-1, 1), hidden threshold 0.2, output 1.3); the whole train step (forward, spike-count
+    loss, exact backward, Adam) autotuned and replayed as one CUDA graph."""
+    import torch
+    from bats_gb300.train import FCLayerSpec, FCTrainStep
+    t, labels, counts = batching_inputs()
+    rng = np.random.default_rng(12)
+    sizes = [1024, 1024, 20]
+    ws = [torch.tensor(rng.uniform(-1, 1, (o, i)).astype(np.float32)) for i, o in zip(sizes[:-1], sizes[1:])]
+    specs = [FCLayerSpec(1024, TAU_S, 0.2, 0.2, K_SPIKE), FCLayerSpec(20, TAU_S, 1.3, 1.3, K_SPIKE)]
+    ts = FCTrainStep(t.shape[0], 1024, t.shape[2], specs, ws, TARGET_TRUE, TARGET_FALSE, learning_rate=LR,
+                     max_simulation=MAX_SIM)
+    ts.set_inputs(torch.tensor(t), torch.tensor(labels))
+    tuned = ts.autotune()
+    graphed = ts.try_capture()
+    fn = ts.replay if graphed else ts.step
+    flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    ms, _ = time_steps(fn, steps, warmup, flush)
+    kb = kernel_breakdown(ts)
+    out = {"value": t.shape[0] * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps,
+           "steps": steps, "batch": int(t.shape[0]), "k_in": int(t.shape[2]), "graph": graphed, "autotuned": tuned,
+           "input_events": {"mean": float(counts.mean()), "max": int(counts.max()), "min": int(counts.min())},
+           "spikes_per_layer_last_step": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
+           "network": "1024-1024-20, K 30, U(-1,1) weights, theta 0.2 hidden / 1.3 output"}
+    del ts
+    torch.cuda.empty_cache()
+    return out
+
+
+def conv_bench(steps: int = 5):
+    """The convolutional network of the reference's MNIST conv experiment (experiments/mnist/train_conv.py:
+    conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> FC 300 -> 10, thresholds 0.04 / 0.8 / 0.6 / 0.3 with
+    delta_theta = theta, tau_s 0.13, weights U(-1, 1)), max_n_spike 10 in every layer, batch 128, on
+    synthetic MNIST-shaped single-spike input; full train step (forward, spike-count loss, exact backward,
+    Adam) through the drop-in layer API."""
+    import torch
+    from bats_gb300 import Network, SpikeCountClassLoss
+    from bats_gb300.Layers import ConvInputLayer, ConvLIFLayer, LIFLayer, PoolingLayer
+    from bats_gb300.Optimizers import AdamOptimizer
+    Bc, Kc = 128, 10
+    rng = np.random.default_rng(3)
+    net = Network()
+    inp = ConvInputLayer(neurons_shape=np.array([28, 28, 1]), name="in")
+    net.add_layer(inp, input=True)
+    conv_init = lambda c, x, y, pc: torch.tensor(rng.uniform(-1, 1, (c, x, y, pc)).astype(np.float32), device="cuda")
+    ff_init = lambda n, m: torch.tensor(rng.uniform(-1, 1, (n, m)).astype(np.float32), device="cuda")
+    c1 = ConvLIFLayer(inp, filters_shape=np.array([5, 5, 15]), tau_s=TAU_S, theta=0.04, delta_theta=0.04,
+                      weight_initializer=conv_init, max_n_spike=Kc, name="conv1")
+    net.add_layer(c1)
+    p1 = PoolingLayer(c1, name="pool1")
+    net.add_layer(p1)
+    c2 = ConvLIFLayer(p1, filters_shape=np.array([5, 5, 40]), tau_s=TAU_S, theta=0.8, delta_theta=0.8,
+                      weight_initializer=conv_init, max_n_spike=Kc, name="conv2")
+    net.add_layer(c2)
+    p2 = PoolingLayer(c2, name="pool2")
+    net.add_layer(p2)
+    f1 = LIFLayer(p2, n_neurons=300, tau_s=TAU_S, theta=0.6, delta_theta=0.6, weight_initializer=ff_init,
+                  max_n_spike=Kc, name="fc")
+    net.add_layer(f1)
+    out = LIFLayer(f1, n_neurons=10, tau_s=TAU_S, theta=0.3, delta_theta=0.3, weight_initializer=ff_init,
+                   max_n_spike=Kc, name="out")
+    net.add_layer(out)
+    loss_fn = SpikeCountClassLoss(TARGET_TRUE, TARGET_FALSE)
+    opt = AdamOptimizer(learning_rate=LR)
+    t, n, labels = make_inputs(Bc, 5)
+    labels_d = torch.tensor(labels, device="cuda")
+    layers = [c1, p1, c2, p2, f1, out]
+
+    def step():
+        net.reset()
+        net.forward(t, n, max_simulation=MAX_SIM, training=True)
+        sp, nsp = net.output_spike_trains
+        loss, err = loss_fn.compute_loss_and_errors(sp, nsp, labels_d)
+        g = net.backward(err)
+        net.apply_deltas(opt.step([None if x is None else x.mean(0) for x in g]))
+
+    flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    ms, _ = time_steps(step, steps, 3, flush)
+    spikes = [int(L.spike_trains[1].sum().item()) for L in layers]
+    return {"value": Bc * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps, "steps": steps,
+            "batch": Bc, "spikes_per_layer": spikes,
+            "network": "28x28x1 -> conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> 300 -> 10, K 10",
+            "what": "full train step through Network/ConvLIFLayer/PoolingLayer/LIFLayer/AdamOptimizer"}
+
+
 def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float = 0.8):
     """Serving loop on the 700-512-512-20 network (max_n_spike 30): requests of 50-5000 events
     (log-uniform) over 700 channels at times U(0, 0.2) s. Peak throughput = requests completed per second
@@ -417,7 +524,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=12.0)
-    ap.add_argument("--workload", default="all", choices=["all", "literal", "active", "serving"],
+    ap.add_argument("--workload", default="all", choices=["all", "literal", "active", "serving", "conv", "batching"],
                     help="all (default): every measurement; otherwise only that one (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline (profiling runs)")
     args = ap.parse_args()
@@ -448,13 +555,15 @@ def main():
         dist = dist_mod
     res = run_ours(args, dist, rank, world)
     serving = serving_bench() if args.workload in ("all", "serving") else None
+    conv = conv_bench() if args.workload in ("all", "conv") else None
+    batching = batching_bench() if args.workload in ("all", "batching") else None
     if rank != 0:
         return
     if args.workload != "all":
         head = res.get(args.workload, {})
         print(json.dumps({"metric": METRIC, "workload": args.workload, "value": head.get("value"),
                           "unit": "samples/s", "steps": args.steps, "warmup": args.warmup, "detail": head,
-                          "serving": serving}))
+                          "serving": serving, "conv": conv, "batching": batching}))
         return
     lit, act = res["literal"], res["active"]
     line = {
@@ -467,7 +576,7 @@ def main():
                    "cuda_graph": lit["graph"]},
         "roofline": lit["roofline"], "e2e": lit["e2e"], "gpu_launches": lit["gpu_launches"], "clocks": lit["clocks"],
         "cpu_baseline": cb, "spikes_per_layer": lit["spikes_per_layer_last_step"], "kernels_ms": lit["kernels_ms"],
-        "active": act, "serving": serving,
+        "active": act, "serving": serving, "conv": conv, "batching": batching,
     }
     print(json.dumps(line))
 
