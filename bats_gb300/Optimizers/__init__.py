@@ -1,2 +1,3 @@
 from .GradientDescentOptimizer import GradientDescentOptimizer
 from .AdamOptimizer import AdamOptimizer
+from .NAdamOptimizer import NAdamOptimizer

@@ -35,6 +35,13 @@ SIGNATURES = {
     "bats_lif_forward_fc_default_algo": (c_int, [c_int, c_int, c_int]),
     "bats_lif_forward_fc_algo": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float,
                                          c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp]),
+    "bats_intensity_to_spike_times": (c_int, [c_vp, c_int, c_int, ctypes.c_double, ctypes.c_double, c_vp, c_vp,
+                                              c_vp]),
+    "bats_nadam_step": (c_int, [c_vp, c_vp, c_vp, c_ll, c_float, c_float, c_float, c_float, ctypes.c_double,
+                                ctypes.c_double, c_vp, c_vp]),
+    "bats_weights_synaptic_scaling": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float,
+                                              c_vp]),
+    "bats_label_weights_synaptic_scaling": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_vp]),
     "bats_conv_forward": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                   c_float, c_float, c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_events_to_trains": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),

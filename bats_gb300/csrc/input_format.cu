@@ -123,3 +123,34 @@ extern "C" int bats_events_max_per_neuron(const int* indices, int batch, int max
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
+
+// Intensity (time-to-first-spike) encoding of the reference's MNIST pipeline
+// (experiments/mnist/Dataset.py:66-71): one spike per input at t = time_window * (1 - x / max_value),
+// evaluated in double as NumPy does, and no spike (+inf, count 0) where t equals time_window (x == 0).
+namespace bats {
+__global__ void intensity_to_spike_times_kernel(const unsigned char* __restrict__ pixels, long long total,
+                                                double time_window, double max_value, float* __restrict__ times,
+                                                int* __restrict__ counts) {
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const double t = time_window * (1.0 - ((double)pixels[q] / max_value));
+        const bool spike = t != time_window;
+        times[q] = spike ? (float)t : BATS_INF;
+        counts[q] = spike ? 1 : 0;
+    }
+}
+}  // namespace bats
+
+extern "C" int bats_intensity_to_spike_times(const unsigned char* pixels, int batch, int n_neurons, double time_window,
+                                             double max_value, float* times, int* counts, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_neurons >= 0 && max_value > 0.0, BATS_ERR_BAD_SHAPE,
+                 "intensity_to_spike_times: bad shape");
+    const long long total = (long long)batch * n_neurons;
+    if (total == 0) return BATS_OK;
+    BATS_REQUIRE(pixels && times && counts, BATS_ERR_NULL, "intensity_to_spike_times: null pointer");
+    const long long blocks = (total + 255) / 256;
+    bats::intensity_to_spike_times_kernel<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, stream>>>(
+        pixels, total, time_window, max_value, times, counts);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}

@@ -210,6 +210,18 @@ def convert_to_spike_per_neuron(indices, times, n_neurons: int, k_cap: int | Non
     return out_t, out_n
 
 
+def intensity_to_spike_times(pixels, time_window: float = 100e-3, max_value: float = 255.0):
+    """8-bit intensities (B, N) -> single-spike trains (B, N, 1) and counts (B, N)
+    (experiments/mnist/Dataset.py:66-71: t = time_window * (1 - x / max_value), no spike where x == 0)."""
+    px = _c(pixels, torch.uint8)
+    B, N = px.shape
+    times = torch.empty((B, N, 1), dtype=F32, device=px.device)
+    counts = torch.empty((B, N), dtype=I32, device=px.device)
+    call("bats_intensity_to_spike_times", ptr(px), B, N, float(time_window), float(max_value), ptr(times),
+         ptr(counts), stream_ptr())
+    return times, counts
+
+
 def aggregate_spikes_conv(n_spikes, spike_times, pre_shape):
     """2x2 pooling (replaces aggregate_spikes_conv + argsort, Wrappers/Inference/aggregate_spikes_conv.py:10-28).
     Returns (n_spikes (B, N_out), times (B, N_out, 4K), indices (B, N_out, 4K) int32)."""
@@ -468,6 +480,31 @@ def adam_step(grad, m, v, beta_1, beta_2, epsilon, lr, bias1, bias2, delta=None,
     call("bats_adam_step", ptr(grad), ptr(m), ptr(v), grad.numel(), float(beta_1), float(beta_2), float(epsilon),
          float(lr), float(bias1), float(bias2), ptr(delta), ptr(weights), ptr(weights_t), n_post, n_pre, ld,
          stream_ptr())
+
+
+def nadam_step(grad, m, v, beta_1, beta_2, epsilon, lr, bias1, bias2, delta):
+    """NAdam on one tensor (bats/Optimizers/NAdamOptimizer.py:35-58); m, v in place, delta written."""
+    call("bats_nadam_step", ptr(grad), ptr(m), ptr(v), grad.numel(), float(beta_1), float(beta_2), float(epsilon),
+         float(lr), float(bias1), float(bias2), ptr(delta), stream_ptr())
+
+
+def apply_weights_synaptic_scaling(weights, silent_ratios, n_spikes, gradient, scaling_threshold: float,
+                                   factor: float):
+    """In place on the per-sample gradient (B, N_post, N_pre)
+    (CuFiles/Regularization/apply_weights_synaptic_scaling.cu)."""
+    B, n_post, n_pre = gradient.shape
+    call("bats_weights_synaptic_scaling", ptr(_c(weights)), ptr(_c(silent_ratios)), ptr(_c(n_spikes, I32)),
+         ptr(gradient), B, n_post, n_pre, float(scaling_threshold), float(factor), stream_ptr())
+    return gradient
+
+
+def apply_label_weights_synaptic_scaling(weights, labels, n_spikes, gradient, factor: float):
+    """In place on the per-sample gradient (B, N_post, N_pre)
+    (CuFiles/Regularization/apply_label_weights_synaptic_scaling.cu)."""
+    B, n_post, n_pre = gradient.shape
+    call("bats_label_weights_synaptic_scaling", ptr(_c(weights)), ptr(_c(labels)), ptr(_c(n_spikes, I32)),
+         ptr(gradient), B, n_post, n_pre, float(factor), stream_ptr())
+    return gradient
 
 
 def add_deltas(weights, delta, weights_t=None):

@@ -78,6 +78,12 @@ int bats_lif_forward_fc(const void* events, const int* ev_count, long long ev_ca
                         float max_simulation, int* n_spikes, float* a, float* x, float* times, float* post_exp_tau,
                         cudaStream_t stream);
 
+/* Time-to-first-spike encoding of 8-bit intensities (B, N): times (B, N, 1) = time_window * (1 - x / max_value)
+ * (in double, then float), +inf and count 0 where x == 0. Replaces Dataset.__to_spikes of the reference's
+ * MNIST experiments (experiments/mnist/Dataset.py:66-71). */
+int bats_intensity_to_spike_times(const unsigned char* pixels, int batch, int n_neurons, double time_window,
+                                  double max_value, float* times, int* counts, cudaStream_t stream);
+
 /* Kernel choice of the FC forward: BATS_FWD_TILE runs one CTA per (post-neuron tile, sample) with a
  * producer warp streaming weight rows (throughput-oriented, large B * N_post); BATS_FWD_LANES runs one warp
  * per (sample, post neuron) with 32 events evaluated in parallel (latency-oriented: few neurons, small
@@ -224,6 +230,28 @@ int bats_adam_powers_advance(double* powers, float beta_1, float beta_2, cudaStr
 int bats_adam_step_device(const float* grad, float* m, float* v, long long count, float beta_1, float beta_2,
                           float epsilon, float learning_rate, const double* powers, float* weights, float* weights_t,
                           int n_post, int n_pre, int ld, cudaStream_t stream);
+
+/* One NAdam step on one tensor: m, v in place, delta written. bias_correction_i = 1 - beta_i^t.
+ * Replaces NAdamOptimizer.step (bats/Optimizers/NAdamOptimizer.py:35-58, kernels :6-20). */
+int bats_nadam_step(const float* grad, float* m, float* v, long long count, float beta_1, float beta_2, float epsilon,
+                    float learning_rate, double bias_correction_1, double bias_correction_2, float* delta,
+                    cudaStream_t stream);
+
+/* Synaptic scaling of the per-sample gradient (B, N_post, N_pre), in place: for samples whose silent ratio is
+ * >= threshold, gradient[s, i, :] -= factor * |W[i, :]| for every post neuron i with no spike in s.
+ * Replaces apply_weights_synaptic_scaling_kernel
+ * (bats/CudaKernels/CuFiles/Regularization/apply_weights_synaptic_scaling.cu:2-25). */
+int bats_weights_synaptic_scaling(const float* weights, const float* silent_ratios, const int* n_spikes,
+                                  float* gradient, int batch, int n_post, int n_pre, float threshold, float factor,
+                                  cudaStream_t stream);
+
+/* Label synaptic scaling, in place: gradient[s, l, :] -= factor * |W[l, :]| with l = (int)labels[s], unless
+ * n_spikes[l] > 0 (the reference reads the label's count from the first row of n_spikes; kept as is).
+ * Labels outside [0, N_post) are skipped. Replaces apply_label_weights_synaptic_scaling_kernel
+ * (bats/CudaKernels/CuFiles/Regularization/apply_label_weights_synaptic_scaling.cu:2-20). */
+int bats_label_weights_synaptic_scaling(const float* weights, const float* labels, const int* n_spikes,
+                                        float* gradient, int batch, int n_post, int n_pre, float factor,
+                                        cudaStream_t stream);
 
 /* weights += delta, optionally refreshing the transposed copy. Replaces LIFLayer.add_deltas
  * (bats/Layers/LIFLayer.py:112-113). */

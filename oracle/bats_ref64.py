@@ -431,6 +431,59 @@ class Adam:
         return out
 
 
+class NAdam:
+    """bats/Optimizers/NAdamOptimizer.py:23-58: deltas -(lr / (sqrt(v_hat) + eps)) *
+    (beta_1 m_hat + (1 - beta_1) g / (1 - beta_1^t))."""
+
+    def __init__(self, learning_rate, beta_1=0.9, beta_2=0.999, epsilon=1e-8):
+        self.lr = float(np.float32(learning_rate))
+        self.b1 = float(np.float32(beta_1))
+        self.b2 = float(np.float32(beta_2))
+        self.eps = float(np.float32(epsilon))
+        self.m = None
+        self.v = None
+        self.t = 0
+
+    def step(self, grads):
+        self.t += 1
+        if self.m is None:
+            self.m = [None if g is None else np.zeros(np.shape(g)) for g in grads]
+            self.v = [None if g is None else np.zeros(np.shape(g)) for g in grads]
+        c1 = 1.0 - self.b1 ** self.t
+        c2 = 1.0 - self.b2 ** self.t
+        out = []
+        for q, g in enumerate(grads):
+            if g is None:
+                out.append(None)
+                continue
+            g = np.asarray(g, dtype=np.float64)
+            self.m[q] = self.b1 * self.m[q] + (1.0 - self.b1) * g
+            self.v[q] = self.b2 * self.v[q] + (1.0 - self.b2) * g * g
+            m_hat, v_hat = self.m[q] / c1, self.v[q] / c2
+            out.append(-(self.lr / (np.sqrt(v_hat) + self.eps)) * (self.b1 * m_hat + (1.0 - self.b1) * g / c1))
+        return out
+
+
+def weights_synaptic_scaling(weights, silent_ratios, n_spikes, gradient, scaling_threshold, factor):
+    """apply_weights_synaptic_scaling.cu:2-25 on a per-sample gradient (B, N_post, N_pre), returned new."""
+    g = np.array(gradient, dtype=np.float64)
+    apply = (np.asarray(silent_ratios)[:, None] >= scaling_threshold) & (np.asarray(n_spikes) <= 0)
+    g -= np.where(apply[:, :, None], factor * np.abs(np.asarray(weights, dtype=np.float64))[None], 0.0)
+    return g
+
+
+def label_weights_synaptic_scaling(weights, labels, n_spikes, gradient, factor):
+    """apply_label_weights_synaptic_scaling.cu:2-20 (the label's spike count read from n_spikes[label], the
+    first sample's row, as the kernel indexes it)."""
+    g = np.array(gradient, dtype=np.float64)
+    W = np.abs(np.asarray(weights, dtype=np.float64))
+    flat = np.asarray(n_spikes).reshape(-1)
+    for s, lab in enumerate(np.asarray(labels).astype(np.int64)):
+        if 0 <= lab < W.shape[0] and flat[lab] <= 0:
+            g[s, lab] -= factor * W[lab]
+    return g
+
+
 def threshold_sensitivity(pre_times, weights, tau_s, theta, delta_theta, max_n_spike, max_simulation=INF,
                           rel_count=1e-5, rel_time=1e-6):
     """Conditioning of the forward pass, for comparing an FP32 evaluation with this float64 one.

@@ -10,6 +10,7 @@ import torch
 from bats_gb300 import Network, SpikeCountClassLoss, SpikeCountLoss, SpikeTimeLoss, TTFSSoftmaxCrossEntropy
 from bats_gb300.Layers import InputLayer, LIFLayer
 from bats_gb300.Optimizers import AdamOptimizer, GradientDescentOptimizer
+from bats_gb300 import kernels as K
 from oracle import bats_ref64 as R
 
 pytestmark = pytest.mark.gpu
@@ -133,3 +134,93 @@ def test_store_restore(cuda, tmp_path):
     layer2.restore(Path(tmp_path))
     assert torch.allclose(layer2.weights, w)
     assert os.path.exists(tmp_path / "test_layer_weights.npy")
+
+
+def test_nadam_matches_oracle_and_converges(cuda):
+    from bats_gb300.Optimizers import NAdamOptimizer
+    rng = np.random.default_rng(2)
+    g = [None, rng.normal(size=(5, 10)).astype(np.float32), rng.normal(size=(2, 5)).astype(np.float32)]
+    ours = NAdamOptimizer(learning_rate=0.05)
+    ref = R.NAdam(0.05)
+    for step in range(20):
+        d = ours.step([None if x is None else cu(x) for x in g])
+        e = ref.step(g)
+        for a, b in zip(d, e):
+            if b is None:
+                assert a is None
+                continue
+            np.testing.assert_allclose(a.cpu().numpy(), b, rtol=2e-5, atol=1e-9)
+        g = [None if x is None else (x * 0.9).astype(np.float32) for x in g]
+    opt = NAdamOptimizer(learning_rate=0.05)
+    torch.manual_seed(0)
+    w = torch.randn(5, 10, device="cuda")
+    for _ in range(1000):
+        w += opt.step([w])[0]
+    assert torch.allclose(w, torch.zeros_like(w), atol=1e-4)
+
+
+def test_synaptic_scaling_regularizers(cuda):
+    rng = np.random.default_rng(3)
+    B, N, M = 6, 7, 9
+    W = rng.normal(size=(N, M)).astype(np.float32)
+    grad = rng.normal(size=(B, N, M)).astype(np.float32)
+    n_sp = rng.integers(0, 2, (B, N)).astype(np.int32)
+    ratios = rng.uniform(0, 1, B).astype(np.float32)
+    g = cu(grad)
+    K.apply_weights_synaptic_scaling(cu(W), cu(ratios), cu(n_sp, torch.int32), g, 0.5, 0.1)
+    np.testing.assert_allclose(g.cpu().numpy(), R.weights_synaptic_scaling(W, ratios, n_sp, grad, 0.5, 0.1),
+                               rtol=1e-6, atol=1e-7)
+    labels = rng.integers(0, N, B).astype(np.float32)
+    labels[0] = N + 3  # not a neuron: skipped
+    g = cu(grad)
+    K.apply_label_weights_synaptic_scaling(cu(W), cu(labels), cu(n_sp, torch.int32), g, 0.2)
+    np.testing.assert_allclose(g.cpu().numpy(), R.label_weights_synaptic_scaling(W, labels, n_sp, grad, 0.2),
+                               rtol=1e-6, atol=1e-7)
+
+
+def test_checkpoint_resumes_training_exactly(cuda, tmp_path):
+    """Weights (reference format) + Adam state saved after 3 steps; a fresh network and optimizer loaded from
+    the checkpoint take the same next 2 steps bit for bit."""
+    from bats_gb300 import checkpoint
+
+    def make():
+        rng = np.random.default_rng(0)
+        net = Network()
+        inp = InputLayer(n_neurons=40, name="in")
+        net.add_layer(inp, input=True)
+        hid = LIFLayer(inp, n_neurons=30, tau_s=0.1, theta=0.2, delta_theta=0.2, max_n_spike=8, name="hid",
+                       weight_initializer=lambda a, b: rng.uniform(-1, 1, (a, b)).astype(np.float32))
+        net.add_layer(hid)
+        out = LIFLayer(hid, n_neurons=5, tau_s=0.1, theta=0.5, delta_theta=0.5, max_n_spike=8, name="out",
+                       weight_initializer=lambda a, b: rng.uniform(-1, 1, (a, b)).astype(np.float32))
+        net.add_layer(out)
+        return net, hid, out
+
+    rng = np.random.default_rng(1)
+    t = np.where(rng.random((8, 40, 1)) < 0.5, rng.uniform(0, 0.05, (8, 40, 1)), np.inf).astype(np.float32)
+    n = np.isfinite(t[:, :, 0]).astype(np.int32)
+    labels = torch.tensor(rng.integers(0, 5, 8), device="cuda")
+    loss_fn = SpikeCountClassLoss(5.0, 1.0)
+
+    def step(net, opt):
+        net.reset()
+        net.forward(t, n, max_simulation=0.2, training=True)
+        sp, nsp = net.output_spike_trains
+        _, err = loss_fn.compute_loss_and_errors(sp, nsp, labels)
+        g = net.backward(err)
+        net.apply_deltas(opt.step([None if x is None else x.mean(0) for x in g]))
+
+    net, hid, out = make()
+    opt = AdamOptimizer(learning_rate=0.01)
+    for _ in range(3):
+        step(net, opt)
+    checkpoint.save(tmp_path, net, opt)
+    assert (tmp_path / "hid_weights.npy").exists() and (tmp_path / "out_weights.npy").exists()
+    for _ in range(2):
+        step(net, opt)
+    net2, hid2, out2 = make()
+    opt2 = AdamOptimizer(learning_rate=0.01)
+    checkpoint.load(tmp_path, net2, opt2)
+    for _ in range(2):
+        step(net2, opt2)
+    assert torch.equal(hid.weights, hid2.weights) and torch.equal(out.weights, out2.weights)

@@ -102,3 +102,16 @@ def test_poisson_arrivals_complete_with_latency_stats(cuda):
     st = latency_stats(res)
     assert st["p99_ms"] >= st["p50_ms"] > 0
     assert server.batches_launched > 1
+
+
+def test_intensity_encoding_matches_the_reference_formula(cuda):
+    """experiments/mnist/Dataset.py:66-71 in NumPy (float64) vs the device encoder."""
+    rng = np.random.default_rng(0)
+    px = rng.integers(0, 256, (7, 784)).astype(np.uint8)
+    px[0, :10] = 0
+    px[1, :10] = 255
+    t, n = K.intensity_to_spike_times(torch.tensor(px, device="cuda"))
+    ref = (100e-3 * (1 - (px.reshape(7, 784, 1) / 255)))
+    ref[ref == 100e-3] = np.inf
+    np.testing.assert_array_equal(t.cpu().numpy(), ref.astype(np.float32))
+    np.testing.assert_array_equal(n.cpu().numpy(), np.isfinite(ref).astype(np.int32).reshape(7, 784))
