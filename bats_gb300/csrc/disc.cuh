@@ -90,4 +90,45 @@ BATS_HD float fc_discriminant(float b2, float a, float c) {
     return fc_discriminant_ref64(b2, a, c);
 }
 
+// (float)((double)x / d) for d > 0 given 1/d ~= r_hi + r_lo (two floats, relative error <= 2^-47), without
+// FP64 on the common path: x * (r_hi + r_lo) is formed as r + g (r = the float nearest to it, g its exact
+// remainder), which lies within 2^-46 |x/d| of the quotient; if |g| plus that bound (and double's own
+// rounding of x/d) stays below half the float spacing around r, both roundings of x/d give r. A zero x
+// gives the zero of its sign. Otherwise (near a midpoint, tiny quotients, d not positive) the double
+// division itself is evaluated.
+#if defined(__CUDA_ARCH__)
+__device__ __noinline__
+#else
+inline
+#endif
+float quotient_ref64(float x, double d) {
+    return (float)((double)x / d);
+}
+
+BATS_HD float quotient_f64_to_f32(float x, float r_hi, float r_lo, double d) {
+    if (x == 0.0f && r_hi > 0.0f) return x;  // +-0 / d = +-0 for d > 0 (zero gradients are common)
+    const float p_hi = BATS_FMUL(x, r_hi);
+    const float p_lo = BATS_FMA(x, r_hi, -p_hi);
+    const float t = BATS_FMA(x, r_lo, p_lo);
+    const float r = BATS_FADD(p_hi, t);
+    const float g = two_sum_err(p_hi, t, r);
+    const float ar = r < 0.0f ? -r : r;
+    const bool in_range = ar >= 0x1p-90f && ar < 0x1p120f && r_hi > 0.0f;
+    const int rbits = BATS_F2I(ar);
+    float lim = BATS_I2F((rbits & 0x7f800000) - (24 << 23));
+    const bool toward_zero = (r > 0.0f) ? (g < 0.0f) : (g > 0.0f);
+    if ((rbits & 0x007fffff) == 0 && toward_zero) lim = BATS_FMUL(lim, 0.5f);
+    const float ag = g < 0.0f ? -g : g;
+    const bool safe = in_range && BATS_FADD(ag, BATS_FMUL(0x1p-44f, ar)) < BATS_FMUL(lim, 1.0f - 0x1p-20f);
+    if (safe) return r;
+    return quotient_ref64(x, d);
+}
+
+// The float pair (hi, lo) with hi + lo ~= 1/d to about 2^-48 relative, for quotient_f64_to_f32.
+BATS_HD void reciprocal_pair(double d, float& hi, float& lo) {
+    const double r = 1.0 / d;
+    hi = (float)r;
+    lo = (float)(r - (double)hi);
+}
+
 }  // namespace bats

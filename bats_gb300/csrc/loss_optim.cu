@@ -125,11 +125,18 @@ __global__ void spike_time_loss_kernel(const float* __restrict__ spikes, float* 
 __global__ void adam_kernel(const float* __restrict__ grad, float* __restrict__ m, float* __restrict__ v,
                             long long count, float beta_1, float one_minus_beta_1, float beta_2,
                             float one_minus_beta_2, double bias1, double bias2, const double* __restrict__ powers,
+                            float r1_hi, float r1_lo, float r2_hi, float r2_lo,
                             float lr, float eps, float* __restrict__ delta, float* __restrict__ w, float* __restrict__ wt, int n_post,
                             int n_pre, int ld) {
     if (powers) {
+        // State written by adam_powers_kernel: beta^t (double) and the reciprocal pairs of 1 - beta^t.
         bias1 = 1.0 - powers[0];
         bias2 = 1.0 - powers[1];
+        const float4 rp = *reinterpret_cast<const float4*>(powers + 2);
+        r1_hi = rp.x;
+        r1_lo = rp.y;
+        r2_hi = rp.z;
+        r2_lo = rp.w;
     }
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
          q += (long long)gridDim.x * blockDim.x) {
@@ -138,8 +145,10 @@ __global__ void adam_kernel(const float* __restrict__ grad, float* __restrict__ 
         const float nv = beta_2 * v[q] + one_minus_beta_2 * g * g;
         m[q] = nm;
         v[q] = nv;
-        const float m_hat = (float)((double)nm / bias1);
-        const float v_hat = (float)((double)nv / bias2);
+        // (float)((double)nm / (1 - beta_1^t)), (float)((double)nv / (1 - beta_2^t)) without FP64 division
+        // (the double is only formed on the rare fallback path).
+        const float m_hat = quotient_f64_to_f32(nm, r1_hi, r1_lo, bias1);
+        const float v_hat = quotient_f64_to_f32(nv, r2_hi, r2_lo, bias2);
         const float d = -(lr * m_hat / (sqrtf(v_hat) + eps));
         if (delta) delta[q] = d;
         if (w) {
@@ -153,11 +162,66 @@ __global__ void adam_kernel(const float* __restrict__ grad, float* __restrict__ 
     }
 }
 
+// adam_kernel for a weight matrix with its transposed copy: CTA per 32 x 32 tile (block 32 x 8), rows read
+// and written along j, the tile transposed through shared memory so that the copy wt (n_pre, ld) is written
+// along i too (the per-element transposed store of adam_kernel touches one 32-byte sector per element).
+// The arithmetic per element is adam_kernel's.
+__global__ void __launch_bounds__(256)
+adam_tiled_kernel(const float* __restrict__ grad, float* __restrict__ m, float* __restrict__ v, float beta_1,
+                  float one_minus_beta_1, float beta_2, float one_minus_beta_2, double bias1, double bias2,
+                  const double* __restrict__ powers, float r1_hi, float r1_lo, float r2_hi, float r2_lo, float lr,
+                  float eps, float* __restrict__ delta, float* __restrict__ w, float* __restrict__ wt, int n_post,
+                  int n_pre, int ld) {
+    __shared__ float tile[32][33];
+    if (powers) {
+        bias1 = 1.0 - powers[0];
+        bias2 = 1.0 - powers[1];
+        const float4 rp = *reinterpret_cast<const float4*>(powers + 2);
+        r1_hi = rp.x;
+        r1_lo = rp.y;
+        r2_hi = rp.z;
+        r2_lo = rp.w;
+    }
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int j = j0 + tx;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int i = i0 + ty + 8 * r;
+        if (i < n_post && j < n_pre) {
+            const long long q = (long long)i * n_pre + j;
+            const float g = grad[q];
+            const float nm = beta_1 * m[q] + one_minus_beta_1 * g;
+            const float nv = beta_2 * v[q] + one_minus_beta_2 * g * g;
+            m[q] = nm;
+            v[q] = nv;
+            const float m_hat = quotient_f64_to_f32(nm, r1_hi, r1_lo, bias1);
+            const float v_hat = quotient_f64_to_f32(nv, r2_hi, r2_lo, bias2);
+            const float d = -(lr * m_hat / (sqrtf(v_hat) + eps));
+            if (delta) delta[q] = d;
+            const float nw = w[q] + d;
+            w[q] = nw;
+            tile[ty + 8 * r][tx] = nw;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int jj = j0 + ty + 8 * r;  // row of wt
+        const int ii = i0 + tx;          // column of wt
+        if (jj < n_pre && ii < n_post) wt[(long long)jj * ld + ii] = tile[tx][ty + 8 * r];
+    }
+}
+
 // beta_1^t, beta_2^t kept on the device so that a captured step can advance t without host input.
 __global__ void adam_powers_kernel(double* powers, float beta_1, float beta_2) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         powers[0] *= (double)beta_1;
         powers[1] *= (double)beta_2;
+        float4 rp;
+        reciprocal_pair(1.0 - powers[0], rp.x, rp.y);
+        reciprocal_pair(1.0 - powers[1], rp.z, rp.w);
+        *reinterpret_cast<float4*>(powers + 2) = rp;
     }
 }
 
@@ -252,10 +316,21 @@ extern "C" int bats_adam_step(const float* grad, float* m, float* v, long long c
     BATS_REQUIRE(grad && m && v && (delta || weights), BATS_ERR_NULL, "adam_step: null pointer");
     BATS_REQUIRE(!weights_t || ((long long)n_post * n_pre == count && ld >= n_post), BATS_ERR_BAD_SHAPE,
                  "adam_step: transposed copy needs n_post*n_pre == count");
-    bats::adam_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
-        grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
-        bias_correction_1, bias_correction_2, nullptr, learning_rate, epsilon, delta, weights, weights_t, n_post, n_pre,
-        ld);
+    float r1h, r1l, r2h, r2l;
+    bats::reciprocal_pair(bias_correction_1, r1h, r1l);
+    bats::reciprocal_pair(bias_correction_2, r2h, r2l);
+    if (weights && weights_t) {
+        dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
+        bats::adam_tiled_kernel<<<grid, block, 0, stream>>>(
+            grad, m, v, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
+            bias_correction_1, bias_correction_2, nullptr, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta, weights,
+            weights_t, n_post, n_pre, ld);
+    } else {
+        bats::adam_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
+            grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
+            bias_correction_1, bias_correction_2, nullptr, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta, weights,
+            weights_t, n_post, n_pre, ld);
+    }
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -276,9 +351,17 @@ extern "C" int bats_adam_step_device(const float* grad, float* m, float* v, long
     BATS_REQUIRE(grad && m && v && weights && powers, BATS_ERR_NULL, "adam_step_device: null pointer");
     BATS_REQUIRE(!weights_t || ((long long)n_post * n_pre == count && ld >= n_post), BATS_ERR_BAD_SHAPE,
                  "adam_step_device: transposed copy needs n_post*n_pre == count");
-    bats::adam_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
-        grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0, 0.0,
-        powers, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre, ld);
+    if (weights_t) {
+        dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
+        bats::adam_tiled_kernel<<<grid, block, 0, stream>>>(
+            grad, m, v, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0, 0.0,
+            powers, 0.0f, 0.0f, 0.0f, 0.0f, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre, ld);
+    } else {
+        bats::adam_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
+            grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0,
+            0.0, powers, 0.0f, 0.0f, 0.0f, 0.0f, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre,
+            ld);
+    }
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -7,6 +7,7 @@
 // larger weights, by factor * |w|.
 #include <cmath>
 #include "abi_util.h"
+#include "disc.cuh"
 
 namespace bats {
 
@@ -17,8 +18,8 @@ namespace bats {
 // reference's compute_deltas_kernel receives it.
 __global__ void nadam_kernel(const float* __restrict__ grad, float* __restrict__ m, float* __restrict__ v,
                              long long count, float beta_1, float one_minus_beta_1, float beta_2,
-                             float one_minus_beta_2, double bias1, double bias2, float bias1_f, float lr, float eps,
-                             float* __restrict__ delta) {
+                             float one_minus_beta_2, double bias1, double bias2, float bias1_f, float r1_hi,
+                             float r1_lo, float r2_hi, float r2_lo, float lr, float eps, float* __restrict__ delta) {
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
          q += (long long)gridDim.x * blockDim.x) {
         const float g = grad[q];
@@ -26,8 +27,8 @@ __global__ void nadam_kernel(const float* __restrict__ grad, float* __restrict__
         const float nv = beta_2 * v[q] + one_minus_beta_2 * g * g;
         m[q] = nm;
         v[q] = nv;
-        const float m_hat = (float)((double)nm / bias1);
-        const float v_hat = (float)((double)nv / bias2);
+        const float m_hat = quotient_f64_to_f32(nm, r1_hi, r1_lo, bias1);  // (float)((double)nm / bias1)
+        const float v_hat = quotient_f64_to_f32(nv, r2_hi, r2_lo, bias2);
         delta[q] = -(lr / (sqrtf(v_hat) + eps)) * (beta_1 * m_hat + one_minus_beta_1 * g / bias1_f);
     }
 }
@@ -79,9 +80,13 @@ extern "C" int bats_nadam_step(const float* grad, float* m, float* v, long long 
     BATS_REQUIRE(count >= 0, BATS_ERR_BAD_SHAPE, "nadam_step: bad shape");
     if (count == 0) return BATS_OK;
     BATS_REQUIRE(grad && m && v && delta, BATS_ERR_NULL, "nadam_step: null pointer");
+    float r1h, r1l, r2h, r2l;
+    bats::reciprocal_pair(bias_correction_1, r1h, r1l);
+    bats::reciprocal_pair(bias_correction_2, r2h, r2l);
     bats::nadam_kernel<<<bats::grid_for(count, 256), 256, 0, stream>>>(
         grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
-        bias_correction_1, bias_correction_2, (float)bias_correction_1, learning_rate, epsilon, delta);
+        bias_correction_1, bias_correction_2, (float)bias_correction_1, r1h, r1l, r2h, r2l, learning_rate, epsilon,
+        delta);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

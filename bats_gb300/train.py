@@ -86,7 +86,7 @@ class FCTrainStep:
         self.graph: Optional[torch.cuda.CUDAGraph] = None
         self.capture_error = None
         # beta_1^t, beta_2^t on the device, advanced by one launch per step (keeps the step capturable).
-        self.powers = torch.ones((2,), dtype=torch.float64, device=dev)
+        self.powers = torch.tensor([1.0, 1.0, 0.0, 0.0], dtype=torch.float64, device=dev)
         # Host staging for end-to-end steps.
         self.h_times = torch.empty(self.in_times.shape, dtype=f32, pin_memory=True)
         self.h_labels = torch.empty((B,), dtype=i32, pin_memory=True)

@@ -298,6 +298,38 @@ def run_ours(args, dist, rank, world):
     return result
 
 
+def profile_one_step(workload):
+    """One eager train step with an NVTX range per launch (L1.sort, L1.forward, ...), after set-up, autotuning
+    and 3 warm-up steps, for targeted ncu captures: ncu --nvtx --nvtx-include "L2.forward/" ..."""
+    import torch
+    if workload == "batching":
+        from bats_gb300.train import FCLayerSpec, FCTrainStep
+        t, labels, _ = batching_inputs()
+        rng = np.random.default_rng(12)
+        sizes = [1024, 1024, 20]
+        ws = [torch.tensor(rng.uniform(-1, 1, (o, i)).astype(np.float32)) for i, o in zip(sizes[:-1], sizes[1:])]
+        specs = [FCLayerSpec(1024, TAU_S, 0.2, 0.2, K_SPIKE), FCLayerSpec(20, TAU_S, 1.3, 1.3, K_SPIKE)]
+        ts = FCTrainStep(t.shape[0], 1024, t.shape[2], specs, ws, TARGET_TRUE, TARGET_FALSE, learning_rate=LR,
+                         max_simulation=MAX_SIM)
+        ts.set_inputs(torch.tensor(t), torch.tensor(labels))
+    else:
+        ts = build_train_step(workload)
+    ts.autotune()
+    for _ in range(3):
+        ts.step()
+    flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    flush_l2(flush)
+    torch.cuda.synchronize()
+    from bats_gb300._lib import stream_ptr
+    s = stream_ptr()
+    for name, fn in ts.launches:
+        torch.cuda.nvtx.range_push(name)
+        fn(s)
+        torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    print(json.dumps({"profiled_step": workload, "launches": [n for n, _ in ts.launches]}))
+
+
 def plain_api_rate(variant, steps, flush):
     import torch
     from bats_gb300 import Network, SpikeCountClassLoss
@@ -527,6 +559,9 @@ def main():
     ap.add_argument("--workload", default="all", choices=["all", "literal", "active", "serving", "conv", "batching"],
                     help="all (default): every measurement; otherwise only that one (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline (profiling runs)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="with --workload literal|active|batching: set up and autotune the step, then run one "
+                         "eager step with an NVTX range named after every launch (for ncu --nvtx-include)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -543,6 +578,10 @@ def main():
                 "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
+        return
+
+    if args.profile_step:
+        profile_one_step(args.workload)
         return
 
     # CPU baseline first (spawned workers, before any GPU context exists in this process).

@@ -220,8 +220,9 @@ int bats_adam_step(const float* grad, float* m, float* v, long long count, float
                    float learning_rate, double bias_correction_1, double bias_correction_2, float* delta,
                    float* weights, float* weights_t, int n_post, int n_pre, int ld, cudaStream_t stream);
 
-/* Device-side Adam bias-correction state for captured steps: powers[0..1] (double) *= beta_1, beta_2.
- * Start from {1, 1}; call once per step before bats_adam_step_device. Replaces the host-side
+/* Device-side Adam bias-correction state for captured steps, 4 doubles: powers[0..1] *= beta_1, beta_2,
+ * then powers[2..3] hold (as four floats) the pairs hi + lo ~= 1 / (1 - beta_i^t) the update kernel divides by.
+ * Start from {1, 1, 0, 0}; call once per step before bats_adam_step_device. Replaces the host-side
  * `self.__t += 1` and `beta ** t` of AdamOptimizer.step (bats/Optimizers/AdamOptimizer.py:36, 49-50). */
 int bats_adam_powers_advance(double* powers, float beta_1, float beta_2, cudaStream_t stream);
 

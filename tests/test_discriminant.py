@@ -1,8 +1,13 @@
-"""The FC solver's discriminant without FP64 (bats_gb300/csrc/disc.cuh) against the reference's double
-expression (float)((double)fl(b*b) - 4.0*a*c) (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:57),
-bit for bit, on the host: random operands over the solver's ranges, near-tangential cases (b^2 ~ 4ac),
-mixed signs, and adversarial cases whose exact value lies at or near a midpoint between floats, at or
-next to powers of two, where rounding twice (to double, then to float) differs from rounding once."""
+"""FP64-free evaluations (bats_gb300/csrc/disc.cuh) against the double expressions they replace, bit for
+bit, on the host:
+* the FC solver's discriminant (float)((double)fl(b*b) - 4.0*a*c)
+  (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:57): random operands over the solver's ranges,
+  near-tangential cases (b^2 ~ 4ac), mixed signs, and adversarial cases whose exact value lies at or near a
+  midpoint between floats, at or next to powers of two, where rounding twice (to double, then to float)
+  differs from rounding once;
+* the optimizers' bias-corrected moments (float)((double)m / (1 - beta^t)): bias corrections of Adam's
+  and NAdam's betas over thousands of steps, random and power-of-two numerators, and numerators placed at
+  float midpoints of the quotient."""
 import os
 import shutil
 import subprocess
@@ -47,6 +52,22 @@ int main(int argc, char** argv) {
         if (q & 16) p = std::ldexp(1.0, e0 - 24) * (1.0 + (U(rng) - 0.5) * std::ldexp(1.0, -(int)(U(rng) * 30)));
         if (q & 32) p = -p;
         check(b2, (float)(p / (4.0 * cc)), cc);
+    }
+    // Quotients x / d (d > 0) near float midpoints.
+    for (long long q = 0; q < n; ++q) {
+        double d = q % 2 ? 1.0 - std::pow(0.999, 1 + (int)(U(rng) * 5000)) : 1.0 - std::pow(0.9, 1 + (int)(U(rng) * 200));
+        float x = (float)((U(rng) - 0.5) * std::pow(10.0, (U(rng) - 0.5) * 16));
+        if (q % 3 == 0) {
+            float m = (float)std::ldexp(1.0 + U(rng), (int)(U(rng) * 30) - 15);
+            double mid = (double)m + std::ldexp((double)std::nextafter(m, 1e30f) - (double)m, -1);
+            x = (float)(mid * d);
+        }
+        float hi, lo;
+        bats::reciprocal_pair(d, hi, lo);
+        float a = bats::quotient_f64_to_f32(x, hi, lo, d), b = bats::quotient_ref64(x, d);
+        uint32_t ai, bi; std::memcpy(&ai, &a, 4); std::memcpy(&bi, &b, 4);
+        ++total;
+        if (ai != bi) { if (bad < 5) std::printf("quotient mismatch x=%a d=%a got %a want %a\n", x, d, a, b); ++bad; }
     }
     // Special values.
     const float sp[] = {0.0f, -0.0f, 1e-45f, 1e-30f, 1e30f, 3e38f, INFINITY, -INFINITY, NAN, 1.0f, -1.0f};

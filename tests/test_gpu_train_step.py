@@ -1,0 +1,106 @@
+"""The batched, graph-captured train step (bats_gb300.train.FCTrainStep) against the layer-by-layer drop-in
+API on the same network, inputs and Adam settings: forward, spike-count loss, exact backward with the
+batch-mean gradient and Adam.
+
+* The first step's loss is identical (same forward kernels and loss).
+* After each of 3 steps the weights agree within 1e-6 of the weight scale: the batch mean is the same sum
+  taken in another order (group partials instead of per-sample gradients and torch.mean), so the
+  gradients differ in the last bits, and Adam's first steps move every weight by about the learning rate.
+* Replaying the captured CUDA graph gives the eager step's result bit for bit, and the autotuned step
+  (other kernel variants and gradient groups) agrees with the untuned one within the same tolerance.
+"""
+import numpy as np
+import pytest
+import torch
+
+from bats_gb300 import Network, SpikeCountClassLoss
+from bats_gb300.Layers import InputLayer, LIFLayer
+from bats_gb300.Optimizers import AdamOptimizer
+from bats_gb300.autotune import Autotuner
+from bats_gb300.train import FCLayerSpec, FCTrainStep
+from tests._helpers import mnist_like_input
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [784, 120, 10]
+THETAS = [0.2, 1.3]
+TAU_S, K, LR, MAX_SIM = 0.13, 20, 3e-3, 0.2
+
+
+def case(B=32, seed=0):
+    t, n = mnist_like_input(B, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    ws = [rng.uniform(-1, 1, (o, i)).astype(np.float32) for i, o in zip(SIZES[:-1], SIZES[1:])]
+    labels = rng.integers(0, SIZES[-1], B).astype(np.int32)
+    return t, n, ws, labels
+
+
+def make_step(t, ws, labels):
+    specs = [FCLayerSpec(o, TAU_S, th, th, K) for o, th in zip(SIZES[1:], THETAS)]
+    ts = FCTrainStep(t.shape[0], SIZES[0], 1, specs, [torch.tensor(w) for w in ws], 15.0, 3.0, learning_rate=LR,
+                     max_simulation=MAX_SIM)
+    ts.set_inputs(torch.tensor(t), torch.tensor(labels))
+    return ts
+
+
+def api_steps(t, n, ws, labels, steps):
+    net = Network()
+    prev = InputLayer(n_neurons=SIZES[0], name="in")
+    net.add_layer(prev, input=True)
+    layers = []
+    for i, (w, th) in enumerate(zip(ws, THETAS)):
+        L = LIFLayer(prev, n_neurons=w.shape[0], tau_s=TAU_S, theta=th, delta_theta=th, max_n_spike=K,
+                     weight_initializer=lambda a, b, w=w: torch.tensor(w, device="cuda"), name=f"l{i}")
+        net.add_layer(L)
+        layers.append(L)
+        prev = L
+    loss_fn = SpikeCountClassLoss(15.0, 3.0)
+    opt = AdamOptimizer(learning_rate=LR)
+    lab = torch.tensor(labels, device="cuda")
+    out = []
+    for _ in range(steps):
+        net.reset()
+        net.forward(t, n, max_simulation=MAX_SIM, training=True)
+        sp, nsp = net.output_spike_trains
+        loss, err = loss_fn.compute_loss_and_errors(sp, nsp, lab)
+        g = net.backward(err)
+        net.apply_deltas(opt.step([None if x is None else x.mean(0) for x in g]))
+        out.append((loss.clone(), [L.weights.clone() for L in layers]))
+    return out
+
+
+def test_train_step_matches_layer_api(cuda):
+    t, n, ws, labels = case()
+    ref = api_steps(t, n, ws, labels, 3)
+    ts = make_step(t, ws, labels)
+    for k in range(3):
+        ts.step()
+        torch.cuda.synchronize()
+        if k == 0:
+            assert torch.equal(ts.loss, ref[0][0]), "first-step loss differs from the layer API"
+        for w, rw in zip(ts.W, ref[k][1]):
+            assert float((w - rw).abs().max()) <= 1e-6 * float(rw.abs().max()), f"step {k}"
+    assert int(ts.out[0][0].sum()) > 0, "the hidden layer should spike"
+
+
+def test_graph_replay_equals_eager_and_autotune_keeps_results(cuda):
+    t, n, ws, labels = case(seed=3)
+    eager = make_step(t, ws, labels)
+    graphed = make_step(t, ws, labels)
+    assert graphed.try_capture(), graphed.capture_error  # runs one eager step, then captures
+    eager.step()
+    for _ in range(2):
+        eager.step()
+        graphed.replay()
+    torch.cuda.synchronize()
+    for a, b in zip(eager.W, graphed.W):
+        assert torch.equal(a, b)
+    tuned = make_step(t, ws, labels)
+    tuned.autotune(Autotuner(path=None), force=True)
+    plain = make_step(t, ws, labels)
+    for _ in range(2):
+        tuned.step()
+        plain.step()
+    torch.cuda.synchronize()
+    for a, b in zip(tuned.W, plain.W):
+        assert float((a - b).abs().max()) <= 1e-6 * float(b.abs().max())
