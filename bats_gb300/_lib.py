@@ -45,6 +45,9 @@ SIGNATURES = {
     "bats_conv_forward": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                   c_float, c_float, c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_events_to_trains": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
+    "bats_events_to_trains_csr": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
+    "bats_serve_fc_batch": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_int, c_int, c_vp, c_vp, c_vp,
+                                    c_vp, c_int, c_vp, c_size, c_vp, c_vp, c_vp, c_vp]),
     "bats_events_max_per_neuron": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_vp, c_vp]),
     "bats_pool_forward": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
     "bats_backward_prep": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
@@ -103,6 +106,15 @@ def load():
             fn.argtypes = args
         _lib = lib
         return lib
+
+
+class BatsFcLayer(ctypes.Structure):
+    """struct BatsFcLayer of include/bats_gb300.h (one layer of bats_serve_fc_batch)."""
+    _fields_ = [("n_pre", c_int), ("k_pre", c_int), ("n_post", c_int), ("k_post", c_int), ("weights_t", c_vp),
+                ("ld", c_int), ("tau_s", c_float), ("tau", c_float), ("c", c_float), ("delta_theta_tau", c_float),
+                ("max_simulation", c_float), ("algo", c_int), ("events", c_vp), ("slots", c_vp),
+                ("ev_count", c_vp), ("n_spikes", c_vp), ("a", c_vp), ("x", c_vp), ("times", c_vp),
+                ("post_exp_tau", c_vp)]
 
 
 def call(name: str, *args):

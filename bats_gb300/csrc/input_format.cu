@@ -16,9 +16,9 @@ namespace bats {
 constexpr int CONV_WARPS = 4;
 
 __global__ void __launch_bounds__(CONV_WARPS * 32)
-events_to_trains_kernel(const int* __restrict__ indices, const float* __restrict__ times, int batch, int max_events,
-                        int n_neurons, int k_cap, float* __restrict__ out_times, int* __restrict__ out_counts,
-                        int* __restrict__ overflow) {
+events_to_trains_kernel(const int* __restrict__ indices, const float* __restrict__ times,
+                        const int* __restrict__ offsets, int batch, int max_events, int n_neurons, int k_cap,
+                        float* __restrict__ out_times, int* __restrict__ out_counts, int* __restrict__ overflow) {
     const int lane = threadIdx.x & 31;
     const int s = blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);
     if (s >= batch) return;
@@ -27,12 +27,15 @@ events_to_trains_kernel(const int* __restrict__ indices, const float* __restrict
     for (long long q = lane; q < (long long)n_neurons * k_cap; q += 32) out_times[tb + q] = BATS_INF;
     for (int q = lane; q < n_neurons; q += 32) cnt[q] = 0;
     __syncwarp();
-    const int* idx = indices + (long long)s * max_events;
-    const float* tm = times + (long long)s * max_events;
+    // Padded rows (B, max_events), or with offsets the events offsets[s] .. offsets[s + 1] of a flat list.
+    const long long first = offsets ? (long long)offsets[s] : (long long)s * max_events;
+    const int n_ev = offsets ? offsets[s + 1] - offsets[s] : max_events;
+    const int* idx = indices + first;
+    const float* tm = times + first;
     int dropped = 0;
-    for (int m0 = 0; m0 < max_events; m0 += 32) {
+    for (int m0 = 0; m0 < n_ev; m0 += 32) {
         const int m = m0 + lane;
-        int j = m < max_events ? idx[m] : -1;
+        int j = m < n_ev ? idx[m] : -1;
         // The sample ends at its first negative index.
         const unsigned neg = __ballot_sync(0xffffffffu, j < 0 || j >= n_neurons);
         const int stop = neg ? __ffs(neg) - 1 : 32;
@@ -105,7 +108,21 @@ extern "C" int bats_events_to_trains(const int* indices, const float* times, int
                  "events_to_trains: null pointer");
     const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
     bats::events_to_trains_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
-        indices, times, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+        indices, times, nullptr, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_events_to_trains_csr(const int* indices, const float* times, const int* offsets, int batch,
+                                         int n_neurons, int k_cap, float* out_times, int* out_counts, int* overflow,
+                                         cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_neurons >= 0 && k_cap > 0, BATS_ERR_BAD_SHAPE, "events_to_trains_csr: bad shape");
+    if (batch == 0 || n_neurons == 0) return BATS_OK;
+    BATS_REQUIRE(indices && times && offsets && out_times && out_counts, BATS_ERR_NULL,
+                 "events_to_trains_csr: null pointer");
+    const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
+    bats::events_to_trains_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
+        indices, times, offsets, batch, 0, n_neurons, k_cap, out_times, out_counts, overflow);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -4,13 +4,15 @@ Requests are spike-event lists of different lengths (neuron index, time). They a
 "lanes": each lane owns a CUDA stream and device-resident buffers for up to `max_batch` requests (event
 lists, spike trains, per-layer sorted events and outputs) plus pinned host staging, and the network's
 transposed weights are uploaded once. Whenever a lane is free and requests are waiting, the pending
-requests (up to max_batch, oldest first) are packed and launched on that lane: host -> device copy,
-event-list -> spike-train conversion, and per layer the event sort and the LIF forward, then the output
-spike counts and times are copied back. Several lanes are in flight at once, so requests that arrive while
-others are on the GPU start as soon as a lane frees up and their work overlaps on the device. The lane
-pool starts with one lane and grows, while every lane is busy and requests wait, up to max_lanes, each new
-lane only if the free HBM reported by the driver (cudaMemGetInfo) leaves room for it; admission refuses
-requests when free HBM (re-read at most every 5 ms) falls below a floor or the queue is full. The forward
+requests (up to max_batch, oldest first) are packed into one flat event list and launched on that lane
+with a single native call (bats_serve_fc_batch): host -> device copy, event-list -> spike-train
+conversion, and per layer the event sort and the LIF forward, then the output spike counts and times
+are copied back. Several lanes are in flight at once, so requests that arrive while
+others are on the GPU start as soon as a lane frees up and their work overlaps on the device. The number
+of lanes is max_lanes or as many as the free HBM reported by the driver (cudaMemGetInfo, times
+hbm_fraction) holds, all allocated up front so that serving never allocates; admission refuses requests
+when free HBM (re-read at most every 5 ms) falls below a floor or the queue is full. Many lanes of small
+batches (16 x 16 by default) keep the per-batch latency short while the lanes together fill the GPU. The forward
 kernel variant of every layer is chosen per batch-size bucket by autotune(). A request's result does not
 depend on which other requests share its batch (the kernels treat samples independently), which
 tests/test_gpu_serving.py checks bit for bit.
@@ -18,6 +20,9 @@ tests/test_gpu_serving.py checks bit for bit.
 from __future__ import annotations
 
 import collections
+import contextlib
+import ctypes
+import gc
 import time
 from dataclasses import dataclass, field
 from typing import Deque, Dict, List, Optional, Sequence
@@ -26,8 +31,22 @@ import numpy as np
 import torch
 
 from . import kernels as K
-from ._lib import call, ptr
+from ._lib import BatsFcLayer, call, ptr
 from .autotune import Autotuner, get_tuner
+
+
+@contextlib.contextmanager
+def no_gc_pauses():
+    """Automatic garbage collection off while serving (restored afterwards): a generation-2 collection
+    over the tens of thousands of request and result objects of a busy loop stops the host for about
+    30 ms, which shows up directly in the latency tail. The serving objects hold no reference cycles."""
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if was:
+            gc.enable()
 
 
 @dataclass
@@ -66,10 +85,13 @@ class _Lane:
         B, E = s.max_batch, s.max_events
         f32, i32 = torch.float32, torch.int32
         self.stream = torch.cuda.Stream(device=device)
-        self.h_idx = torch.empty((B, E), dtype=i32, pin_memory=True)
-        self.h_t = torch.empty((B, E), dtype=f32, pin_memory=True)
-        self.d_idx = torch.empty((B, E), dtype=i32, device=device)
-        self.d_t = torch.empty((B, E), dtype=f32, device=device)
+        # Flat event list of a batch (up to B * E events) + offsets, pinned on the host and on the device.
+        self.h_idx = torch.empty((B * E,), dtype=i32, pin_memory=True)
+        self.h_t = torch.empty((B * E,), dtype=f32, pin_memory=True)
+        self.h_off = torch.empty((B + 1,), dtype=i32, pin_memory=True)
+        self.d_idx = torch.empty((B * E,), dtype=i32, device=device)
+        self.d_t = torch.empty((B * E,), dtype=f32, device=device)
+        self.d_off = torch.empty((B + 1,), dtype=i32, device=device)
         self.trains = torch.empty((B, s.n_inputs, s.k_in), dtype=f32, device=device)
         self.train_counts = torch.empty((B, s.n_inputs), dtype=i32, device=device)
         self.overflow = torch.zeros((1,), dtype=i32, device=device)
@@ -84,15 +106,28 @@ class _Lane:
         self.ws = torch.empty(max(256, s.sort_ws), dtype=torch.uint8, device=device)
         self.h_counts = torch.empty(self.out[-1][0].shape, dtype=i32, pin_memory=True)
         self.h_times = torch.empty(self.out[-1][3].shape, dtype=f32, pin_memory=True)
-        self.h_overflow = torch.empty((1,), dtype=i32, pin_memory=True)
+        self.h_overflow = torch.zeros((1,), dtype=i32, pin_memory=True)
         self.done = torch.cuda.Event()
         self.batch: List[Request] = []
         # numpy views of the pinned buffers (no per-request torch calls on the host path)
-        self.np_idx = self.h_idx.numpy().reshape(-1)
-        self.np_t = self.h_t.numpy().reshape(-1)
+        self.np_idx = self.h_idx.numpy()
+        self.np_t = self.h_t.numpy()
+        self.np_off = self.h_off.numpy()
         self.np_counts = self.h_counts.numpy()
         self.np_times = self.h_times.numpy()
         self.np_overflow = self.h_overflow.numpy()
+        # The layer descriptors of bats_serve_fc_batch, pointing at this lane's buffers.
+        self.layers = (BatsFcLayer * len(s.specs))()
+        n_prev, k_prev = s.n_inputs, s.k_in
+        for li, spec in enumerate(s.specs):
+            tau32, c, dtt = s.consts[li]
+            n, a, x, t, z = self.out[li]
+            self.layers[li] = BatsFcLayer(n_prev, k_prev, spec.n_neurons, spec.max_n_spike, ptr(s.wt[li]),
+                                          s.wt[li].shape[1], float(np.float32(spec.tau_s)), float(tau32), float(c),
+                                          float(dtt), float(np.float32(s.max_sim)), K.FWD_AUTO,
+                                          ptr(self.ev[li].events), ptr(self.ev[li].slots), ptr(self.ev[li].counts),
+                                          ptr(n), ptr(a), ptr(x), ptr(t), ptr(z))
+            n_prev, k_prev = spec.n_neurons, spec.max_n_spike
 
     def busy(self) -> bool:
         return bool(self.batch) and not self.done.query()
@@ -101,7 +136,7 @@ class _Lane:
     def bytes_needed(server: "InferenceServer") -> int:
         s = server
         B, E = s.max_batch, s.max_events
-        total = B * E * 8 + B * s.n_inputs * (s.k_in * 4 + 4)
+        total = B * E * 8 + (B + 1) * 4 + B * s.n_inputs * (s.k_in * 4 + 4)
         n_prev, k_prev = s.n_inputs, s.k_in
         for spec in s.specs:
             total += B * n_prev * k_prev * 20 + B * 4
@@ -112,7 +147,7 @@ class _Lane:
 
 class InferenceServer:
     def __init__(self, weights: Sequence, specs: Sequence[LayerSpec], n_inputs: int, max_events: int,
-                 k_in: int = 32, max_batch: int = 64, max_lanes: int = 4, hbm_fraction: float = 0.5,
+                 k_in: int = 32, max_batch: int = 16, max_lanes: int = 16, hbm_fraction: float = 0.5,
                  max_simulation: float = float("inf"), max_pending: int = 1 << 16, device="cuda"):
         self.dev = torch.device(device)
         self.specs = list(specs)
@@ -134,9 +169,12 @@ class InferenceServer:
         self.max_lanes = int(max_lanes)
         self.max_pending = int(max_pending)
         self._free_hbm, self._free_t = 0, -1.0
-        if self._free_hbm_now(force=True) * self.hbm_fraction < self.lane_bytes:
+        # Lanes are the batch slots: as many as max_lanes, or as free HBM (times hbm_fraction) allows, all
+        # allocated here so that no allocation happens while serving.
+        n_lanes = int(min(self.max_lanes, (self._free_hbm_now(force=True) * self.hbm_fraction) // self.lane_bytes))
+        if n_lanes < 1:
             raise RuntimeError(f"not enough free HBM for one lane ({self.lane_bytes} bytes)")
-        self.lanes = [_Lane(self, self.dev)]
+        self.lanes = [_Lane(self, self.dev) for _ in range(n_lanes)]
         self.pending: Deque[Request] = collections.deque()
         self.results: Dict[int, Result] = {}
         self.rejected: List[int] = []
@@ -165,43 +203,28 @@ class InferenceServer:
         self.pending.append(req)
         return True
 
-    def _grow(self) -> Optional[_Lane]:
-        """A new lane when every lane is busy, requests wait and free HBM allows it."""
-        if len(self.lanes) >= self.max_lanes:
-            return None
-        if self._free_hbm_now(force=True) * self.hbm_fraction < self.lane_bytes + self.HBM_FLOOR:
-            return None
-        lane = _Lane(self, self.dev)
-        self.lanes.append(lane)
-        return lane
-
     # -- device work ------------------------------------------------------------------------------------
     def _launch(self, lane: _Lane, batch: List[Request]) -> None:
+        """Pack the batch as one flat event list + offsets into the lane's pinned buffers and enqueue the whole
+        batch (copies, conversion, every layer, copies back) with one call of bats_serve_fc_batch."""
         B = len(batch)
-        L = max(1, max(len(r.indices) for r in batch))
-        # Pack the batch contiguously as (B, L); a sample ends at its first negative index.
-        hi = lane.np_idx[:B * L].reshape(B, L)
-        ht = lane.np_t[:B * L].reshape(B, L)
-        for q, r in enumerate(batch):
-            n = len(r.indices)
-            hi[q, :n] = r.indices
-            ht[q, :n] = r.times
-            if n < L:
-                hi[q, n] = -1
+        lens = np.fromiter((len(r.indices) for r in batch), dtype=np.int64, count=B)
+        off = lane.np_off[:B + 1]
+        off[0] = 0
+        np.cumsum(lens, out=off[1:])
+        total = int(off[B])
+        if total:
+            np.concatenate([r.indices for r in batch], out=lane.np_idx[:total], casting="unsafe")
+            np.concatenate([r.times for r in batch], out=lane.np_t[:total], casting="unsafe")
+        for li, algo in enumerate(self._algos_for(B)):
+            lane.layers[li].algo = int(algo)
         lane.batch = batch
         with torch.cuda.stream(lane.stream):
-            s = lane.stream.cuda_stream
-            d_idx = lane.d_idx.view(-1)[:B * L]
-            d_t = lane.d_t.view(-1)[:B * L]
-            d_idx.copy_(lane.h_idx.view(-1)[:B * L], non_blocking=True)
-            d_t.copy_(lane.h_t.view(-1)[:B * L], non_blocking=True)
-            lane.overflow.zero_()
-            call("bats_events_to_trains", ptr(d_idx), ptr(d_t), B, L, self.n_inputs, self.k_in,
-                 ptr(lane.trains), ptr(lane.train_counts), ptr(lane.overflow), s)
-            self._layers(lane, B, self._algos_for(B), s)
-            lane.h_counts[:B].copy_(lane.out[-1][0][:B], non_blocking=True)
-            lane.h_times[:B].copy_(lane.out[-1][3][:B], non_blocking=True)
-            lane.h_overflow.copy_(lane.overflow, non_blocking=True)
+            call("bats_serve_fc_batch", lane.h_idx.data_ptr(), lane.h_t.data_ptr(), lane.h_off.data_ptr(), B, total,
+                 ptr(lane.d_idx), ptr(lane.d_t), ptr(lane.d_off), self.n_inputs, self.k_in, ptr(lane.trains),
+                 ptr(lane.train_counts), ptr(lane.overflow), ctypes.addressof(lane.layers), len(self.specs),
+                 ptr(lane.ws), lane.ws.numel(), lane.h_counts.data_ptr(), lane.h_times.data_ptr(),
+                 lane.h_overflow.data_ptr(), lane.stream.cuda_stream)
             lane.done.record(lane.stream)
         self.batches_launched += 1
 
@@ -268,19 +291,21 @@ class InferenceServer:
 
     def _collect(self, lane: _Lane) -> List[Result]:
         now = time.perf_counter()
-        out = []
         if int(lane.np_overflow[0]) != 0:
             raise RuntimeError("a request has more spikes on one input neuron than the server's k_in")
+        B = len(lane.batch)
+        counts = lane.np_counts[:B].copy()  # one copy per batch; results are views into it
+        times = lane.np_times[:B].copy()
+        out = []
         for q, r in enumerate(lane.batch):
-            res = Result(r.rid, lane.np_counts[q].copy(), lane.np_times[q].copy(), r.t_arrival, now)
+            res = Result(r.rid, counts[q], times[q], r.t_arrival, now)
             self.results[r.rid] = res
             out.append(res)
         lane.batch = []
         return out
 
     def pump(self) -> List[Result]:
-        """Collect finished lanes and launch pending requests on free lanes (growing the lane pool while
-        free HBM allows). Non-blocking."""
+        """Collect finished lanes and launch pending requests on free lanes. Non-blocking."""
         done = []
         for lane in self.lanes:
             if lane.batch and lane.done.query():
@@ -291,17 +316,13 @@ class InferenceServer:
             if lane.batch:
                 continue
             self._launch(lane, [self.pending.popleft() for _ in range(min(self.max_batch, len(self.pending)))])
-        while self.pending:
-            lane = self._grow()
-            if lane is None:
-                break
-            self._launch(lane, [self.pending.popleft() for _ in range(min(self.max_batch, len(self.pending)))])
         return done
 
     def drain(self) -> List[Result]:
         out = []
-        while self.pending or any(l.batch for l in self.lanes):
-            out.extend(self.pump())
+        with no_gc_pauses():
+            while self.pending or any(l.batch for l in self.lanes):
+                out.extend(self.pump())
         return out
 
     def infer(self, requests: Sequence[Request]) -> List[Result]:
@@ -348,12 +369,13 @@ def run_poisson(server: InferenceServer, requests: Sequence[Request], rate: floa
     arrivals = t0 + np.cumsum(gaps)
     q = 0
     results = []
-    while q < len(requests) or server.pending or any(l.batch for l in server.lanes):
-        now = time.perf_counter()
-        while q < len(requests) and arrivals[q] <= now:
-            server.submit(requests[q], now=arrivals[q])
-            q += 1
-        results.extend(server.pump())
+    with no_gc_pauses():
+        while q < len(requests) or server.pending or any(l.batch for l in server.lanes):
+            now = time.perf_counter()
+            while q < len(requests) and arrivals[q] <= now:
+                server.submit(requests[q], now=arrivals[q])
+                q += 1
+            results.extend(server.pump())
     return results
 
 

@@ -520,7 +520,7 @@ def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float =
     import torch
     from bats_gb300.serving import InferenceServer, latency_stats, make_network, make_requests, run_poisson
     ws, specs = make_network()
-    server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=64, max_lanes=4)
+    server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=16, max_lanes=16)
     pool = make_requests(1000, seed=7)
     tuned = server.autotune(pool[:64])
 

@@ -120,6 +120,11 @@ int bats_events_to_trains(const int* indices, const float* times, int batch, int
 
 /* Largest per-neuron spike count of each sample of an event list (the K of convert_to_spike_per_neuron,
  * Wrappers/Inference/convert_to_spike_per_neuron.py:11-18), using scratch_counts (B, N). */
+/* bats_events_to_trains over a flat event list: sample s owns events offsets[s] .. offsets[s + 1] - 1
+ * (offsets: batch + 1 ints, device). No counterpart in the reference (its input is padded). */
+int bats_events_to_trains_csr(const int* indices, const float* times, const int* offsets, int batch, int n_neurons,
+                              int k_cap, float* out_times, int* out_counts, int* overflow, cudaStream_t stream);
+
 int bats_events_max_per_neuron(const int* indices, int batch, int max_events, int n_neurons, int* scratch_counts,
                                int* out_max, cudaStream_t stream);
 
@@ -261,6 +266,39 @@ int bats_add_deltas(float* weights, const float* delta, long long count, float* 
 
 /* out (cols, ld) = in (rows, cols)^T. Builds the transposed weights read by the FC kernels. */
 int bats_transpose(const float* in, int rows, int cols, float* out, int ld, cudaStream_t stream);
+
+/* One fully-connected layer of a served network, for bats_serve_fc_batch: shapes, transposed weights
+ * (n_pre, ld), constants as for bats_lif_forward_fc (tau = 2 tau_s, c = theta/tau, delta_theta/tau), the
+ * forward kernel variant, and the layer's device buffers for `batch` samples: sorted events
+ * (n_pre*k_pre records per sample), their slots and counts, and the outputs (n_spikes (B, n_post);
+ * a, x, times, post_exp_tau (B, n_post, k_post)). */
+typedef struct BatsFcLayer {
+    int n_pre, k_pre, n_post, k_post;
+    const float* weights_t;
+    int ld;
+    float tau_s, tau, c, delta_theta_tau, max_simulation;
+    int algo;
+    void* events;
+    int* slots;
+    int* ev_count;
+    int* n_spikes;
+    float* a;
+    float* x;
+    float* times;
+    float* post_exp_tau;
+} BatsFcLayer;
+
+/* One inference batch of an FC network, enqueued on `stream` with no host synchronisation: copies the flat
+ * event list (h_indices/h_times, total_events entries) and offsets (batch + 1) from pinned host memory,
+ * builds the input spike trains (k_in slots per input neuron, overflow counted in d_overflow), runs every
+ * layer's sort and forward, and copies the last layer's counts (B, n_post) and times (B, n_post, k_post)
+ * and the overflow count back to pinned host memory. No counterpart in the reference (the serving
+ * pattern's batch step). */
+int bats_serve_fc_batch(const int* h_indices, const float* h_times, const int* h_offsets, int batch, int total_events,
+                        int* d_indices, float* d_times, int* d_offsets, int n_inputs, int k_in, float* d_trains,
+                        int* d_train_counts, int* d_overflow, const BatsFcLayer* layers, int n_layers,
+                        void* sort_workspace, size_t sort_workspace_bytes, int* h_out_counts, float* h_out_times,
+                        int* h_overflow, cudaStream_t stream);
 
 #ifdef __cplusplus
 }
