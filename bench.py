@@ -279,12 +279,19 @@ def run_ours(args, dist, rank, world):
             e2e_s = time.perf_counter() - t0
             e2e = {"value": world * B * args.steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": ts.h2d_bytes,
                    "d2h_bytes_per_step": ts.d2h_bytes}
+        traffic, traffic_src = None, None
+        tpath = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tpath):
+            tinfo = json.load(open(tpath)).get(variant, {})
+            if tinfo.get("kernel") == top:
+                traffic, traffic_src = tinfo.get("bytes"), tinfo.get("source")
         result[variant] = {
             "value": sps, "ms_per_step": ms / args.steps, "graph": graphed, "autotuned": tuned, "clocks": clocks,
             "e2e": e2e,
             "spikes_per_layer_last_step": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
             "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+                         "traffic_source": traffic_src,
                          "algorithmic_bytes_per_launch": abytes, "launch_ms": top_ms,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
             "gpu_launches": ts.launches_per_step * args.steps,
@@ -299,8 +306,9 @@ def run_ours(args, dist, rank, world):
 
 
 def profile_one_step(workload):
-    """One eager train step with an NVTX range per launch (L1.sort, L1.forward, ...), after set-up, autotuning
-    and 3 warm-up steps, for targeted ncu captures: ncu --nvtx --nvtx-include "L2.forward/" ..."""
+    """One eager train step inside an NVTX range "step", with a nested range per launch (L1.sort, L1.forward,
+    ...), after set-up, autotuning and 3 warm-up steps, for targeted ncu captures:
+    ncu --nvtx --nvtx-include "step/" (the step's launch list) or --nvtx-include "step/L2.forward/"."""
     import torch
     if workload == "batching":
         from bats_gb300.train import FCLayerSpec, FCTrainStep
@@ -322,10 +330,12 @@ def profile_one_step(workload):
     torch.cuda.synchronize()
     from bats_gb300._lib import stream_ptr
     s = stream_ptr()
+    torch.cuda.nvtx.range_push("step")
     for name, fn in ts.launches:
         torch.cuda.nvtx.range_push(name)
         fn(s)
         torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     print(json.dumps({"profiled_step": workload, "launches": [n for n, _ in ts.launches]}))
 
