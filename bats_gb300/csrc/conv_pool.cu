@@ -21,6 +21,7 @@
 // Pooling (replaces aggregate_spikes_conv + argsort, .../Inference/aggregate_spikes_conv.cu:6-43,
 // Wrappers/Inference/aggregate_spikes_conv.py:10-28; backward bats/Layers/PoolingLayer.py:55-66):
 // a stable 4-way merge of the children's sorted spike lists, inf slots last in concatenation order.
+#include <cooperative_groups.h>
 #include "common.cuh"
 #include "abi_util.h"
 
@@ -185,6 +186,121 @@ __global__ void conv_backward_kernel(const Event* __restrict__ ev, const int* __
     }
 }
 
+// Conv backward on a cluster of CONV_BWD_CLUSTER CTAs per sample (thread-block cluster, distributed
+// shared memory). Thread = filter tap (co, dx, dy); the sample's events are dealt to the cluster's CTAs in
+// groups of 32 (group g to CTA rank g % CONV_BWD_CLUSTER), so that eight times as many CTAs hide the
+// latency of the post-spike lookups. Every CTA accumulates its events' gradient terms in a shared-memory
+// copy of the per-sample filter gradient (taps x C), in event order; at the end each CTA sums one slice of
+// the gradient over the cluster's copies in rank order (deterministic) and writes it. The pre-spike errors
+// of a group of events are reduced over the taps inside the CTA that owns the group. Four events are
+// processed at a time so that their lookups (binary searches over the post neuron's spike times, table
+// entries) are in flight together.
+constexpr int CONV_BWD_CLUSTER = 8;
+constexpr int CONV_BWD_ILP = 4;
+
+__global__ void __launch_bounds__(1024)
+conv_backward_cluster_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_slot,
+                             const int* __restrict__ ev_count, long long ev_cap, const float* __restrict__ W, int Y,
+                             int C, int fx, int fy, int C_out, int Xo, int Yo, const float* __restrict__ post_t,
+                             const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
+                             int search_top, float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
+                             float* __restrict__ pre_err) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) float Gs[];  // taps * C
+    __shared__ Event sev[32];
+    __shared__ float sred[32][33];
+    const unsigned rank = cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int s = blockIdx.y;
+    const int taps = C_out * fx * fy;
+    const int total = taps * C;
+    const int n_post = Xo * Yo * C_out;
+    for (int q = tid; q < total; q += blockDim.x) Gs[q] = 0.0f;
+    const int E = ev_count[s];
+    const Event* evs = ev + (long long)s * ev_cap;
+    __syncthreads();
+    for (int g = (int)rank; g * 32 < E; g += CONV_BWD_CLUSTER) {
+        const int m0 = g * 32;
+        const int cnt = min(32, E - m0);
+        if (tid < cnt) sev[tid] = evs[m0 + tid];
+        __syncthreads();
+        for (int q0 = 0; q0 < cnt; q0 += CONV_BWD_ILP) {
+            float term[CONV_BWD_ILP];
+#pragma unroll
+            for (int u = 0; u < CONV_BWD_ILP; ++u) term[u] = 0.0f;
+            for (int tp = tid; tp < taps; tp += blockDim.x) {
+                const int co = tp / (fx * fy), dx = (tp / fy) % fx, dy = tp % fy;
+                long long pn[CONV_BWD_ILP];
+                int nv[CONV_BWD_ILP], pos[CONV_BWD_ILP], cc[CONV_BWD_ILP];
+                float et[CONV_BWD_ILP];
+#pragma unroll
+                for (int u = 0; u < CONV_BWD_ILP; ++u) {
+                    nv[u] = 0;
+                    pos[u] = 0;
+                    pn[u] = 0;
+                    cc[u] = 0;
+                    et[u] = 0.0f;
+                    if (q0 + u < cnt) {
+                        const Event e = sev[q0 + u];
+                        cc[u] = e.j % C;
+                        const int xy = e.j / C, yy = xy % Y, xx = xy / Y;
+                        const int xo = xx - dx, yo = yy - dy;
+                        et[u] = e.t;
+                        if (xo >= 0 && yo >= 0 && xo < Xo && yo < Yo) {
+                            pn[u] = (long long)s * n_post + (xo * Yo + yo) * C_out + co;
+                            nv[u] = nvalid[pn[u]];
+                        }
+                    }
+                }
+                // Fixed-depth binary searches, the ILP searches interleaved: pos = #{k < n : t_k <= t}.
+                for (int step = search_top; step > 0; step >>= 1) {
+#pragma unroll
+                    for (int u = 0; u < CONV_BWD_ILP; ++u) {
+                        const int cand = pos[u] + step;
+                        if (cand <= nv[u] && post_t[pn[u] * k_post + cand - 1] <= et[u]) pos[u] = cand;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < CONV_BWD_ILP; ++u) {
+                    if (pos[u] < nv[u]) {
+                        const Event e = sev[q0 + u];
+                        const float2 AB = tab[pn[u] * (k_post + 1) + pos[u]];
+                        Gs[tp * C + cc[u]] += fmaf(e.es, AB.x, -(e.e * AB.y));
+                        if (pre_err) term[u] += W[(long long)tp * C + cc[u]] * (AB.x * e.es / tau_s - AB.y * e.e / tau);
+                    }
+                }
+            }
+            if (pre_err) {
+#pragma unroll
+                for (int u = 0; u < CONV_BWD_ILP; ++u) {
+                    float v = term[u];
+#pragma unroll
+                    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0 && q0 + u < cnt) sred[q0 + u][warp] = v;
+                }
+            }
+        }
+        __syncthreads();
+        if (pre_err && tid < cnt) {
+            float acc = 0.0f;
+            for (int w = 0; w < nwarps; ++w) acc += sred[tid][w];
+            pre_err[(long long)s * pre_slots + ev_slot[(long long)s * ev_cap + m0 + tid]] = acc;
+        }
+        __syncthreads();
+    }
+    cluster.sync();
+    const int per = (total + CONV_BWD_CLUSTER - 1) / CONV_BWD_CLUSTER;
+    const int q_end = min(total, ((int)rank + 1) * per);
+    for (int q = (int)rank * per + tid; q < q_end; q += blockDim.x) {
+        float acc = 0.0f;
+        for (int r = 0; r < CONV_BWD_CLUSTER; ++r) acc += cluster.map_shared_rank(Gs, r)[q];
+        grad[(long long)s * total + q] = acc;
+    }
+    cluster.sync();  // no CTA leaves while another still reads its shared memory
+}
+
 // Pool forward: one thread per (sample, pooled neuron).
 __global__ void pool_forward_kernel(const int* __restrict__ n_spikes, const float* __restrict__ times, int batch, int X,
                                     int Y, int C, int K, int* __restrict__ out_n, float* __restrict__ out_t,
@@ -306,6 +422,31 @@ extern "C" int bats_conv_backward(const void* events, const int* ev_slot, const 
     BATS_CUDA(cudaMemsetAsync(grad_per_sample, 0, (size_t)batch * taps * C * sizeof(float), stream));
     if (pre_errors) BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)batch * pre_slots * sizeof(float), stream));
     int threads = (int)std::min<long long>(1024, ((taps + 31) / 32) * 32);
+    const size_t gbytes = (size_t)taps * C * sizeof(float);
+    if (gbytes <= 160 * 1024) {
+        // Cluster path: the per-sample filter gradient lives in shared memory of every CTA of the cluster.
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_cluster_kernel, (int)gbytes));
+        int top = 1;
+        while (top * 2 <= k_post) top *= 2;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(bats::CONV_BWD_CLUSTER, batch);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = gbytes;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = bats::CONV_BWD_CLUSTER;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_cluster_kernel,
+                                     reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights,
+                                     Y, C, fx, fy, C_out, Xo, Yo, post_times,
+                                     reinterpret_cast<const float2*>(tables), nvalid, k_post, top, tau_s, tau,
+                                     pre_slots, grad_per_sample, pre_errors));
+        return BATS_OK;
+    }
     bats::conv_backward_kernel<<<batch, threads, 0, stream>>>(
         reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights, Y, C, fx, fy, C_out, Xo, Yo,
         post_times, reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots, grad_per_sample,

@@ -465,38 +465,47 @@ def batching_bench(steps: int = 5, warmup: int = 3):
     return out
 
 
+CONV_THETAS = (0.04, 0.8, 0.6, 0.3)
+
+
+def conv_weights(seed=3):
+    rng = np.random.default_rng(seed)
+    return [rng.uniform(-1, 1, (15, 5, 5, 1)).astype(np.float32), rng.uniform(-1, 1, (40, 5, 5, 15)).astype(np.float32),
+            rng.uniform(-1, 1, (300, 640)).astype(np.float32), rng.uniform(-1, 1, (10, 300)).astype(np.float32)]
+
+
 def conv_bench(steps: int = 5):
     """The convolutional network of the reference's MNIST conv experiment (experiments/mnist/train_conv.py:
     conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> FC 300 -> 10, thresholds 0.04 / 0.8 / 0.6 / 0.3 with
     delta_theta = theta, tau_s 0.13, weights U(-1, 1)), max_n_spike 10 in every layer, batch 128, on
     synthetic MNIST-shaped single-spike input; full train step (forward, spike-count loss, exact backward,
-    Adam) through the drop-in layer API."""
+    Adam) through the drop-in layer API, and the same step on the reference's own CUDA kernels."""
     import torch
     from bats_gb300 import Network, SpikeCountClassLoss
     from bats_gb300.Layers import ConvInputLayer, ConvLIFLayer, LIFLayer, PoolingLayer
     from bats_gb300.Optimizers import AdamOptimizer
     Bc, Kc = 128, 10
-    rng = np.random.default_rng(3)
+    w1, w2, w3, w4 = conv_weights()
     net = Network()
     inp = ConvInputLayer(neurons_shape=np.array([28, 28, 1]), name="in")
     net.add_layer(inp, input=True)
-    conv_init = lambda c, x, y, pc: torch.tensor(rng.uniform(-1, 1, (c, x, y, pc)).astype(np.float32), device="cuda")
-    ff_init = lambda n, m: torch.tensor(rng.uniform(-1, 1, (n, m)).astype(np.float32), device="cuda")
-    c1 = ConvLIFLayer(inp, filters_shape=np.array([5, 5, 15]), tau_s=TAU_S, theta=0.04, delta_theta=0.04,
-                      weight_initializer=conv_init, max_n_spike=Kc, name="conv1")
+    c1 = ConvLIFLayer(inp, filters_shape=np.array([5, 5, 15]), tau_s=TAU_S, theta=CONV_THETAS[0],
+                      delta_theta=CONV_THETAS[0], weight_initializer=lambda *a: torch.tensor(w1, device="cuda"),
+                      max_n_spike=Kc, name="conv1")
     net.add_layer(c1)
     p1 = PoolingLayer(c1, name="pool1")
     net.add_layer(p1)
-    c2 = ConvLIFLayer(p1, filters_shape=np.array([5, 5, 40]), tau_s=TAU_S, theta=0.8, delta_theta=0.8,
-                      weight_initializer=conv_init, max_n_spike=Kc, name="conv2")
+    c2 = ConvLIFLayer(p1, filters_shape=np.array([5, 5, 40]), tau_s=TAU_S, theta=CONV_THETAS[1],
+                      delta_theta=CONV_THETAS[1], weight_initializer=lambda *a: torch.tensor(w2, device="cuda"),
+                      max_n_spike=Kc, name="conv2")
     net.add_layer(c2)
     p2 = PoolingLayer(c2, name="pool2")
     net.add_layer(p2)
-    f1 = LIFLayer(p2, n_neurons=300, tau_s=TAU_S, theta=0.6, delta_theta=0.6, weight_initializer=ff_init,
-                  max_n_spike=Kc, name="fc")
+    f1 = LIFLayer(p2, n_neurons=300, tau_s=TAU_S, theta=CONV_THETAS[2], delta_theta=CONV_THETAS[2],
+                  weight_initializer=lambda *a: torch.tensor(w3, device="cuda"), max_n_spike=Kc, name="fc")
     net.add_layer(f1)
-    out = LIFLayer(f1, n_neurons=10, tau_s=TAU_S, theta=0.3, delta_theta=0.3, weight_initializer=ff_init,
-                   max_n_spike=Kc, name="out")
+    out = LIFLayer(f1, n_neurons=10, tau_s=TAU_S, theta=CONV_THETAS[3], delta_theta=CONV_THETAS[3],
+                   weight_initializer=lambda *a: torch.tensor(w4, device="cuda"), max_n_spike=Kc, name="out")
     net.add_layer(out)
     loss_fn = SpikeCountClassLoss(TARGET_TRUE, TARGET_FALSE)
     opt = AdamOptimizer(learning_rate=LR)
@@ -515,10 +524,62 @@ def conv_bench(steps: int = 5):
     flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ms, _ = time_steps(step, steps, 3, flush)
     spikes = [int(L.spike_trains[1].sum().item()) for L in layers]
-    return {"value": Bc * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps, "steps": steps,
-            "batch": Bc, "spikes_per_layer": spikes,
-            "network": "28x28x1 -> conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> 300 -> 10, K 10",
-            "what": "full train step through Network/ConvLIFLayer/PoolingLayer/LIFLayer/AdamOptimizer"}
+    res = {"value": Bc * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps, "steps": steps,
+           "batch": Bc, "spikes_per_layer": spikes,
+           "network": "28x28x1 -> conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> 300 -> 10, K 10",
+           "what": "full train step through Network/ConvLIFLayer/PoolingLayer/LIFLayer/AdamOptimizer"}
+    res["refkern"] = refkern_conv_rate(t, n, labels, flush)
+    return res
+
+
+def refkern_conv_rate(t, n, labels, flush, steps=1):
+    """The conv network's train step on the reference's own CUDA kernels (oracle/refkern.py), same weights
+    and inputs."""
+    import torch
+    from oracle import refkern
+    if not refkern.available():
+        return {"unavailable": "reference kernels not built (oracle/_ref)"}
+    Kc = 10
+    ws = [torch.tensor(w, device="cuda") for w in conv_weights()]
+    L1 = refkern.RefConvLIF(ws[0], (28, 28, 1), TAU_S, CONV_THETAS[0], CONV_THETAS[0], Kc)
+    L2 = refkern.RefConvLIF(ws[1], (12, 12, 15), TAU_S, CONV_THETAS[1], CONV_THETAS[1], Kc)
+    L3 = refkern.RefLIF(ws[2], TAU_S, CONV_THETAS[2], CONV_THETAS[2], Kc)
+    L4 = refkern.RefLIF(ws[3], TAU_S, CONV_THETAS[3], CONV_THETAS[3], Kc)
+    td, nd = torch.tensor(t, device="cuda"), torch.tensor(n, device="cuda")
+    Bc = td.shape[0]
+    tt = torch.full((Bc, 10), TARGET_FALSE, device="cuda")
+    tt[torch.arange(Bc), torch.tensor(labels, device="cuda").long()] = TARGET_TRUE
+    params = [L1.w, L2.w, L3.w, L4.w]
+    m = [torch.zeros_like(w) for w in params]
+    v = [torch.zeros_like(w) for w in params]
+    state = {"t": 0}
+
+    def step():
+        o1 = L1.forward(td, nd, np.float32(MAX_SIM))
+        pn1, pt1, pi1 = refkern.pool_forward(o1[0], o1[3], (24, 24, 15))
+        o2 = L2.forward(pt1, pn1, np.float32(MAX_SIM))
+        pn2, pt2, pi2 = refkern.pool_forward(o2[0], o2[3], (8, 8, 40))
+        o3 = L3.forward(pt2, pn2, np.float32(MAX_SIM))
+        o4 = L4.forward(o3[3], o3[0], np.float32(MAX_SIM))
+        err = (tt - o4[0].float())[:, :, None].repeat(1, 1, Kc).contiguous()
+        g4, e3 = L4.backward(err, want_pre=True)
+        g3, ep2 = L3.backward(e3, want_pre=True)
+        e2 = refkern.pool_backward(ep2, pi2, o2[3].shape)
+        g2, ep1 = L2.backward(e2.contiguous(), want_pre=True)
+        e1 = refkern.pool_backward(ep1, pi1, o1[3].shape)
+        g1, _ = L1.backward(e1.contiguous(), want_pre=False)
+        state["t"] += 1
+        for i, g in enumerate((g1, g2, g3, g4)):
+            g = g.mean(0)
+            m[i].mul_(0.9).add_(0.1 * g)
+            v[i].mul_(0.999).add_(0.001 * g * g)
+            mh = m[i] / (1 - 0.9 ** state["t"])
+            vh = v[i] / (1 - 0.999 ** state["t"])
+            params[i].add_(-(LR * mh / (vh.sqrt() + 1e-8)))
+
+    ms, _ = time_steps(step, steps, 1, flush)
+    return {"value": Bc * steps / (ms / 1e3), "unit": "samples/s", "steps": steps,
+            "what": "reference CUDA kernels (unmodified, oracle/_ref) with the reference wrappers' launch shapes"}
 
 
 def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float = 0.8):
