@@ -366,7 +366,7 @@ __global__ void reduce_groups_kernel(const float* __restrict__ partial, long lon
 // over the tile's warps, into partial[(s, m, tile, 0..1)]; pre_err_scatter_kernel sums the tiles in
 // order, applies the event's factors and writes the result to the event's (neuron, slot).
 template <int TILE, int STAGES>
-__global__ void __launch_bounds__(TILE + 32)
+__global__ void __launch_bounds__(TILE + 32, 3)
 bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                    const float* __restrict__ wt, int ld, const float* __restrict__ post_t,
                    const float2* __restrict__ tab, const int* __restrict__ nvalid, int n_post, int k_post,
@@ -484,23 +484,24 @@ bwd_pre_err_narrow_kernel(const Event* __restrict__ ev, const int* __restrict__ 
     stage_post(post_t, tab, nvalid, s, n_post, k_post, st, stab, snv);
     cp_async_wait_all();
     __syncthreads();
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= E) return;
-    const long long em = (long long)s * ev_cap + m;
-    const Event e = ev[em];
-    const float* wrow = wt + (long long)e.j * ld;
-    float sa = 0.0f, sb = 0.0f;
-    for (int i = 0; i < n_post; ++i) {
-        const int n = snv[i];
-        const int p = post_position(st + i * k_post, n, e.t);
-        if (p < n) {
-            const float w = __ldg(wrow + i);
-            const float2 AB = stab[i * (k_post + 1) + p];
-            sa += w * AB.x;
-            sb += w * AB.y;
+    // The sample's events, strided over the CTAs of its row of the grid.
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < E; m += gridDim.x * blockDim.x) {
+        const long long em = (long long)s * ev_cap + m;
+        const Event e = ev[em];
+        const float* wrow = wt + (long long)e.j * ld;
+        float sa = 0.0f, sb = 0.0f;
+        for (int i = 0; i < n_post; ++i) {
+            const int n = snv[i];
+            const int p = post_position(st + i * k_post, n, e.t);
+            if (p < n) {
+                const float w = __ldg(wrow + i);
+                const float2 AB = stab[i * (k_post + 1) + p];
+                sa += w * AB.x;
+                sb += w * AB.y;
+            }
         }
+        pre_err[(long long)s * slots_per_sample + ev_slot[em]] = sa * e.es / tau_s - sb * e.e / tau;
     }
-    pre_err[(long long)s * slots_per_sample + ev_slot[em]] = sa * e.es / tau_s - sb * e.e / tau;
 }
 
 // Sums the per-tile partials of each event in tile order and writes
@@ -678,7 +679,8 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
                             (size_t)n_post * sizeof(int);
         BATS_REQUIRE(smem <= 160 * 1024, BATS_ERR_BAD_SHAPE, "pre_errors: k_post too large for a narrow layer");
         BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_narrow_kernel, (int)smem));
-        dim3 grid((unsigned)((ev_cap + 127) / 128), batch);
+        // At most 8 CTAs per sample (each stages the sample's post data once); empty samples exit at once.
+        dim3 grid((unsigned)std::min<long long>((ev_cap + 127) / 128, 8), batch);
         bats::bwd_pre_err_narrow_kernel<<<grid, 128, smem, stream>>>(
             reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights_t, ld, post_times,
             reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, slots, tau_s, tau, pre_errors);

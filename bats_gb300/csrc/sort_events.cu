@@ -147,14 +147,40 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     const long long sample_off = (long long)s * n_slots;
     const float* tsrc = times + sample_off;
 
-    // Count valid slots first so that the buffers can be chosen.
+    // Count valid slots first so that the buffers can be chosen (16-byte loads when the rows allow).
     int n = 0;
-    for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
-        const int slot = r0 + tid;
-        const bool f = slot < n_slots && tsrc[slot] < BATS_INF;
-        int tot;
-        block_exclusive_flag_scan(f, sh, tot);
-        n += tot;
+    if ((n_slots & 3) == 0) {
+        const float4* t4 = reinterpret_cast<const float4*>(tsrc);
+        const int n4 = n_slots >> 2;
+        for (int r0 = 0; r0 < n4; r0 += SORT_THREADS) {
+            const int q = r0 + tid;
+            int c = 0;
+            if (q < n4) {
+                const float4 v = t4[q];
+                c = (v.x < BATS_INF) + (v.y < BATS_INF) + (v.z < BATS_INF) + (v.w < BATS_INF);
+            }
+            for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+            n += c;
+        }
+        // n holds this warp's total; sum over warps.
+        if ((tid & 31) == 0) sh.warp_tot[tid >> 5] = n;
+        __syncthreads();
+        n = 0;
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; ++w) n += sh.warp_tot[w];
+        __syncthreads();
+    } else {
+        for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
+            const int slot = r0 + tid;
+            n += __syncthreads_count(slot < n_slots && tsrc[slot] < BATS_INF);
+        }
+    }
+    if (n == 0) {
+        // No spike in this sample: empty event list (and empty buckets).
+        if (tid == 0) ev_count[s] = 0;
+        if (ev_bucketed)
+            for (int q = tid; q <= n_buckets; q += SORT_THREADS) bucket_off[(long long)s * (n_buckets + 1) + q] = 0;
+        return;
     }
 
     uint32_t *ka, *va, *kb, *vb;
