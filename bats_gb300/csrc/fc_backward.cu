@@ -329,7 +329,37 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
             for (int q = tid; q < cnt; q += TILE) sev[q] = evs[m0 + q];
             __syncthreads();
             if (n == 0) continue;
-            for (int m = 0; m < cnt; ++m) {
+            // Four events at a time: their terms are formed in event order (the cursor only moves
+            // forward), then the four shared-memory updates are issued with all loads first when the
+            // four pre neurons differ (the usual case), so that they do not wait on one another. Every
+            // G[j][i] still receives its terms in event order.
+            int m = 0;
+            for (; m + 4 <= cnt; m += 4) {
+                float v[4];
+                int jj[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const Event e = sev[m + u];
+                    cur.advance_past(e.t);
+                    jj[u] = e.j - J0;
+                    v[u] = cur.valid() ? fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y)) : 0.0f;
+                }
+                const bool distinct = jj[0] != jj[1] && jj[0] != jj[2] && jj[0] != jj[3] && jj[1] != jj[2] &&
+                                      jj[1] != jj[3] && jj[2] != jj[3];
+                if (distinct) {
+                    float g[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) g[u] = G[jj[u]][tid];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (v[u] != 0.0f) G[jj[u]][tid] = g[u] + v[u];
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (v[u] != 0.0f) G[jj[u]][tid] += v[u];
+                }
+            }
+            for (; m < cnt; ++m) {
                 const Event e = sev[m];
                 cur.advance_past(e.t);
                 if (cur.valid()) G[e.j - J0][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
