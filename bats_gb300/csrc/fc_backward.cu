@@ -161,9 +161,10 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
         nvalid[nb + lane] = n;
     }
     const int K1 = K + 1;
+    __shared__ int sN[PREP_WARPS][32];
+    sN[warp][lane] = n;
     if (!__any_sync(0xffffffffu, n > 0)) {
-        // Silent neurons: empty tables, zero factors, errors unchanged.
-        if (lane < cnt) tab[(nb + lane) * K1] = make_float2(0.0f, 0.0f);
+        // Silent neurons: nothing to read or write but zero factors (no table entry is ever read past n).
         if (f1)
             for (int q = lane; q < nk; q += 32) {
                 f1[base + q] = 0.0f;
@@ -171,8 +172,12 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
             }
         return;
     }
+    __syncwarp();
+    // Only the leading valid slots of each neuron are read (and written back below).
     for (int q = lane; q < nk; q += 32) {
-        const int o = (q / K) * PREP_KS + q % K;
+        const int r = q / K, k = q % K;
+        if (k >= sN[warp][r]) continue;
+        const int o = r * PREP_KS + k;
         cp_async4(sZ + o, z + base + q);
         cp_async4(sX + o, x + base + q);
         cp_async4(sA + o, a + base + q);
@@ -215,24 +220,22 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
             rt[p] = sa;
             rx[p] = sb;
         }
-        for (int p = n; p <= K && p < PREP_KS; ++p) {
-            rt[p] = 0.0f;
-            rx[p] = 0.0f;
-        }
     }
     __syncwarp();
     for (int q = lane; q < nk; q += 32) {
-        const int o = (q / K) * PREP_KS + q % K;
-        err[base + q] = sE[o];
+        const int r = q / K, k = q % K;
+        const int o = r * PREP_KS + k;
+        if (k < sN[warp][r]) err[base + q] = sE[o];
         if (f1) {
             f1[base + q] = sA[o];
             f2[base + q] = sZ[o];
         }
     }
+    // Table entries p < n only: the consumers never read an entry at or past a neuron's count.
     const int nt = cnt * K1;
     for (int q = lane; q < nt; q += 32) {
-        const int o = (q / K1) * PREP_KS + q % K1;
-        tab[nb * K1 + q] = make_float2(sT[o], sX[o]);
+        const int r = q / K1, p = q % K1;
+        if (p < sN[warp][r]) tab[nb * K1 + q] = make_float2(sT[r * PREP_KS + p], sX[r * PREP_KS + p]);
     }
 }
 
@@ -504,7 +507,7 @@ bwd_pre_err_narrow_kernel(const Event* __restrict__ ev, const int* __restrict__ 
                           const float* __restrict__ post_t, const float2* __restrict__ tab,
                           const int* __restrict__ nvalid, int n_post, int k_post, long long slots_per_sample,
                           float tau_s, float tau, float* __restrict__ pre_err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* stab = reinterpret_cast<float2*>(smem_raw);
     float* st = reinterpret_cast<float*>(stab + n_post * (k_post + 1));
     int* snv = reinterpret_cast<int*>(st + n_post * k_post);
