@@ -209,16 +209,27 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
             ra[k] = v1;
             rz[k] = v2;
         }
-        // Suffix tables in the reference's accumulation order; (SA_p, SB_p) into (t, x) rows.
-        for (int p = 0; p < n; ++p) {
-            float sa = 0.0f, sb = 0.0f;
-            for (int k = p; k < n; ++k) {
-                const float ek = re[k];
-                sa += ek * ra[k];
-                sb += ek * rz[k];
+        // Suffix tables in the reference's accumulation order (each SA_p, SB_p summed upwards from k = p);
+        // four p at a time so that their eight accumulation chains overlap. (SA_p, SB_p) into (t, x) rows.
+        for (int p0 = 0; p0 < n; p0 += 4) {
+            float sa[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sb[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            for (int k = p0; k < n; ++k) {
+                const float ek = re[k], fa = ra[k], fb = rz[k];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (k >= p0 + u) {
+                        sa[u] += ek * fa;
+                        sb[u] += ek * fb;
+                    }
+                }
             }
-            rt[p] = sa;
-            rx[p] = sb;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (p0 + u < n) {
+                    rt[p0 + u] = sa[u];
+                    rx[p0 + u] = sb[u];
+                }
+            }
         }
     }
     __syncwarp();

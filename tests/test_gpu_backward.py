@@ -220,3 +220,34 @@ def test_narrow_layer_kernels(cuda, n_post):
     scale = R.propagate_errors_to_pre_spikes(np.abs(f1), np.abs(f2), post, pre, np.abs(W), np.abs(e),
                                              float(np.float32(tau_s)), -float(tau32))
     assert_sum_close(pe.cpu().numpy(), ref, scale, what="narrow pre errors vs oracle")
+
+
+def test_layer_prep_matches_generic_prep_bit_for_bit(cuda):
+    """bats_backward_prep_layer (warp-staged, valid slots only, interleaved suffix sums) against the
+    one-thread-per-neuron bats_backward_prep on the same forward state: reset errors, factors, counts and
+    every table entry before a neuron's count are identical."""
+    t, n_in = multi_spike_input(16, 60, 5, 0.1, seed=11, p_silent=0.1)
+    rng = np.random.default_rng(11)
+    W = (rng.uniform(-0.3, 1.0, (70, 60)) * 1.5).astype(np.float32)
+    tau_s, th = 0.1, 0.2
+    ev = K.sort_events(cu(t), tau_s, 2 * tau_s)
+    n, a, x, ts, z = K.lif_forward_fc(ev, K.transpose_weights(cu(W)), 70, 30, tau_s, th, th)
+    assert int(n.max()) >= 8, "some neurons should spike many times"
+    err = cu(rng.normal(size=ts.shape).astype(np.float32))
+    tau32, c, dtt = K.lif_constants(tau_s, th, th)
+    e1, e2 = err.clone(), err.clone()
+    tl = K.backward_prep(ts, a, x, z, e1, c, tau32, dtt, want_factors=True)
+    B, N, Kp = ts.shape
+    tg = K.BackwardTables(torch.empty_like(ts), torch.empty_like(ts), torch.empty((B, N, Kp + 1, 2), device="cuda"),
+                          torch.empty((B, N), dtype=torch.int32, device="cuda"))
+    from bats_gb300._lib import call, ptr, stream_ptr
+    call("bats_backward_prep", ptr(ts), ptr(a), ptr(x), ptr(z), ptr(e2), B, N, Kp, float(c), float(tau32), float(dtt),
+         1, 1, ptr(tg.f1), ptr(tg.f2), ptr(tg.tables), ptr(tg.nvalid), stream_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(tl.nvalid, tg.nvalid)
+    assert torch.equal(e1, e2)
+    assert torch.equal(tl.f1, tg.f1) and torch.equal(tl.f2, tg.f2)
+    nv = tl.nvalid.cpu().numpy()
+    valid = np.arange(Kp + 1)[None, None, :] < nv[:, :, None]
+    a_tab, b_tab = tl.tables.cpu().numpy(), tg.tables.cpu().numpy()
+    assert np.array_equal(a_tab[valid].view(np.uint32), b_tab[valid].view(np.uint32))
