@@ -158,15 +158,25 @@ lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict_
     float a = 0.0f, b = 0.0f;
     int n = 0;
     bool done = false;
+    // The next block's event and weight are loaded one block ahead, so that the gather latency overlaps
+    // the current block's chain and tests.
+    float4 e4_nx = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float w_nx = 0.0f;
+    if (lane < E) {
+        e4_nx = __ldg(reinterpret_cast<const float4*>(evs + lane));
+        w_nx = __ldg(wt + (long long)__float_as_int(e4_nx.y) * ld + i);
+    }
     for (int m0 = 0; m0 < E && !done; m0 += 32) {
         const int m = m0 + lane;
         const int cnt = min(32, E - m0);
         const bool in = lane < cnt;
-        float4 e4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // (t, j, es, e)
-        float w = 0.0f;
-        if (in) {
-            e4 = __ldg(reinterpret_cast<const float4*>(evs + m));
-            w = __ldg(wt + (long long)__float_as_int(e4.y) * ld + i);
+        const float4 e4 = e4_nx;  // (t, j, es, e); zeros past the end
+        const float w = w_nx;
+        e4_nx = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w_nx = 0.0f;
+        if (m + 32 < E) {
+            e4_nx = __ldg(reinterpret_cast<const float4*>(evs + m + 32));
+            w_nx = __ldg(wt + (long long)__float_as_int(e4_nx.y) * ld + i);
         }
         // Window end: the next event's time and exponential (+inf after the last event).
         float t_nx = __shfl_down_sync(0xffffffffu, e4.x, 1);

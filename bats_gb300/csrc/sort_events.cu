@@ -147,28 +147,26 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     const long long sample_off = (long long)s * n_slots;
     const float* tsrc = times + sample_off;
 
-    // Count valid slots first so that the buffers can be chosen (16-byte loads when the rows allow).
+    // Count valid slots first so that the buffers can be chosen. With 16-byte rows (n_slots % 4 == 0) each
+    // warp counts, and later compacts, its own contiguous range of slots, so neither pass needs a
+    // block-wide barrier per round.
     int n = 0;
-    if ((n_slots & 3) == 0) {
-        const float4* t4 = reinterpret_cast<const float4*>(tsrc);
-        const int n4 = n_slots >> 2;
-        for (int r0 = 0; r0 < n4; r0 += SORT_THREADS) {
-            const int q = r0 + tid;
-            int c = 0;
-            if (q < n4) {
-                const float4 v = t4[q];
-                c = (v.x < BATS_INF) + (v.y < BATS_INF) + (v.z < BATS_INF) + (v.w < BATS_INF);
-            }
-            for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-            n += c;
+    const bool vec = (n_slots & 3) == 0;
+    const int n4 = n_slots >> 2;
+    const int per_warp4 = (n4 + SORT_WARPS - 1) / SORT_WARPS;
+    const int w_lo = min(n4, (tid >> 5) * per_warp4), w_hi = min(n4, w_lo + per_warp4);
+    const float4* t4 = reinterpret_cast<const float4*>(tsrc);
+    if (vec) {
+        int c = 0;
+        for (int q = w_lo + (tid & 31); q < w_hi; q += 32) {
+            const float4 v = t4[q];
+            c += (v.x < BATS_INF) + (v.y < BATS_INF) + (v.z < BATS_INF) + (v.w < BATS_INF);
         }
-        // n holds this warp's total; sum over warps.
-        if ((tid & 31) == 0) sh.warp_tot[tid >> 5] = n;
+        for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if ((tid & 31) == 0) sh.warp_tot[tid >> 5] = c;
         __syncthreads();
-        n = 0;
 #pragma unroll
         for (int w = 0; w < SORT_WARPS; ++w) n += sh.warp_tot[w];
-        __syncthreads();
     } else {
         for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
             const int slot = r0 + tid;
@@ -197,19 +195,48 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     }
 
     // Compaction in slot order (stable).
-    int base = 0;
-    for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
-        const int slot = r0 + tid;
-        float t = BATS_INF;
-        if (slot < n_slots) t = tsrc[slot];
-        const bool f = t < BATS_INF;
-        int tot;
-        const int pos = block_exclusive_flag_scan(f, sh, tot);
-        if (f) {
-            ka[base + pos] = float_to_key(t);
-            va[base + pos] = (uint32_t)slot;
+    if (vec) {
+        int base = 0;
+        for (int w = 0; w < (tid >> 5); ++w) base += sh.warp_tot[w];
+        const int lane = tid & 31;
+        for (int q0 = w_lo; q0 < w_hi; q0 += 32) {
+            const int q = q0 + lane;
+            float4 v = make_float4(BATS_INF, BATS_INF, BATS_INF, BATS_INF);
+            if (q < w_hi) v = t4[q];
+            const int c = (v.x < BATS_INF) + (v.y < BATS_INF) + (v.z < BATS_INF) + (v.w < BATS_INF);
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            int pos = base + incl - c;
+            const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (vv[u] < BATS_INF) {
+                    ka[pos] = float_to_key(vv[u]);
+                    va[pos] = (uint32_t)(4 * q + u);
+                    ++pos;
+                }
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
         }
-        base += tot;
+    } else {
+        int base = 0;
+        for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
+            const int slot = r0 + tid;
+            float t = BATS_INF;
+            if (slot < n_slots) t = tsrc[slot];
+            const bool f = t < BATS_INF;
+            int tot;
+            const int pos = block_exclusive_flag_scan(f, sh, tot);
+            if (f) {
+                ka[base + pos] = float_to_key(t);
+                va[base + pos] = (uint32_t)slot;
+            }
+            base += tot;
+        }
     }
     __syncthreads();
 
