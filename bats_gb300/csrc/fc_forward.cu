@@ -290,7 +290,7 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
                            int algo, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0 && ld >= n_post && ld % 4 == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc: bad shape (ld must be >= n_post and a multiple of 4)");
-    BATS_REQUIRE(algo >= BATS_FWD_AUTO && algo <= BATS_FWD_LANES, BATS_ERR_BAD_SHAPE, "lif_forward_fc: unknown algo");
+    BATS_REQUIRE(algo >= BATS_FWD_AUTO && algo <= BATS_FWD_TILE64, BATS_ERR_BAD_SHAPE, "lif_forward_fc: unknown algo");
     if (batch == 0 || n_post == 0) return BATS_OK;
     BATS_REQUIRE(events && ev_count && weights_t && n_spikes && a && x && times && post_exp_tau, BATS_ERR_NULL,
                  "lif_forward_fc: null pointer");
@@ -303,6 +303,9 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
                                              n_spikes, a, x, times, post_exp_tau, stream);
     int* status = nullptr;
     BATS_CUDA((cudaError_t)bats::device_status(&status));
+    if (algo == BATS_FWD_TILE64)
+        return bats::launch_forward<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+                                              n_spikes, a, x, times, post_exp_tau, status, stream);
     if (n_post <= 32)
         return bats::launch_forward<32, 16, 8>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                                n_spikes, a, x, times, post_exp_tau, status, stream);

@@ -145,7 +145,7 @@ def get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron):
     return (B, N * K), idx, reshaped
 
 
-FWD_AUTO, FWD_TILE, FWD_LANES = 0, 1, 2
+FWD_AUTO, FWD_TILE, FWD_LANES, FWD_TILE64 = 0, 1, 2, 3
 
 
 def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: float, theta: float,

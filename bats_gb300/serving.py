@@ -279,9 +279,11 @@ class InferenceServer:
                         trial[li] = algo
                         self._layers(lane, b, trial, s, only=li)
 
-                    best = tuner.pick("fc_forward", shape, {"tile": lambda: run(K.FWD_TILE),
-                                                             "lanes": lambda: run(K.FWD_LANES)})
-                    algos[li] = K.FWD_TILE if best == "tile" else K.FWD_LANES
+                    cands = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES}
+                    if spec.n_neurons > 64:
+                        cands["tile64"] = K.FWD_TILE64
+                    best = tuner.pick("fc_forward", shape, {k: (lambda a=a: run(a)) for k, a in cands.items()})
+                    algos[li] = cands[best]
                     names.append(best)
             torch.cuda.synchronize()
             self.algo_table[b] = algos

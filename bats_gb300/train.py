@@ -198,9 +198,12 @@ class FCTrainStep:
                 fwd[f"{tag}.forward"](s)
                 self.fwd_algo[li] = saved
 
-            best = tuner.pick("fc_forward", shape, {"tile": lambda: run_fwd(K.FWD_TILE),
-                                                     "lanes": lambda: run_fwd(K.FWD_LANES)}, force=force)
-            self.fwd_algo[li] = K.FWD_TILE if best == "tile" else K.FWD_LANES
+            algos = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES}
+            if spec.n_neurons > 64:
+                algos["tile64"] = K.FWD_TILE64
+            best = tuner.pick("fc_forward", shape, {k: (lambda a=a: run_fwd(a)) for k, a in algos.items()},
+                              force=force)
+            self.fwd_algo[li] = algos[best]
             cands = {}
             for parts in ((4, 8, 16, 32) if spec.n_neurons > 32 else (16, 32, 64, 128, 256)):
                 g = max(2, -(-B // parts))

@@ -92,6 +92,7 @@ int bats_intensity_to_spike_times(const unsigned char* pixels, int batch, int n_
 #define BATS_FWD_AUTO 0
 #define BATS_FWD_TILE 1
 #define BATS_FWD_LANES 2
+#define BATS_FWD_TILE64 3 /* the tile kernel with 64-neuron tiles whatever N_post (more CTAs, less reuse) */
 int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap);
 int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
                              int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,

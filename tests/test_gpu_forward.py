@@ -163,7 +163,7 @@ def _both_algos(t, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
     ev = K.sort_events(tt, np.float32(tau_s), np.float32(2 * tau_s))
     wt = K.transpose_weights(torch.tensor(W, device="cuda"))
     outs = []
-    for algo in (K.FWD_TILE, K.FWD_LANES):
+    for algo in (K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64):
         o = K.lif_forward_fc(ev, wt, W.shape[0], K_post, tau_s, theta, dtheta, max_sim, algo=algo)
         outs.append([v.cpu().numpy() for v in o])
     return outs
@@ -181,7 +181,8 @@ def _assert_identical(p, q, what):
 
 @pytest.mark.parametrize("case", ["small", "mnist_active", "long_narrow", "long_wide", "cap_and_cut"])
 def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
-    """The warp-per-neuron forward (32 events per step, FWD_LANES) is bit-identical to the tile kernel on
+    """The warp-per-neuron forward (32 events per step, FWD_LANES) and the 64-neuron-tile variant are
+    bit-identical to the tile kernel on
     short and long event streams, narrow and wide layers, a full spike buffer and a max_simulation cut; on
     a long stream it also matches the reference kernels."""
     rng = np.random.default_rng(5)
@@ -202,9 +203,10 @@ def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
         t, n_in = multi_spike_input(3, 50, 6, 0.2, seed=6, p_silent=0.0)
         W = np.abs(rng.normal(0, 1, (40, 50))).astype(np.float32)
         args = (0.1, 0.05, 0.05, 4, 0.12)
-    tile, lanes = _both_algos(t, W, *args)
+    tile, lanes, tile64 = _both_algos(t, W, *args)
     assert tile[0].sum() > 0, "the case should spike"
     _assert_identical(tile, lanes, case)
+    _assert_identical(tile, tile64, case + " (64-neuron tiles)")
     if case == "long_narrow":
         ref = run_ref(t, n_in, W, *args)
         check_against(lanes, ref, None, what="lanes vs reference kernels")
