@@ -88,7 +88,11 @@ class ConvLIFLayer(AbstractConvLayer):
 
     def forward(self, max_simulation: float, training: bool = False) -> None:
         pre_spike_per_neuron, _ = self.__previous_layer.spike_trains
-        self.__events = K.sort_events(pre_spike_per_neuron, self.__tau_s, self.__tau)
+        # Bucketed copy grouped by input position (bucket width = input channels) for the backward pass,
+        # when the input has at most 255 positions.
+        X, Y, C = (int(v) for v in self.__previous_layer.neurons_shape)
+        self.__events = K.sort_events(pre_spike_per_neuron, self.__tau_s, self.__tau, bucketed=X * Y <= 255,
+                                      bucket_width=C)
         (self.__n_spike_per_neuron, self.__a, self.__x, self.__spike_times_per_neuron,
          self.__post_exp_tau) = K.conv_forward(self.__events, self.__weights, self.__previous_layer.neurons_shape,
                                                self.__max_n_spike, self.__tau_s, self.__theta, self.__delta_theta,

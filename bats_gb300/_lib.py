@@ -49,6 +49,8 @@ SIGNATURES = {
     "bats_serve_fc_batch": (c_int, [c_vp, c_vp, c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_int, c_int, c_vp, c_vp, c_vp,
                                     c_vp, c_int, c_vp, c_size, c_vp, c_vp, c_vp, c_vp]),
     "bats_events_max_per_neuron": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_vp, c_vp]),
+    "bats_conv_backward_grouped": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
+                                           c_int, c_vp, c_vp, c_vp, c_int, c_float, c_float, c_vp, c_vp, c_vp]),
     "bats_pool_forward": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
     "bats_backward_prep": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                    c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -148,6 +148,39 @@ __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t,
     }
 }
 
+// Position of one post neuron's spike train relative to a time-ordered scan of pre spikes: p = first
+// post spike with t_p > the current pre-spike time, with its suffix-table entry AB = (SA_p, SB_p)
+// ((0, 0) once p reaches the neuron's n valid spikes). The entry after the current one is loaded ahead,
+// so an advance does not wait on a global load.
+struct PostCursor {
+    const float* tp;
+    const float2* tb;
+    int n, p;
+    float tn, tn1;
+    float2 AB, AB1;
+    __device__ __forceinline__ void init(const float* tp_, const float2* tb_, int n_) {
+        tp = tp_;
+        tb = tb_;
+        n = n_;
+        p = 0;
+        tn = n > 0 ? tp[0] : BATS_INF;
+        AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
+        tn1 = n > 1 ? tp[1] : BATS_INF;
+        AB1 = n > 1 ? tb[1] : make_float2(0.0f, 0.0f);
+    }
+    __device__ __forceinline__ void advance_past(float t) {
+        while (tn <= t) {
+            ++p;
+            tn = tn1;
+            AB = AB1;
+            const bool more = p + 1 < n;
+            tn1 = more ? tp[p + 1] : BATS_INF;
+            AB1 = more ? tb[p + 1] : make_float2(0.0f, 0.0f);
+        }
+    }
+    __device__ __forceinline__ bool valid() const { return p < n; }
+};
+
 // Sum over the 32 lanes of v[e] for e = 0..31, leaving lane l with the total for e = l.
 // 31 shuffles instead of 32 separate butterflies; the summation order is fixed.
 __device__ __forceinline__ float warp_transpose_reduce32(float (&v)[32]) {

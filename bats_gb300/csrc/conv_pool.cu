@@ -301,6 +301,105 @@ conv_backward_cluster_kernel(const Event* __restrict__ ev, const int* __restrict
     cluster.sync();  // no CTA leaves while another still reads its shared memory
 }
 
+// Conv backward over events grouped by input position (the bucketed copy of the sort with
+// bucket_width = C: one bucket per (x, y), time order inside), on a cluster of CONV_BWD_CLUSTER CTAs per
+// sample (position groups dealt to the ranks). Thread = filter tap (co, dx, dy). Within a position group
+// every tap sees one and the same post neuron (x - dx, y - dy, co), so its spike data is set up once per
+// group and followed by a forward-only cursor over the group's time-ordered events, instead of a search
+// per (event, tap). A spike's slot (neuron j, k-th spike of j) follows from the order of appearance of j
+// in the group. The per-sample gradient copies are combined over the cluster as in
+// conv_backward_cluster_kernel; pre errors are reduced over the taps in the CTA that owns the group.
+__global__ void __launch_bounds__(1024)
+conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restrict__ boff, int n_pos,
+                             long long ev_cap, const float* __restrict__ W, int Y, int C, int fx, int fy, int C_out,
+                             int Xo, int Yo, int k_pre, const float* __restrict__ post_t,
+                             const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
+                             float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
+                             float* __restrict__ pre_err) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) float Gs[];  // taps * C, then C spike counters
+    __shared__ Event sev[32];
+    __shared__ float sred[32][33];
+    __shared__ int sslot[32];
+    const unsigned rank = cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int s = blockIdx.y;
+    const int taps = C_out * fx * fy;
+    const int total = taps * C;
+    int* kcount = reinterpret_cast<int*>(Gs + total);
+    const int n_post = Xo * Yo * C_out;
+    for (int q = tid; q < total; q += blockDim.x) Gs[q] = 0.0f;
+    const int* bo = boff + (long long)s * (n_pos + 1);
+    const Event* evs = ev_b + (long long)s * ev_cap;
+    // At most one tap per thread here (taps <= blockDim checked by the launcher).
+    const int tp = tid;
+    const bool has_tap = tp < taps;
+    const int co = has_tap ? tp / (fx * fy) : 0, dx = has_tap ? (tp / fy) % fx : 0, dy = has_tap ? tp % fy : 0;
+    __syncthreads();
+    for (int g = (int)rank; g < n_pos; g += CONV_BWD_CLUSTER) {
+        const int beg = bo[g], end = bo[g + 1];
+        if (beg >= end) continue;  // uniform over the CTA
+        const int xx = g / Y, yy = g % Y;
+        const int xo = xx - dx, yo = yy - dy;
+        const bool in = has_tap && xo >= 0 && yo >= 0 && xo < Xo && yo < Yo;
+        PostCursor cur;
+        const long long pn = in ? (long long)s * n_post + (xo * Yo + yo) * C_out + co : 0;
+        cur.init(post_t + pn * k_post, tab + pn * (k_post + 1), in ? nvalid[pn] : 0);
+        for (int q = tid; q < C; q += blockDim.x) kcount[q] = 0;
+        __syncthreads();
+        for (int m0 = beg; m0 < end; m0 += 32) {
+            const int cnt = min(32, end - m0);
+            if (tid < cnt) sev[tid] = evs[m0 + tid];
+            __syncthreads();
+            if (tid == 0) {
+                // Slots of the chunk's spikes: j * k_pre + (order of appearance of j in the group).
+                for (int q = 0; q < cnt; ++q) {
+                    const int j = sev[q].j;
+                    const int c = j % C;
+                    sslot[q] = j * k_pre + kcount[c];
+                    ++kcount[c];
+                }
+            }
+            for (int q = 0; q < cnt; ++q) {
+                const Event e = sev[q];
+                float term = 0.0f;
+                if (in) {
+                    cur.advance_past(e.t);
+                    if (cur.valid()) {
+                        const int cc = e.j % C;
+                        Gs[tp * C + cc] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
+                        if (pre_err)
+                            term = W[(long long)tp * C + cc] * (cur.AB.x * e.es / tau_s - cur.AB.y * e.e / tau);
+                    }
+                }
+                if (pre_err) {
+#pragma unroll
+                    for (int o = 16; o >= 1; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+                    if (lane == 0) sred[q][warp] = term;
+                }
+            }
+            __syncthreads();
+            if (pre_err && tid < cnt) {
+                float acc = 0.0f;
+                for (int w = 0; w < nwarps; ++w) acc += sred[tid][w];
+                pre_err[(long long)s * pre_slots + sslot[tid]] = acc;
+            }
+            __syncthreads();
+        }
+    }
+    cluster.sync();
+    const int per = (total + CONV_BWD_CLUSTER - 1) / CONV_BWD_CLUSTER;
+    const int q_end = min(total, ((int)rank + 1) * per);
+    for (int q = (int)rank * per + tid; q < q_end; q += blockDim.x) {
+        float acc = 0.0f;
+        for (int r = 0; r < CONV_BWD_CLUSTER; ++r) acc += cluster.map_shared_rank(Gs, r)[q];
+        grad[(long long)s * total + q] = acc;
+    }
+    cluster.sync();
+}
+
 // Pool forward: one thread per (sample, pooled neuron).
 __global__ void pool_forward_kernel(const int* __restrict__ n_spikes, const float* __restrict__ times, int batch, int X,
                                     int Y, int C, int K, int* __restrict__ out_n, float* __restrict__ out_t,
@@ -452,6 +551,47 @@ extern "C" int bats_conv_backward(const void* events, const int* ev_slot, const 
         post_times, reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots, grad_per_sample,
         pre_errors);
     BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_conv_backward_grouped(const void* events_bucketed, const int* bucket_offsets, long long ev_cap,
+                                          const float* weights, int batch, int X, int Y, int C, int fx, int fy,
+                                          int C_out, int k_pre, const float* post_times, const void* tables,
+                                          const int* nvalid, int k_post, float tau_s, float tau,
+                                          float* grad_per_sample, float* pre_errors, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && X >= fx && Y >= fy && fx > 0 && fy > 0 && C > 0 && C_out > 0 && k_post > 0 &&
+                     k_pre > 0,
+                 BATS_ERR_BAD_SHAPE, "conv_backward_grouped: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(events_bucketed && bucket_offsets && weights && post_times && tables && nvalid && grad_per_sample,
+                 BATS_ERR_NULL, "conv_backward_grouped: null pointer");
+    const long long taps = (long long)C_out * fx * fy;
+    BATS_REQUIRE(taps <= 1024 && (long long)X * Y <= 255, BATS_ERR_BAD_SHAPE,
+                 "conv_backward_grouped: needs at most 1024 taps and 255 input positions");
+    const int Xo = X - fx + 1, Yo = Y - fy + 1;
+    const long long pre_slots = (long long)X * Y * C * k_pre;
+    const size_t smem = (size_t)taps * C * sizeof(float) + (size_t)C * sizeof(int);
+    BATS_REQUIRE(smem <= 160 * 1024, BATS_ERR_BAD_SHAPE, "conv_backward_grouped: filter gradient too large");
+    if (pre_errors) BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)batch * pre_slots * sizeof(float), stream));
+    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_grouped_kernel, (int)smem));
+    const int threads = (int)(((taps + 31) / 32) * 32);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(bats::CONV_BWD_CLUSTER, batch);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = bats::CONV_BWD_CLUSTER;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_grouped_kernel,
+                                 reinterpret_cast<const bats::Event*>(events_bucketed), bucket_offsets, X * Y, ev_cap,
+                                 weights, Y, C, fx, fy, C_out, Xo, Yo, k_pre, post_times,
+                                 reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots,
+                                 grad_per_sample, pre_errors));
     return BATS_OK;
 }
 

@@ -34,39 +34,6 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 
-// Position of one post neuron's spike train relative to a time-ordered scan of pre spikes: p = first
-// post spike with t_p > the current pre-spike time, with its suffix-table entry AB = (SA_p, SB_p)
-// ((0, 0) once p reaches the neuron's n valid spikes). The entry after the current one is loaded ahead,
-// so an advance does not wait on a global load.
-struct PostCursor {
-    const float* tp;
-    const float2* tb;
-    int n, p;
-    float tn, tn1;
-    float2 AB, AB1;
-    __device__ __forceinline__ void init(const float* tp_, const float2* tb_, int n_) {
-        tp = tp_;
-        tb = tb_;
-        n = n_;
-        p = 0;
-        tn = n > 0 ? tp[0] : BATS_INF;
-        AB = n > 0 ? tb[0] : make_float2(0.0f, 0.0f);
-        tn1 = n > 1 ? tp[1] : BATS_INF;
-        AB1 = n > 1 ? tb[1] : make_float2(0.0f, 0.0f);
-    }
-    __device__ __forceinline__ void advance_past(float t) {
-        while (tn <= t) {
-            ++p;
-            tn = tn1;
-            AB = AB1;
-            const bool more = p + 1 < n;
-            tn1 = more ? tp[p + 1] : BATS_INF;
-            AB1 = more ? tb[p + 1] : make_float2(0.0f, 0.0f);
-        }
-    }
-    __device__ __forceinline__ bool valid() const { return p < n; }
-};
-
 // One thread per (sample, post neuron): recurrent (reset) errors in place, factors, suffix tables.
 //   recurrent: propagate_recurrent_errors.cu:17-22   factors: compute_factors.cu:20-30
 __global__ void bwd_prep_kernel(const float* __restrict__ t, const float* __restrict__ a, const float* __restrict__ x,

@@ -69,6 +69,7 @@ class Events:
     k: int
     bucketed: torch.Tensor | None = None
     bucket_offsets: torch.Tensor | None = None
+    bucket_width: int = 64
 
     @property
     def cap(self) -> int:
@@ -79,12 +80,13 @@ class Events:
         return self.events.shape[0]
 
 
-def alloc_events(batch: int, n_neurons: int, k: int, device="cuda", bucketed: bool = True) -> Events:
+def alloc_events(batch: int, n_neurons: int, k: int, device="cuda", bucketed: bool = True,
+                 bucket_width: int = BUCKET_WIDTH) -> Events:
     cap = n_neurons * k
     ev = Events(torch.empty((batch, cap, 4), dtype=F32, device=device),
                 torch.empty((batch, cap), dtype=I32, device=device),
-                torch.empty((batch,), dtype=I32, device=device), n_neurons, k)
-    n_buckets = (n_neurons + BUCKET_WIDTH - 1) // BUCKET_WIDTH
+                torch.empty((batch,), dtype=I32, device=device), n_neurons, k, bucket_width=int(bucket_width))
+    n_buckets = (n_neurons + bucket_width - 1) // bucket_width
     if bucketed and n_buckets <= 255:
         ev.bucketed = torch.empty((batch, cap, 4), dtype=F32, device=device)
         ev.bucket_offsets = torch.empty((batch, n_buckets + 1), dtype=I32, device=device)
@@ -92,20 +94,20 @@ def alloc_events(batch: int, n_neurons: int, k: int, device="cuda", bucketed: bo
 
 
 def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=None, out: Events | None = None,
-                bucketed: bool = True):
+                bucketed: bool = True, bucket_width: int = BUCKET_WIDTH):
     """Per-sample time sort of all valid pre-spikes (replaces get_sorted_spikes_indices, the
     take_along_axis gathers and compute_pre_exps; bats/Layers/LIFLayer.py:66-84). With `bucketed`, also
     the bucketed copy used by the weight gradient."""
     t = _c(spike_times)
     B, N, K = t.shape
     if out is None:
-        out = alloc_events(B, N, K, t.device, bucketed=bucketed)
+        out = alloc_events(B, N, K, t.device, bucketed=bucketed, bucket_width=bucket_width)
     ws_bytes = call_size("bats_sort_events_workspace_bytes", B, N, K)
     ws = workspace(ws_bytes, t.device) if ws_bytes else None
     es = _c(exp_tau_s) if exp_tau_s is not None else None
     ee = _c(exp_tau) if exp_tau is not None else None
     call("bats_sort_events", ptr(t), B, N, K, float(tau_s), float(tau), ptr(es), ptr(ee), ptr(out.events),
-         ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets), BUCKET_WIDTH, ptr(ws),
+         ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets), out.bucket_width, ptr(ws),
          ws_bytes, stream_ptr())
     return out
 
@@ -326,8 +328,10 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
         out = torch.empty(shape, dtype=F32, device=dev)
     ws_bytes = call_size("bats_weights_gradient_workspace_bytes", B, n_post, n_pre, g)
     ws = workspace(ws_bytes, dev) if ws_bytes else None
-    call("bats_weights_gradient", ptr(events.events), ptr(events.counts), ptr(events.bucketed),
-         ptr(events.bucket_offsets), events.cap, ptr(post_times), ptr(tabs.tables), ptr(tabs.nvalid), B, n_post,
+    # The bucketed copy serves this kernel only when it is grouped by BUCKET_WIDTH pre neurons.
+    by_bucket = events.bucketed is not None and events.bucket_width == BUCKET_WIDTH
+    call("bats_weights_gradient", ptr(events.events), ptr(events.counts), ptr(events.bucketed if by_bucket else None),
+         ptr(events.bucket_offsets if by_bucket else None), events.cap, ptr(post_times), ptr(tabs.tables), ptr(tabs.nvalid), B, n_post,
          k_post, n_pre, g, int(reduce == "mean"), ptr(out), ptr(ws), ws_bytes, stream_ptr())
     return out
 
@@ -376,6 +380,13 @@ def conv_backward(events: Events, filters, pre_shape, post_times, tabs: Backward
     dev = post_times.device
     grad = torch.empty((B, C_out, fx, fy, C), dtype=F32, device=dev)
     pre = torch.empty((B, events.n_neurons, events.k), dtype=F32, device=dev) if want_pre_errors else None
+    if (events.bucketed is not None and events.bucket_width == C and X * Y <= 255 and C_out * fx * fy <= 1024
+            and C_out * fx * fy * C * 4 + 4 * C <= 160 * 1024):
+        # Events grouped by input position: one post neuron per tap and group.
+        call("bats_conv_backward_grouped", ptr(events.bucketed), ptr(events.bucket_offsets), events.cap, ptr(W), B,
+             X, Y, C, fx, fy, C_out, events.k, ptr(post_times), ptr(tabs.tables), ptr(tabs.nvalid), k_post,
+             float(tau_s), float(tau), ptr(grad), ptr(pre), stream_ptr())
+        return grad, pre
     call("bats_conv_backward", ptr(events.events), ptr(events.slots), ptr(events.counts), events.cap, ptr(W), B, X, Y,
          C, fx, fy, C_out, events.k, ptr(post_times), ptr(tabs.tables), ptr(tabs.nvalid), k_post, float(tau_s),
          float(tau), ptr(grad), ptr(pre), stream_ptr())

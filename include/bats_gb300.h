@@ -106,6 +106,15 @@ int bats_conv_forward(const void* events, const int* ev_count, long long ev_cap,
                       float tau, float max_simulation, int* n_spikes, float* a, float* x, float* times,
                       float* post_exp_tau, cudaStream_t stream);
 
+/* bats_conv_backward over the events grouped by input position (the bucketed copy of bats_sort_events with
+ * bucket_width = C: one bucket per (x, y)); same outputs. For at most 1024 filter taps and 255 input
+ * positions. No counterpart in the reference (same results as compute_weights_gradient_conv +
+ * propagate_errors_to_pre_spikes_conv, computed from the position-grouped events). */
+int bats_conv_backward_grouped(const void* events_bucketed, const int* bucket_offsets, long long ev_cap,
+                               const float* weights, int batch, int X, int Y, int C, int fx, int fy, int C_out,
+                               int k_pre, const float* post_times, const void* tables, const int* nvalid, int k_post,
+                               float tau_s, float tau, float* grad_per_sample, float* pre_errors, cudaStream_t stream);
+
 /* 2x2 spike-union pooling of a (X, Y, C) layer with K slots: counts, times sorted over 4K slots and
  * the flat (batch-global) source slot of every output slot. Replaces aggregate_spikes_conv
  * (bats/CudaKernels/Wrappers/Inference/aggregate_spikes_conv.py:10-28). */

@@ -9,7 +9,7 @@ import torch
 from bats_gb300 import kernels as K
 from oracle import bats_ref64 as R
 from oracle import refkern
-from tests._helpers import conditioned_reference, count_mismatches, leading_mask, mnist_like_input
+from tests._helpers import conditioned_reference, count_mismatches, leading_mask, mnist_like_input, multi_spike_input
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -107,3 +107,29 @@ def test_conv_pool_conv_stack_vs_reference_kernels(cuda):
     scale_p = np.abs(rpe2).max() + 1e-30
     assert np.max(np.abs(g2 - rg2)) <= 1e-5 * scale_g, np.max(np.abs(g2 - rg2)) / scale_g
     assert np.max(np.abs(pe2 - rpe2)) <= 1e-5 * scale_p, np.max(np.abs(pe2 - rpe2)) / scale_p
+
+
+def test_position_grouped_conv_backward_matches_cluster_kernel(cuda):
+    """The conv backward over events grouped by input position (bucket width = input channels) gives the
+    per-sample filter gradient and the pre-spike errors of the event-ordered cluster kernel, up to the order
+    of the sums (1e-5 of the largest entry), on a 12x12x15 -> 5x5x8 layer with multi-spike input."""
+    import dataclasses
+    t, n_in = multi_spike_input(6, 12 * 12 * 15, 3, 0.2, seed=21, p_silent=0.3)
+    rng = np.random.default_rng(21)
+    filt = rng.uniform(-1, 1, (8, 5, 5, 15)).astype(np.float32)
+    tau_s = np.float32(0.13)
+    ev = K.sort_events(cu(t), tau_s, np.float32(2 * tau_s), bucket_width=15)
+    assert ev.bucketed is not None and ev.bucket_width == 15
+    out = K.conv_forward(ev, cu(filt), (12, 12, 15), 4, 0.13, 0.8, 0.8, 0.2)
+    n, a, x, ts, z = out
+    assert int(n.sum()) > 50
+    err = cu(rng.normal(size=ts.shape).astype(np.float32))
+    tau32, c, dtt = K.lif_constants(0.13, 0.8, 0.8)
+    tabs = K.backward_prep(ts, a, x, z, err, c, tau32, dtt)
+    g1, p1 = K.conv_backward(ev, cu(filt), (12, 12, 15), ts, tabs, tau_s, tau32, want_pre_errors=True)
+    plain = dataclasses.replace(ev, bucketed=None, bucket_offsets=None)
+    g2, p2 = K.conv_backward(plain, cu(filt), (12, 12, 15), ts, tabs, tau_s, tau32, want_pre_errors=True)
+    g1, g2, p1, p2 = (v.cpu().numpy().astype(np.float64) for v in (g1, g2, p1, p2))
+    assert np.abs(g1).max() > 0 and np.abs(p1).max() > 0
+    assert np.max(np.abs(g1 - g2)) <= 1e-5 * np.abs(g2).max()
+    assert np.max(np.abs(p1 - p2)) <= 1e-5 * np.abs(p2).max()
