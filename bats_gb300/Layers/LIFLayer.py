@@ -91,8 +91,11 @@ class LIFLayer(AbstractLayer):
 
     # -- compute -----------------------------------------------------------------------------
     def forward(self, max_simulation: float, training: bool = False) -> None:
-        pre_spike_per_neuron, _ = self.__previous_layer.spike_trains
-        self.__events = K.sort_events(pre_spike_per_neuron, self.__tau_s, self.__tau)
+        pre_spike_per_neuron, pre_n_spike_per_neuron = self.__previous_layer.spike_trains
+        # A LIF layer's trains are +inf past their counts, so the sort reads only the slots below them.
+        counted = isinstance(self.__previous_layer, LIFLayer) and pre_n_spike_per_neuron is not None
+        self.__events = K.sort_events(pre_spike_per_neuron, self.__tau_s, self.__tau,
+                                      pre_counts=pre_n_spike_per_neuron if counted else None)
         self.__wt = K.transpose_weights(self.__weights)
         (self.__n_spike_per_neuron, self.__a, self.__x, self.__spike_times_per_neuron,
          self.__post_exp_tau) = K.lif_forward_fc(self.__events, self.__wt, self.n_neurons, self.__max_n_spike,

@@ -34,8 +34,14 @@ extern "C" int bats_serve_fc_batch(const int* h_indices, const float* h_times, c
     const float* pre = d_trains;
     for (int l = 0; l < n_layers; ++l) {
         const BatsFcLayer& L = layers[l];
-        rc = bats_sort_events(pre, batch, L.n_pre, L.k_pre, L.tau_s, L.tau, nullptr, nullptr, L.events, L.slots,
-                              L.ev_count, nullptr, nullptr, 0, sort_workspace, sort_workspace_bytes, stream);
+        // The input trains are read whole; a LIF layer's output only below its spike counts.
+        if (l == 0)
+            rc = bats_sort_events(pre, batch, L.n_pre, L.k_pre, L.tau_s, L.tau, nullptr, nullptr, L.events, L.slots,
+                                  L.ev_count, nullptr, nullptr, 0, sort_workspace, sort_workspace_bytes, stream);
+        else
+            rc = bats_sort_events_counted(pre, layers[l - 1].n_spikes, batch, L.n_pre, L.k_pre, L.tau_s, L.tau,
+                                          nullptr, nullptr, L.events, L.slots, L.ev_count, nullptr, nullptr, 0,
+                                          sort_workspace, sort_workspace_bytes, stream);
         if (rc != BATS_OK) return rc;
         rc = bats_lif_forward_fc_algo(L.events, L.ev_count, (long long)L.n_pre * L.k_pre, L.weights_t, L.ld, batch,
                                       L.n_post, L.k_post, L.c, L.delta_theta_tau, L.tau, L.max_simulation,

@@ -47,6 +47,29 @@ __device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh,
     return off + in_warp;
 }
 
+// Block-wide exclusive scan of one int per thread (in thread order); block_total gets the sum.
+__device__ __forceinline__ int block_exclusive_scan(int v, SortShared& sh, int& block_total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) sh.warp_tot[warp] = incl;
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < SORT_WARPS; ++w) {
+        const int c = sh.warp_tot[w];
+        off += (w < warp) ? c : 0;
+        tot += c;
+    }
+    __syncthreads();
+    block_total = tot;
+    return off + incl - v;
+}
+
 // Exclusive scan of sh.hist (256 bins, one per thread) into sh.base; clears sh.wcnt.
 __device__ __forceinline__ void scan_bins(SortShared& sh) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -108,6 +131,15 @@ __device__ __forceinline__ void stable_pass(const uint32_t* ka, const uint32_t* 
     __syncthreads();
 }
 
+// Valid (finite) times among the first pre_counts[j] slots of pre neuron j.
+__device__ __forceinline__ int leading_valid(const int* cnt_src, const float* tsrc, int j, int k_pre) {
+    const int c = min(max(cnt_src[j], 0), k_pre);
+    const float* tj = tsrc + (long long)j * k_pre;
+    int v = 0;
+    for (int q = 0; q < c; ++q) v += tj[q] < BATS_INF;
+    return v;
+}
+
 __device__ __forceinline__ Event make_event(uint32_t key, uint32_t slot, int k_pre, long long sample_off,
                                             const float* exp_s_in, const float* exp_in, float tau_s, float tau) {
     Event e;
@@ -133,7 +165,8 @@ struct BucketDigit {
 };
 
 __global__ void __launch_bounds__(SORT_THREADS)
-sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, float tau_s, float tau,
+sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_counts, int n_slots, int k_pre,
+                   float tau_s, float tau,
                    const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out,
                    int* __restrict__ slot_out, int* __restrict__ ev_count, Event* __restrict__ ev_bucketed,
                    int* __restrict__ bucket_off, int bucket_width, int n_buckets, long long cap,
@@ -147,11 +180,14 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     const long long sample_off = (long long)s * n_slots;
     const float* tsrc = times + sample_off;
 
-    // Count valid slots first so that the buffers can be chosen. With 16-byte rows (n_slots % 4 == 0) each
-    // warp counts, and later compacts, its own contiguous range of slots, so neither pass needs a
-    // block-wide barrier per round.
+    // Count valid slots first so that the buffers can be chosen. With the pre layer's spike counts, neuron
+    // j's valid slots are its first pre_counts[j] (the forward kernels write +inf after them), so only
+    // those are read. Otherwise, with 16-byte rows (n_slots % 4 == 0) each warp counts, and later
+    // compacts, its own contiguous range of slots, so neither pass needs a block-wide barrier per round.
     int n = 0;
-    const bool vec = (n_slots & 3) == 0;
+    const int n_pre = n_slots / k_pre;
+    const int* cnt_src = pre_counts ? pre_counts + (long long)s * n_pre : nullptr;
+    const bool vec = !cnt_src && (n_slots & 3) == 0;
     const int n4 = n_slots >> 2;
     const int per_warp4 = (n4 + SORT_WARPS - 1) / SORT_WARPS;
     const int w_lo = min(n4, (tid >> 5) * per_warp4), w_hi = min(n4, w_lo + per_warp4);
@@ -167,6 +203,15 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
         __syncthreads();
 #pragma unroll
         for (int w = 0; w < SORT_WARPS; ++w) n += sh.warp_tot[w];
+    } else if (cnt_src) {
+        int c = 0;
+        for (int j = tid; j < n_pre; j += SORT_THREADS) c += leading_valid(cnt_src, tsrc, j, k_pre);
+        for (int o = 16; o >= 1; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if ((tid & 31) == 0) sh.warp_tot[tid >> 5] = c;
+        __syncthreads();
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; ++w) n += sh.warp_tot[w];
+        __syncthreads();
     } else {
         for (int r0 = 0; r0 < n_slots; r0 += SORT_THREADS) {
             const int slot = r0 + tid;
@@ -195,7 +240,27 @@ sort_events_kernel(const float* __restrict__ times, int n_slots, int k_pre, floa
     }
 
     // Compaction in slot order (stable).
-    if (vec) {
+    if (cnt_src) {
+        // Thread per pre neuron, rounds of SORT_THREADS neurons; each copies its leading valid slots.
+        int base = 0;
+        for (int r0 = 0; r0 < n_pre; r0 += SORT_THREADS) {
+            const int j = r0 + tid;
+            const int c = j < n_pre ? leading_valid(cnt_src, tsrc, j, k_pre) : 0;
+            int tot;
+            int pos = base + block_exclusive_scan(c, sh, tot);
+            const int slot0 = j * k_pre;
+            const int lim = c > 0 ? min(max(cnt_src[j], 0), k_pre) : 0;
+            for (int q = 0; q < lim; ++q) {
+                const float t = tsrc[slot0 + q];
+                if (t < BATS_INF) {
+                    ka[pos] = float_to_key(t);
+                    va[pos] = (uint32_t)(slot0 + q);
+                    ++pos;
+                }
+            }
+            base += tot;
+        }
+    } else if (vec) {
         int base = 0;
         for (int w = 0; w < (tid >> 5); ++w) base += sh.warp_tot[w];
         const int lane = tid & 31;
@@ -292,10 +357,10 @@ extern "C" size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_p
     return (size_t)batch * 4 * cap * sizeof(uint32_t);
 }
 
-extern "C" int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, float tau_s,
-                                float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out, int* slot_out,
-                                int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
-                                void* workspace, size_t workspace_bytes, cudaStream_t stream) {
+static int sort_events_impl(const float* pre_times, const int* pre_counts, int batch, int n_pre, int k_pre,
+                            float tau_s, float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out,
+                            int* slot_out, int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
+                            void* workspace, size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_pre >= 0 && k_pre > 0, BATS_ERR_BAD_SHAPE, "sort_events: bad shape");
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(pre_times && ev_out && ev_count, BATS_ERR_NULL, "sort_events: null pointer");
@@ -315,9 +380,28 @@ extern "C" int bats_sort_events(const float* pre_times, int batch, int n_pre, in
     const size_t smem = sizeof(bats::SortShared) + 4 * bats::SORT_SMEM_ITEMS * sizeof(uint32_t);
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel, (int)smem));
     bats::sort_events_kernel<<<batch, bats::SORT_THREADS, smem, stream>>>(
-        pre_times, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out,
+        pre_times, pre_counts, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out,
         ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets, cap,
         reinterpret_cast<uint32_t*>(workspace));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
+}
+
+extern "C" int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, float tau_s,
+                                float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out, int* slot_out,
+                                int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
+                                void* workspace, size_t workspace_bytes, cudaStream_t stream) {
+    return sort_events_impl(pre_times, nullptr, batch, n_pre, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out, slot_out,
+                            ev_count, ev_bucketed, bucket_offsets, bucket_width, workspace, workspace_bytes, stream);
+}
+
+extern "C" int bats_sort_events_counted(const float* pre_times, const int* pre_counts, int batch, int n_pre,
+                                        int k_pre, float tau_s, float tau, const float* exp_tau_s,
+                                        const float* exp_tau, void* ev_out, int* slot_out, int* ev_count,
+                                        void* ev_bucketed, int* bucket_offsets, int bucket_width, void* workspace,
+                                        size_t workspace_bytes, cudaStream_t stream) {
+    BATS_REQUIRE(pre_counts || batch == 0, BATS_ERR_NULL, "sort_events_counted: null pre_counts");
+    return sort_events_impl(pre_times, pre_counts, batch, n_pre, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out,
+                            slot_out, ev_count, ev_bucketed, bucket_offsets, bucket_width, workspace, workspace_bytes,
+                            stream);
 }

@@ -94,10 +94,11 @@ def alloc_events(batch: int, n_neurons: int, k: int, device="cuda", bucketed: bo
 
 
 def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=None, out: Events | None = None,
-                bucketed: bool = True, bucket_width: int = BUCKET_WIDTH):
+                bucketed: bool = True, bucket_width: int = BUCKET_WIDTH, pre_counts=None):
     """Per-sample time sort of all valid pre-spikes (replaces get_sorted_spikes_indices, the
     take_along_axis gathers and compute_pre_exps; bats/Layers/LIFLayer.py:66-84). With `bucketed`, also
-    the bucketed copy used by the weight gradient."""
+    the bucketed copy used by the weight gradient. `pre_counts` (B, N) int32, the spike counts of a LIF
+    layer's output (slots past each count are +inf), lets the sort read only the slots below the counts."""
     t = _c(spike_times)
     B, N, K = t.shape
     if out is None:
@@ -106,6 +107,13 @@ def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=N
     ws = workspace(ws_bytes, t.device) if ws_bytes else None
     es = _c(exp_tau_s) if exp_tau_s is not None else None
     ee = _c(exp_tau) if exp_tau is not None else None
+    if pre_counts is not None:
+        pc = _c(pre_counts, I32)
+        assert tuple(pc.shape) == (B, N), "pre_counts must be (B, N)"
+        call("bats_sort_events_counted", ptr(t), ptr(pc), B, N, K, float(tau_s), float(tau), ptr(es), ptr(ee),
+             ptr(out.events), ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets),
+             out.bucket_width, ptr(ws), ws_bytes, stream_ptr())
+        return out
     call("bats_sort_events", ptr(t), B, N, K, float(tau_s), float(tau), ptr(es), ptr(ee), ptr(out.events),
          ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets), out.bucket_width, ptr(ws),
          ws_bytes, stream_ptr())

@@ -231,20 +231,24 @@ class InferenceServer:
     def _layers(self, lane: _Lane, B: int, algos: Sequence[int], s: int, only: Optional[int] = None) -> None:
         """Per layer: event sort of the previous layer's spike trains, then the LIF forward with the given
         kernel variant. With `only`, just that layer's forward (used by the autotuner)."""
-        pre = lane.trains
+        pre, pre_n = lane.trains, None
         for li, spec in enumerate(self.specs):
             ev = lane.ev[li]
             tau32, c, dtt = self.consts[li]
-            if only is None:
+            if only is None and pre_n is None:
                 call("bats_sort_events", ptr(pre), B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)),
                      float(tau32), None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), None, None, 0,
                      ptr(lane.ws), lane.ws.numel(), s)
+            elif only is None:
+                call("bats_sort_events_counted", ptr(pre), ptr(pre_n), B, ev.n_neurons, ev.k,
+                     float(np.float32(spec.tau_s)), float(tau32), None, None, ptr(ev.events), ptr(ev.slots),
+                     ptr(ev.counts), None, None, 0, ptr(lane.ws), lane.ws.numel(), s)
             n, a, x, t, z = lane.out[li]
             if only is None or only == li:
                 call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.wt[li]),
                      self.wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt), float(tau32),
                      float(np.float32(self.max_sim)), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), int(algos[li]), s)
-            pre = t
+            pre, pre_n = t, n
 
     @staticmethod
     def _bucket(B: int) -> int:

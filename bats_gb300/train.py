@@ -101,22 +101,29 @@ class FCTrainStep:
         B = self.B
         ws, wsb = ptr(self.ws), self.ws.numel()
         L = []
-        pre_times = self.in_times
+        pre_times, pre_counts = self.in_times, None
         for li, spec in enumerate(self.specs):
             ev = self.ev[li]
             tau32, c, dtt = K.lif_constants(spec.tau_s, spec.theta, spec.delta_theta)
             tag = f"L{li + 1}"
-            L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), ev=ev, spec=spec, tau32=tau32: call(
-                "bats_sort_events", pt, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32), None,
-                None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
-                K.BUCKET_WIDTH, ws, wsb, s)))
+            if pre_counts is None:  # the network input: every slot is read
+                L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), ev=ev, spec=spec, tau32=tau32: call(
+                    "bats_sort_events", pt, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32),
+                    None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed),
+                    ptr(ev.bucket_offsets), K.BUCKET_WIDTH, ws, wsb, s)))
+            else:  # a LIF layer's output: only the slots below its spike counts
+                L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), pc=ptr(pre_counts), ev=ev, spec=spec,
+                          tau32=tau32: call(
+                    "bats_sort_events_counted", pt, pc, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)),
+                    float(tau32), None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed),
+                    ptr(ev.bucket_offsets), K.BUCKET_WIDTH, ws, wsb, s)))
             n, a, x, t, z = self.out[li]
             L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
                       call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
                            self.Wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt),
                            float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o), self.fwd_algo[li],
                            s)))
-            pre_times = t
+            pre_times, pre_counts = t, n
         n_out = self.out[-1][0]
         L.append(("loss", lambda s: call("bats_spike_count_loss", ptr(n_out), 0, None, ptr(self.labels),
                                          float(self.tt), float(self.tf), B, n_out.shape[1],

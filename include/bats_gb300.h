@@ -69,6 +69,17 @@ int bats_sort_events(const float* pre_times, int batch, int n_pre, int k_pre, fl
                      void* events_bucketed, int* bucket_offsets, int bucket_width, void* workspace,
                      size_t workspace_bytes, cudaStream_t stream);
 
+/* bats_sort_events given the pre layer's spike counts pre_counts (B, N_pre), as the reference's sort receives
+ * them (get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron),
+ * bats/CudaKernels/Wrappers/Inference/get_sorted_spikes_indices.py:7). Neuron j's slots q >= pre_counts[s, j]
+ * (clamped to [0, K_pre]) must hold +inf, as bats_lif_forward_fc writes them; only the slots below the count
+ * are read (and non-finite times among them skipped), so the outputs are identical to bats_sort_events on the
+ * same times. */
+int bats_sort_events_counted(const float* pre_times, const int* pre_counts, int batch, int n_pre, int k_pre,
+                             float tau_s, float tau, const float* exp_tau_s, const float* exp_tau, void* events,
+                             int* slot_out, int* ev_count, void* events_bucketed, int* bucket_offsets,
+                             int bucket_width, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
 /* Fully-connected LIF forward: spike counts (B, N_post) and a, x, times, post_exp_tau (B, N_post, K_post);
  * times/post_exp_tau are +inf after the spikes, a/x are undefined there. c = theta/tau,
  * delta_theta_tau = delta_theta/tau. Replaces get_spike_weights + compute_spike_times

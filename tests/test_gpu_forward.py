@@ -137,6 +137,57 @@ def test_sort_events_large_sample_uses_global_path(cuda):
         assert np.array_equal(ev.slots.cpu().numpy()[s, :cnt[s]], slots)
 
 
+def _events_equal(p, q, what):
+    cnt = p.counts.cpu().numpy()
+    assert np.array_equal(cnt, q.counts.cpu().numpy()), what
+    pe, qe = p.events.cpu().numpy(), q.events.cpu().numpy()
+    ps, qs = p.slots.cpu().numpy(), q.slots.cpu().numpy()
+    pb, qb = p.bucketed.cpu().numpy(), q.bucketed.cpu().numpy()
+    assert np.array_equal(p.bucket_offsets.cpu().numpy(), q.bucket_offsets.cpu().numpy()), what
+    for s in range(cnt.shape[0]):
+        c = cnt[s]
+        assert np.array_equal(pe[s, :c].view(np.uint32), qe[s, :c].view(np.uint32)), what
+        assert np.array_equal(ps[s, :c], qs[s, :c]), what
+        assert np.array_equal(pb[s, :c].view(np.uint32), qb[s, :c].view(np.uint32)), what
+
+
+@pytest.mark.parametrize("case", ["lif_output", "large", "irregular"])
+def test_sort_events_counted_matches_full_scan(cuda, case):
+    """The sort given the pre layer's spike counts (reading only the slots below them) returns the same
+    events, slots, counts and bucketed copy as the full scan: on a LIF layer's output, above the
+    shared-memory capacity, and with counts past K, negative counts, empty samples and non-finite times
+    below a count."""
+    rng = np.random.default_rng(21)
+    if case == "lif_output":
+        t, n_in = mnist_like_input(8, seed=3)
+        W = rng.uniform(-1, 1, (800, 784)).astype(np.float32)
+        (n, _, _, ts, _), _ = run_fc(t, W, 0.13, 0.2, 0.2, 30, 0.2)
+        assert n.sum() > 0
+        times, counts = ts, n.astype(np.int32)
+    elif case == "large":
+        times = np.sort(rng.uniform(0, 1, (3, 700, 12)).astype(np.float32), axis=2)
+        counts = rng.integers(0, 13, (3, 700)).astype(np.int32)
+        counts[0] = 12  # 8400 events: the global-memory path
+        times[np.arange(12)[None, None, :] >= counts[:, :, None]] = np.inf
+    else:
+        times = rng.uniform(0, 1, (4, 50, 5)).astype(np.float32)
+        counts = rng.integers(0, 6, (4, 50)).astype(np.int32)
+        times[np.arange(5)[None, None, :] >= counts[:, :, None]] = np.inf
+        counts[0, :3] = 9      # clamped to K
+        counts[0, 3] = -2      # treated as 0 (its slots are all inf)
+        times[0, 3] = np.inf
+        counts[1] = 0
+        times[1] = np.inf      # empty sample
+        times[2, 7, 0] = np.inf if counts[2, 7] > 1 else times[2, 7, 0]  # hole below a count
+        times[3, 9, :] = np.inf
+        counts[3, 9] = 5       # count above the finite slots
+    tt = torch.tensor(times, device="cuda")
+    full = K.sort_events(tt, np.float32(0.1), np.float32(0.2))
+    part = K.sort_events(tt, np.float32(0.1), np.float32(0.2), pre_counts=torch.tensor(counts, device="cuda"))
+    torch.cuda.synchronize()
+    _events_equal(full, part, case)
+
+
 def test_edge_cases(cuda):
     rng = np.random.default_rng(9)
     W = rng.uniform(-1, 1, (37, 20)).astype(np.float32)
