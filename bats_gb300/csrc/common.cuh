@@ -181,12 +181,15 @@ struct PostCursor {
     __device__ __forceinline__ bool valid() const { return p < n; }
 };
 
-// Sum over the 32 lanes of v[e] for e = 0..31, leaving lane l with the total for e = l.
-// 31 shuffles instead of 32 separate butterflies; the summation order is fixed.
-__device__ __forceinline__ float warp_transpose_reduce32(float (&v)[32]) {
+// Sum over the 32 lanes of v[e] for e = 0..N-1 (N = 32 or 16), leaving lane l with the total for
+// e = l mod N. N - 1 shuffles (N for N = 16: the two half-warps are added last) instead of N separate
+// butterflies; the summation order is fixed.
+template <int N>
+__device__ __forceinline__ float warp_transpose_reduce(float (&v)[N]) {
+    static_assert(N == 32 || N == 16, "32 or 16 values per lane");
     const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
+    for (int off = N / 2; off >= 1; off >>= 1) {
         const bool upper = (lane & off) != 0;
 #pragma unroll
         for (int q = 0; q < off; ++q) {
@@ -195,6 +198,7 @@ __device__ __forceinline__ float warp_transpose_reduce32(float (&v)[32]) {
             v[q] = keep + __shfl_xor_sync(0xffffffffu, send, off);
         }
     }
+    if (N == 16) v[0] += __shfl_xor_sync(0xffffffffu, v[0], 16);
     return v[0];
 }
 

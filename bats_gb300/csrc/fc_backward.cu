@@ -369,25 +369,24 @@ __global__ void reduce_groups_kernel(const float* __restrict__ partial, long lon
 
 // Errors of the pre-synaptic spikes. Grid (post tiles, B), TILE consumer threads (one per post
 // neuron) + one producer warp. As in the forward kernel, the producer streams the sample's events and
-// their weight-row segments wt[j, tile] into shared-memory stages with bulk copies; a stage holds 32
-// events. The reference's per-(pre spike, post neuron) term is w * (SA e_s / tau_s - SB e / tau) with
+// their weight-row segments wt[j, tile] into shared-memory stages with bulk copies; a stage holds SEV
+// (16) events. The reference's per-(pre spike, post neuron) term is w * (SA e_s / tau_s - SB e / tau) with
 // SA, SB the suffix sums of the post neuron after the event; summed over post neurons this is
 // (sum w SA) e_s / tau_s - (sum w SB) e / tau, so each consumer only forms w*SA and w*SB for its neuron.
-// Both are summed over the warp by fixed-order transpose-reductions (31 shuffles per 32 events), then
+// Both are summed over the warp by fixed-order transpose-reductions (16 shuffles per 16 events), then
 // over the tile's warps, into partial[(s, m, tile, 0..1)]; pre_err_scatter_kernel sums the tiles in
 // order, applies the event's factors and writes the result to the event's (neuron, slot).
-template <int TILE, int STAGES>
-__global__ void __launch_bounds__(TILE + 32, 3)
+template <int TILE, int SEV, int STAGES>
+__global__ void __launch_bounds__(TILE + 32, 4)
 bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                    const float* __restrict__ wt, int ld, const float* __restrict__ post_t,
                    const float2* __restrict__ tab, const int* __restrict__ nvalid, int n_post, int k_post,
                    float2* __restrict__ partial, int n_tiles, int* __restrict__ status) {
-    constexpr int SEV = 32;
     constexpr int WARPS = TILE / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using Smem = StreamSmem<TILE, SEV, STAGES>;
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
-    __shared__ float2 sred[2][WARPS][32];
+    __shared__ float2 sred[2][WARPS][SEV];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int s = blockIdx.y;
     const int tile0 = blockIdx.x * TILE;
@@ -413,9 +412,9 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
         if (!stream_acquire(sm, k, status)) return;
         const int m0 = k * SEV;
         const int cnt = min(SEV, E - m0);
-        float va[32], vb[32];
+        float va[SEV], vb[SEV];
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
+        for (int q = 0; q < SEV; ++q) {
             const float t = sm.evs[slot][q].t;
             if (q < cnt) cur.advance_past(t);
             const float w = sm.rows[slot][q][tid];
@@ -424,13 +423,13 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
             vb[q] = use ? w * cur.AB.y : 0.0f;
         }
         stream_release(sm, k);
-        const float ra = warp_transpose_reduce32(va);
-        const float rb = warp_transpose_reduce32(vb);
+        const float ra = warp_transpose_reduce<SEV>(va);
+        const float rb = warp_transpose_reduce<SEV>(vb);
         float2* dst = partial + ((long long)s * ev_cap + m0) * n_tiles + blockIdx.x;
         if (WARPS == 1) {
             if (lane < cnt) dst[(long long)lane * n_tiles] = make_float2(ra, rb);
         } else {
-            sred[k & 1][warp][lane] = make_float2(ra, rb);
+            if (lane < SEV) sred[k & 1][warp][lane] = make_float2(ra, rb);
             asm volatile("bar.sync 1, %0;" ::"r"(TILE) : "memory");
             if (warp == 0 && lane < cnt) {
                 float sa = 0.0f, sb = 0.0f;
@@ -658,12 +657,13 @@ template <int TILE>
 static int launch_pre_err(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld,
                           const float* post_times, const void* tables, const int* nvalid, int batch, int n_post,
                           int k_post, float2* part, int* status, cudaStream_t stream) {
-    constexpr int STAGES = 4;
+    constexpr int SEV = 16, STAGES = 6;
     const int tiles = (n_post + TILE - 1) / TILE;
-    const size_t smem = sizeof(bats::StreamSmem<TILE, 32, STAGES>);
-    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_kernel<TILE, STAGES>, (int)smem));
+    const size_t smem = sizeof(bats::StreamSmem<TILE, SEV, STAGES>);
+    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_kernel<TILE, SEV, STAGES>,
+                                                      (int)smem));
     dim3 grid(tiles, batch);
-    bats::bwd_pre_err_kernel<TILE, STAGES><<<grid, TILE + 32, smem, stream>>>(
+    bats::bwd_pre_err_kernel<TILE, SEV, STAGES><<<grid, TILE + 32, smem, stream>>>(
         reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, wt, ld, post_times,
         reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, part, tiles, status);
     BATS_CUDA(cudaGetLastError());

@@ -312,8 +312,10 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
     if (n_post <= 64)
         return bats::launch_forward<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                               n_spikes, a, x, times, post_exp_tau, status, stream);
-    return bats::launch_forward<128, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
-                                           n_spikes, a, x, times, post_exp_tau, status, stream);
+    // 8-event stages: half the shared memory of 16-event stages, so 7 CTAs (28 consumer warps) fit on an SM
+    // instead of 4, and a replay after a possible crossing covers fewer events.
+    return bats::launch_forward<128, 8, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+                                          n_spikes, a, x, times, post_exp_tau, status, stream);
 }
 
 extern "C" int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap) {
