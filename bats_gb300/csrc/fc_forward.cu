@@ -71,19 +71,32 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
             // stage overlap; events past the sample's end (last stage) leave the state unchanged.
             float aa = a, bb = b;
             unsigned cand = 0u;
+            if (m0 + SEV < E) {
+                // A full stage followed by more events (every stage but the last): no bounds to select on.
 #pragma unroll
-            for (int u = 0; u < SEV; ++u) {
-                const float4 e4 = *reinterpret_cast<const float4*>(&se[u]);  // (t, j, es, e)
-                const float e_nx = se[u + 1].e;
-                const float w = sm.rows[slot][u][tid];
-                const bool in = u < cnt;
-                const float a2 = fmaf(w, e4.z, aa);
-                const float b2 = fmaf(w, e4.w, bb);
-                aa = in ? a2 : aa;
-                bb = in ? b2 : bb;
-                const float e_next = (m0 + u + 1 < E) ? e_nx : BATS_INF;
-                const bool maybe = !no_crossing<false, false>(aa, bb, e4.w, e_next, sk);
-                cand |= (in && maybe) ? (1u << u) : 0u;
+                for (int u = 0; u < SEV; ++u) {
+                    const float4 e4 = *reinterpret_cast<const float4*>(&se[u]);  // (t, j, es, e)
+                    const float e_nx = se[u + 1].e;
+                    const float w = sm.rows[slot][u][tid];
+                    aa = fmaf(w, e4.z, aa);
+                    bb = fmaf(w, e4.w, bb);
+                    cand |= no_crossing<false, false>(aa, bb, e4.w, e_nx, sk) ? 0u : (1u << u);
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < SEV; ++u) {
+                    const float4 e4 = *reinterpret_cast<const float4*>(&se[u]);
+                    const float e_nx = se[u + 1].e;
+                    const float w = sm.rows[slot][u][tid];
+                    const bool in = u < cnt;
+                    const float a2 = fmaf(w, e4.z, aa);
+                    const float b2 = fmaf(w, e4.w, bb);
+                    aa = in ? a2 : aa;
+                    bb = in ? b2 : bb;
+                    const float e_next = (m0 + u + 1 < E) ? e_nx : BATS_INF;
+                    const bool maybe = !no_crossing<false, false>(aa, bb, e4.w, e_next, sk);
+                    cand |= (in && maybe) ? (1u << u) : 0u;
+                }
             }
             if (cand == 0u) {
                 a = aa;
