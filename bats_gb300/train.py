@@ -315,6 +315,62 @@ class FCTrainStep:
         torch.cuda.current_stream().synchronize()
         return self.h_loss.numpy()
 
+    def train_host(self, batches) -> List[np.ndarray]:
+        """Train on an iterable of host batches (times (B, N_in, K_in), labels (B,)), one step per batch;
+        returns each step's per-sample losses. Every step copies its inputs host -> device and its losses
+        back, as step_host does, but the copies are pipelined: batch i+1 is staged into pinned memory and
+        copied on a side stream while step i computes (two pinned and two device slots), and step i's
+        losses are read back when its slot is reused. Results are those of step_host called per batch."""
+        dev = self.in_times.device
+        if not hasattr(self, "_pipe"):
+            self._pipe = {
+                "h_in": [torch.empty(self.in_times.shape, dtype=torch.float32, pin_memory=True) for _ in range(2)],
+                "h_lab": [torch.empty((self.B,), dtype=torch.int32, pin_memory=True) for _ in range(2)],
+                "d_in": [torch.empty_like(self.in_times) for _ in range(2)],
+                "d_lab": [torch.empty_like(self.labels) for _ in range(2)],
+                "h_loss": [torch.empty((self.B,), dtype=torch.float32, pin_memory=True) for _ in range(2)],
+                "copy": torch.cuda.Stream(device=dev),
+            }
+        P = self._pipe
+        comp = torch.cuda.current_stream(dev)
+        staged = [None, None]    # H2D of the slot finished (the pinned buffer may be refilled)
+        consumed = [None, None]  # the step has copied the device slot into its input buffers
+        done = [None, None]      # the step's losses are in the pinned loss slot
+        losses: List[np.ndarray] = []
+        order: List[int] = []
+        for i, (times, labels) in enumerate(batches):
+            k = i & 1
+            if done[k] is not None:  # step i-2: read its losses before the slot is reused
+                done[k].synchronize()
+                losses.append(P["h_loss"][k].numpy().copy())
+            if staged[k] is not None:
+                staged[k].synchronize()
+            P["h_in"][k].numpy()[...] = times
+            P["h_lab"][k].numpy()[...] = labels
+            cs = P["copy"]
+            if consumed[k] is not None:
+                cs.wait_event(consumed[k])
+            with torch.cuda.stream(cs):
+                P["d_in"][k].copy_(P["h_in"][k], non_blocking=True)
+                P["d_lab"][k].copy_(P["h_lab"][k], non_blocking=True)
+                staged[k] = torch.cuda.Event()
+                staged[k].record(cs)
+            comp.wait_event(staged[k])
+            self.in_times.copy_(P["d_in"][k], non_blocking=True)
+            self.labels.copy_(P["d_lab"][k], non_blocking=True)
+            consumed[k] = torch.cuda.Event()
+            consumed[k].record(comp)
+            self.run()
+            P["h_loss"][k].copy_(self.loss, non_blocking=True)
+            done[k] = torch.cuda.Event()
+            done[k].record(comp)
+            order.append(k)
+        n = len(order)
+        for k in order[max(0, n - 2):]:  # the last one or two steps, in step order
+            done[k].synchronize()
+            losses.append(P["h_loss"][k].numpy().copy())
+        return losses
+
     @property
     def h2d_bytes(self) -> int:
         return self.h_times.numel() * 4 + self.h_labels.numel() * 4

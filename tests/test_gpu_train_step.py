@@ -104,3 +104,25 @@ def test_graph_replay_equals_eager_and_autotune_keeps_results(cuda):
     torch.cuda.synchronize()
     for a, b in zip(tuned.W, plain.W):
         assert float((a - b).abs().max()) <= 1e-6 * float(b.abs().max())
+
+
+def test_train_host_pipeline_matches_step_host(cuda):
+    """train_host (inputs copied from host memory on a side stream while the previous step computes,
+    losses read back per step) gives the losses and weights of step_host called batch by batch, bit for
+    bit, over five different batches (graph replay in both)."""
+    batches = []
+    for q in range(5):
+        t, _, _, labels = case(seed=10 + q)
+        batches.append((t, labels))
+    t0, _, ws, labels0 = case()
+    a = make_step(t0, ws, labels0)
+    b = make_step(t0, ws, labels0)
+    assert a.try_capture() and b.try_capture()
+    ref = [a.step_host(t, lab).copy() for t, lab in batches]
+    got = b.train_host(batches)
+    torch.cuda.synchronize()
+    assert len(got) == len(ref)
+    for q, (x, y) in enumerate(zip(ref, got)):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), f"loss of step {q}"
+    for wa, wb in zip(a.W, b.W):
+        assert torch.equal(wa, wb)
