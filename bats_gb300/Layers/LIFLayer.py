@@ -108,7 +108,7 @@ class LIFLayer(AbstractLayer):
                 and errors.is_contiguous()):
             errors = to_device(errors, torch.float32).clone()
         tabs = K.backward_prep(self.__spike_times_per_neuron, self.__a, self.__x, self.__post_exp_tau, errors,
-                               self.__c, self.__tau, self.__delta_theta_tau)
+                               self.__c, self.__tau, self.__delta_theta_tau, n_spikes=self.__n_spike_per_neuron)
         weights_grad = K.weights_gradient(self.__events, self.__spike_times_per_neuron, tabs,
                                           self.__previous_layer.n_neurons, per_sample=True)
         if self.__previous_layer.trainable:

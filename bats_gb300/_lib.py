@@ -56,6 +56,8 @@ SIGNATURES = {
     "bats_pool_forward": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
     "bats_backward_prep": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                    c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "bats_backward_prep_counted": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float,
+                                           c_float, c_vp, c_vp, c_vp]),
     "bats_backward_prep_layer": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                          c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_weights_gradient_workspace_bytes": (c_size, [c_int, c_int, c_int, c_int]),

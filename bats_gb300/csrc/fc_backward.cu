@@ -217,6 +217,130 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
     }
 }
 
+// Layer-path prep given the forward's spike counts: only each neuron's leading min(n_spikes, K) slots
+// are read (the forward writes +inf past them), so silent slots cost nothing. A warp handles 32 neurons
+// and stages their valid slots compactly in shared memory (at most PREPC_CAP per round; a round takes
+// the next lanes whose slots fit), then each lane runs bwd_prep_layer_kernel's arithmetic on its
+// neuron, so errors, tables and counts are identical to it (n = the first +inf time below the count,
+// or the count).
+constexpr int PREPC_WARPS = 4;
+constexpr int PREPC_CAP = 256;
+
+struct PrepCompact {
+    float t[PREPC_CAP], z[PREPC_CAP], x[PREPC_CAP], a[PREPC_CAP], e[PREPC_CAP];
+    unsigned char owner[PREPC_CAP];
+};
+
+__global__ void __launch_bounds__(PREPC_WARPS * 32)
+bwd_prep_counted_kernel(const float* __restrict__ t, const int* __restrict__ n_spikes, const float* __restrict__ a,
+                        const float* __restrict__ x, const float* __restrict__ z, float* __restrict__ err,
+                        long long total, int K, float c, float tau, float dtt, float2* __restrict__ tab,
+                        int* __restrict__ nvalid) {
+    __shared__ PrepCompact sm_all[PREPC_WARPS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    PrepCompact& sm = sm_all[warp];
+    const long long nb = ((long long)blockIdx.x * PREPC_WARPS + warp) * 32;
+    if (nb >= total) return;
+    const int cnt = (int)min(32LL, total - nb);
+    const int K1 = K + 1;
+    const int n_in = lane < cnt ? min(max(n_spikes[nb + lane], 0), K) : 0;
+    // Inclusive prefix of the counts over the warp's lanes.
+    int incl = n_in;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int excl = incl - n_in;
+    int r0 = 0, base = 0;
+    while (r0 < 32) {
+        const unsigned in_round = __ballot_sync(0xffffffffu, lane >= r0 && incl - base <= PREPC_CAP);
+        const int r1 = 32 - __clz(in_round);
+        const int V = __shfl_sync(0xffffffffu, incl, r1 - 1) - base;
+        const bool mine = lane >= r0 && lane < r1;
+        const int off = excl - base;  // this lane's first compact entry (valid when mine)
+        if (mine)
+            for (int k = 0; k < n_in; ++k) sm.owner[off + k] = (unsigned char)lane;
+        __syncwarp();
+        for (int q0 = 0; q0 < V; q0 += 32) {
+            const int q = q0 + lane;
+            const int r = q < V ? sm.owner[q] : 0;
+            const int ro = __shfl_sync(0xffffffffu, excl, r) - base;
+            if (q < V) {
+                const long long src = (nb + r) * K + (q - ro);
+                cp_async4(sm.t + q, t + src);
+                cp_async4(sm.z + q, z + src);
+                cp_async4(sm.x + q, x + src);
+                cp_async4(sm.a + q, a + src);
+                cp_async4(sm.e + q, err + src);
+            }
+        }
+        cp_async_wait_all();
+        __syncwarp();
+        int n = 0;
+        if (mine) {
+            float* rt = sm.t + off;
+            float* rz = sm.z + off;
+            float* rx = sm.x + off;
+            float* ra = sm.a + off;
+            float* re = sm.e + off;
+            n = n_in;
+            for (int k = 0; k < n_in; ++k)
+                if (isinf(rt[k])) {
+                    n = k;
+                    break;
+                }
+            float cum = 0.0f;
+            for (int k = n - 1; k >= 0; --k) {
+                const float ek = re[k] + cum * rz[k];
+                re[k] = ek;
+                cum += ek * dtt / rx[k];
+            }
+            for (int k = 0; k < n; ++k) {
+                const float xk = rx[k];
+                ra[k] = tau / ra[k] * (1 + rz[k] * c / xk);
+                rz[k] = tau / xk;
+            }
+            for (int p0 = 0; p0 < n; p0 += 4) {
+                float sa[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sb[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                for (int k = p0; k < n; ++k) {
+                    const float ek = re[k], fa = ra[k], fb = rz[k];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (k >= p0 + u) {
+                            sa[u] += ek * fa;
+                            sb[u] += ek * fb;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (p0 + u < n) {
+                        rt[p0 + u] = sa[u];
+                        rx[p0 + u] = sb[u];
+                    }
+                }
+            }
+        }
+        if (mine && lane < cnt) nvalid[nb + lane] = n;
+        __syncwarp();
+        for (int q0 = 0; q0 < V; q0 += 32) {
+            const int q = q0 + lane;
+            const int r = q < V ? sm.owner[q] : 0;
+            const int ro = __shfl_sync(0xffffffffu, excl, r) - base;
+            const int nr = __shfl_sync(0xffffffffu, n, r);
+            const int k = q - ro;
+            if (q < V && k < nr) {
+                err[(nb + r) * K + k] = sm.e[q];
+                tab[(nb + r) * K1 + k] = make_float2(sm.t[q], sm.x[q]);
+            }
+        }
+        __syncwarp();
+        r0 = r1;
+        base += V;
+    }
+}
+
 constexpr int BWD_CHUNK = 128;
 
 // Weight gradient. Grid (post tiles, pre chunks, sample groups); each thread owns one post
@@ -583,6 +707,25 @@ extern "C" int bats_backward_prep_layer(const float* post_times, const float* a,
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_prep_layer_kernel, (int)smem));
     bats::bwd_prep_layer_kernel<<<blocks, bats::PREP_WARPS * 32, smem, stream>>>(
         post_times, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau, f1, f2,
+        reinterpret_cast<float2*>(tables), nvalid);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
+extern "C" int bats_backward_prep_counted(const float* post_times, const int* n_spikes, const float* a, const float* x,
+                                          const float* post_exp_tau, float* errors, int batch, int n_post, int k_post,
+                                          float c, float tau, float delta_theta_tau, void* tables, int* nvalid,
+                                          cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0, BATS_ERR_BAD_SHAPE, "backward_prep_counted: bad shape");
+    BATS_REQUIRE(k_post <= 32, BATS_ERR_BAD_SHAPE, "backward_prep_counted: k_post > 32 (use bats_backward_prep_layer)");
+    const long long total = (long long)batch * n_post;
+    if (total == 0) return BATS_OK;
+    BATS_REQUIRE(post_times && n_spikes && a && x && post_exp_tau && errors && tables && nvalid, BATS_ERR_NULL,
+                 "backward_prep_counted: null pointer");
+    const long long warps = (total + 31) / 32;
+    const int blocks = (int)((warps + bats::PREPC_WARPS - 1) / bats::PREPC_WARPS);
+    bats::bwd_prep_counted_kernel<<<blocks, bats::PREPC_WARPS * 32, 0, stream>>>(
+        post_times, n_spikes, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau,
         reinterpret_cast<float2*>(tables), nvalid);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;

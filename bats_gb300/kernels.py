@@ -265,11 +265,12 @@ class BackwardTables:
 
 
 def backward_prep(post_times, a, x, post_exp_tau, errors, c: float, tau: float, delta_theta_tau: float,
-                  recurrent: bool = True, out: BackwardTables | None = None, want_factors: bool = False
-                  ) -> BackwardTables:
+                  recurrent: bool = True, out: BackwardTables | None = None, want_factors: bool = False,
+                  n_spikes=None) -> BackwardTables:
     """Reset errors in place + factors + suffix tables (replaces propagate_recurrent_errors and
     compute_factors, Wrappers/Backpropagation/propagate_recurrent_errors.py:9-16, compute_factors.py:11-22).
-    For the forward kernels' outputs (the layer path); f1/f2 are only materialised if want_factors."""
+    For the forward kernels' outputs (the layer path); f1/f2 are only materialised if want_factors. With the
+    forward's spike counts `n_spikes` (B, N) only the slots below them are read."""
     B, N, K = post_times.shape
     dev = post_times.device
     need_f = want_factors or K > 32 or not recurrent
@@ -278,7 +279,11 @@ def backward_prep(post_times, a, x, post_exp_tau, errors, c: float, tau: float, 
                              torch.empty((B, N, K), dtype=F32, device=dev) if need_f else None,
                              torch.empty((B, N, K + 1, 2), dtype=F32, device=dev),
                              torch.empty((B, N), dtype=I32, device=dev))
-    if recurrent:
+    if recurrent and n_spikes is not None and not need_f:
+        call("bats_backward_prep_counted", ptr(post_times), ptr(_c(n_spikes, I32)), ptr(a), ptr(x),
+             ptr(post_exp_tau), ptr(errors), B, N, K, float(c), float(tau), float(delta_theta_tau),
+             ptr(out.tables), ptr(out.nvalid), stream_ptr())
+    elif recurrent:
         call("bats_backward_prep_layer", ptr(post_times), ptr(a), ptr(x), ptr(post_exp_tau), ptr(errors), B, N, K,
              float(c), float(tau), float(delta_theta_tau), ptr(out.f1), ptr(out.f2), ptr(out.tables),
              ptr(out.nvalid), stream_ptr())

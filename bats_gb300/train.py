@@ -136,10 +136,16 @@ class FCTrainStep:
             tau32, c, dtt = K.lif_constants(spec.tau_s, spec.theta, spec.delta_theta)
             tb = self.tabs[li]
             tag = f"L{li + 1}"
-            L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt, tb=tb:
-                      call("bats_backward_prep_layer", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]), ptr(e), B,
-                           spec.n_neurons, spec.max_n_spike, float(c), float(tau32), float(dtt), ptr(tb.f1),
-                           ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
+            if spec.max_n_spike <= 32:  # only the slots below the forward's spike counts are read
+                L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt,
+                          tb=tb: call("bats_backward_prep_counted", ptr(o[3]), ptr(o[0]), ptr(o[1]), ptr(o[2]),
+                                      ptr(o[4]), ptr(e), B, spec.n_neurons, spec.max_n_spike, float(c),
+                                      float(tau32), float(dtt), ptr(tb.tables), ptr(tb.nvalid), s)))
+            else:
+                L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt,
+                          tb=tb: call("bats_backward_prep_layer", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]),
+                                      ptr(e), B, spec.n_neurons, spec.max_n_spike, float(c), float(tau32),
+                                      float(dtt), ptr(tb.f1), ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
             L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
                 "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
                 ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,

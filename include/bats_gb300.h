@@ -169,6 +169,16 @@ int bats_backward_prep_layer(const float* post_times, const float* a, const floa
                              float delta_theta_tau, float* f1, float* f2, void* tables, int* nvalid,
                              cudaStream_t stream);
 
+/* bats_backward_prep_layer given the forward's spike counts n_spikes (B, N_post): only each neuron's first
+ * min(n_spikes, K) slots are read (the forward writes +inf past them), valid slots are staged compactly, and
+ * errors, tables and nvalid are identical to bats_backward_prep_layer's (nvalid = the first +inf time below
+ * the count, or the count). No f1/f2 output; k_post <= 32. Replaces propagate_recurrent_errors and
+ * compute_factors (bats/CudaKernels/Wrappers/Backpropagation/propagate_recurrent_errors.py:9-16,
+ * compute_factors.py:11-22), which the reference runs over all N_post * K slots. */
+int bats_backward_prep_counted(const float* post_times, const int* n_spikes, const float* a, const float* x,
+                               const float* post_exp_tau, float* errors, int batch, int n_post, int k_post, float c,
+                               float tau, float delta_theta_tau, void* tables, int* nvalid, cudaStream_t stream);
+
 /* Weight gradient of a fully-connected layer. group == 1: per-sample gradient (B, N_post, N_pre) like the
  * reference; group > 1: the batch mean (mean != 0) or sum (N_post, N_pre), accumulated per group of samples
  * and reduced in a fixed order (deterministic). Reads the events grouped in pre-neuron buckets of 64

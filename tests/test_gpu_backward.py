@@ -251,3 +251,47 @@ def test_layer_prep_matches_generic_prep_bit_for_bit(cuda):
     valid = np.arange(Kp + 1)[None, None, :] < nv[:, :, None]
     a_tab, b_tab = tl.tables.cpu().numpy(), tg.tables.cpu().numpy()
     assert np.array_equal(a_tab[valid].view(np.uint32), b_tab[valid].view(np.uint32))
+
+
+@pytest.mark.parametrize("case", ["heavy", "irregular"])
+def test_counted_prep_matches_layer_prep_bit_for_bit(cuda, case):
+    """bats_backward_prep_counted (only the slots below the forward's spike counts, staged compactly in
+    rounds of at most 256 per warp) against bats_backward_prep_layer on the same forward state: reset
+    errors, counts and every table entry before a neuron's count are identical. "heavy": most neurons
+    spike 10-30 times, so warps need several rounds; "irregular": counts past the finite slots, a +inf
+    time below a count, negative counts of silent neurons."""
+    rng = np.random.default_rng(12)
+    if case == "heavy":
+        t, n_in = multi_spike_input(8, 80, 8, 0.15, seed=12, p_silent=0.0)
+        W = (rng.uniform(0.2, 1.0, (96, 80)) * 2.0).astype(np.float32)
+    else:
+        t, n_in = multi_spike_input(16, 60, 5, 0.1, seed=13, p_silent=0.1)
+        W = (rng.uniform(-0.3, 1.0, (70, 60)) * 1.5).astype(np.float32)
+    tau_s, th = 0.1, 0.2
+    ev = K.sort_events(cu(t), tau_s, 2 * tau_s)
+    n, a, x, ts, z = K.lif_forward_fc(ev, K.transpose_weights(cu(W)), W.shape[0], 30, tau_s, th, th)
+    counts = n.clone()
+    if case == "heavy":
+        assert float(n.float().mean()) >= 10, "most neurons should spike many times"
+    else:
+        nn = n.cpu().numpy()
+        s, i = np.argwhere(nn >= 3)[0]
+        ts[s, i, 1] = float("inf")                  # a +inf time below the count
+        s2, i2 = np.argwhere(nn <= 20)[1]
+        counts[s2, i2] += 5                         # count past the finite slots
+        silent = np.argwhere(nn == 0)
+        if len(silent):
+            counts[silent[0][0], silent[0][1]] = -3  # negative count of a silent neuron
+    err = cu(rng.normal(size=ts.shape).astype(np.float32))
+    tau32, c, dtt = K.lif_constants(tau_s, th, th)
+    e1, e2 = err.clone(), err.clone()
+    tl = K.backward_prep(ts, a, x, z, e1, c, tau32, dtt)
+    tc = K.backward_prep(ts, a, x, z, e2, c, tau32, dtt, n_spikes=counts)
+    torch.cuda.synchronize()
+    assert torch.equal(tl.nvalid, tc.nvalid)
+    assert torch.equal(e1, e2)
+    nv = tl.nvalid.cpu().numpy()
+    Kp = ts.shape[2]
+    valid = np.arange(Kp + 1)[None, None, :] < nv[:, :, None]
+    a_tab, b_tab = tl.tables.cpu().numpy(), tc.tables.cpu().numpy()
+    assert np.array_equal(a_tab[valid].view(np.uint32), b_tab[valid].view(np.uint32))
