@@ -295,3 +295,31 @@ def test_counted_prep_matches_layer_prep_bit_for_bit(cuda, case):
     valid = np.arange(Kp + 1)[None, None, :] < nv[:, :, None]
     a_tab, b_tab = tl.tables.cpu().numpy(), tc.tables.cpu().numpy()
     assert np.array_equal(a_tab[valid].view(np.uint32), b_tab[valid].view(np.uint32))
+
+
+@pytest.mark.parametrize("n_post", [60, 200])
+def test_wide_bucketed_gradient_matches_full_event_list(cuda, n_post):
+    """The batch-summed and per-sample weight gradient of wide layers over bucketed events (samples of a
+    group pipelined: the next sample's bucket range, cursor entries and first event chunk loaded ahead)
+    is bit-identical to the one over the full event list: buckets with more events than one chunk (128),
+    empty buckets, a silent sample, groups that do not divide the batch."""
+    import dataclasses
+    t, n_in = multi_spike_input(13, 150, 8, 0.1, seed=17, p_silent=0.3)
+    t[4] = np.inf  # a silent sample
+    rng = np.random.default_rng(17)
+    W = (rng.uniform(-0.5, 1.0, (n_post, 150)) * 1.2).astype(np.float32)
+    tau_s, th = 0.1, 0.5
+    ev = K.sort_events(cu(t), tau_s, 2 * tau_s)
+    offs = ev.bucket_offsets.cpu().numpy()
+    assert (np.diff(offs, axis=1) > 128).any(), "some bucket should need several chunks"
+    wt = K.transpose_weights(cu(W))
+    n, a, x, ts, z = K.lif_forward_fc(ev, wt, n_post, 12, tau_s, th, th)
+    assert int(n.sum()) > 100
+    err = cu(rng.normal(size=ts.shape).astype(np.float32))
+    tau32, c, dtt = K.lif_constants(tau_s, th, th)
+    tab = K.backward_prep(ts, a, x, z, err, c, tau32, dtt)
+    plain = dataclasses.replace(ev, bucketed=None, bucket_offsets=None)
+    for per_sample, group in ((True, None), (False, 2), (False, 5), (False, 13)):
+        g_b = K.weights_gradient(ev, ts, tab, 150, per_sample=per_sample, group=group)
+        g_full = K.weights_gradient(plain, ts, tab, 150, per_sample=per_sample, group=group)
+        assert torch.equal(g_b, g_full), f"bucketed vs full event list (per_sample={per_sample}, group={group})"
