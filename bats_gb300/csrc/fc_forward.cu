@@ -125,11 +125,17 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
         }
         stream_release(sm, k);
     }
-    if (active) {
-        n_spikes[(long long)s * n_post + i] = n;
-        for (int q = n; q < k_post; ++q) {
-            to[q] = BATS_INF;
-            zo[q] = BATS_INF;
+    if (active) n_spikes[(long long)s * n_post + i] = n;
+    // +inf past each neuron's spikes. The warp's 32 neurons own contiguous rows of k_post slots, so the
+    // warp fills them row by row with the lanes along the row (contiguous stores), not lane by neuron.
+    const int i0 = tile0 + warp * 32;
+    const int rows = max(0, min(32, n_post - i0));
+    const long long wbase = ((long long)s * n_post + i0) * k_post;
+    for (int r = 0; r < rows; ++r) {
+        const int nr = __shfl_sync(0xffffffffu, n, r);
+        for (int q = nr + lane; q < k_post; q += 32) {
+            t_out[wbase + (long long)r * k_post + q] = BATS_INF;
+            z_out[wbase + (long long)r * k_post + q] = BATS_INF;
         }
     }
 }
