@@ -405,9 +405,12 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
                          long long ev_cap, const float* __restrict__ post_t, const float2* __restrict__ tab,
                          const int* __restrict__ nvalid, int n_post, int k_post, int n_pre, int batch, int group,
                          float* __restrict__ out) {
+    constexpr int WARPS = TILE / 32;
     __shared__ float G[JC][TILE + 1];
     __shared__ Event sev[BWD_CHUNK];
-    const int tid = threadIdx.x;
+    __shared__ int s_beg[32], s_end_[32];
+    __shared__ unsigned s_spk[WARPS];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int i = blockIdx.x * TILE + tid;
     const bool active = i < n_post;
     const int bucket = blockIdx.y;
@@ -417,57 +420,78 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
 
     const int s_begin = g * group;
     const int s_end = min(batch, s_begin + group);
-    for (int s = s_begin; s < s_end; ++s) {
-        const int* bo = boff + (long long)s * (n_buckets + 1);
-        const int beg = bo[bucket], end = bo[bucket + 1];
-        if (beg >= end) continue;
-        const long long pn = (long long)s * n_post + (active ? i : 0);
-        const int n = active ? nvalid[pn] : 0;
-        const float* tp = post_t + pn * k_post;
-        const float2* tb = tab + pn * (k_post + 1);
-        PostCursor cur;
-        cur.init(tp, tb, n);
-        const Event* evs = ev_b + (long long)s * ev_cap;
-        for (int m0 = beg; m0 < end; m0 += BWD_CHUNK) {
-            const int cnt = min(BWD_CHUNK, end - m0);
-            __syncthreads();
-            for (int q = tid; q < cnt; q += TILE) sev[q] = evs[m0 + q];
-            __syncthreads();
-            if (n == 0) continue;
-            // Four events at a time: their terms are formed in event order (the cursor only moves
-            // forward), then the four shared-memory updates are issued with all loads first when the
-            // four pre neurons differ (the usual case), so that they do not wait on one another. Every
-            // G[j][i] still receives its terms in event order.
-            int m = 0;
-            for (; m + 4 <= cnt; m += 4) {
-                float v[4];
-                int jj[4];
+    for (int s0 = s_begin; s0 < s_end; s0 += 32) {
+        // Window of up to 32 samples: their bucket ranges, and for each whether any neuron of the tile
+        // spiked, are read at once (independent loads), so that samples with nothing to do cost nothing.
+        const int ws = min(32, s_end - s0);
+        __syncthreads();  // the previous window's flags have been read
+        if (tid < ws) {
+            const int* bo = boff + (long long)(s0 + tid) * (n_buckets + 1);
+            s_beg[tid] = bo[bucket];
+            s_end_[tid] = bo[bucket + 1];
+        }
+        unsigned spk = 0u;  // bit q: some neuron of this warp spiked in sample s0 + q
+        for (int q = 0; q < ws; ++q) {
+            const int nq = active ? nvalid[(long long)(s0 + q) * n_post + i] : 0;
+            spk |= __ballot_sync(0xffffffffu, nq > 0) ? (1u << q) : 0u;
+        }
+        if (lane == 0) s_spk[warp] = spk;
+        __syncthreads();
+        unsigned any = 0u;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const Event e = sev[m + u];
+        for (int w = 0; w < WARPS; ++w) any |= s_spk[w];
+        for (int q = 0; q < ws; ++q) {
+            const int s = s0 + q;
+            const int beg = s_beg[q], end = s_end_[q];
+            if (beg >= end || !((any >> q) & 1u)) continue;
+            const long long pn = (long long)s * n_post + (active ? i : 0);
+            const int n = active ? nvalid[pn] : 0;
+            const float* tp = post_t + pn * k_post;
+            const float2* tb = tab + pn * (k_post + 1);
+            PostCursor cur;
+            cur.init(tp, tb, n);
+            const Event* evs = ev_b + (long long)s * ev_cap;
+            for (int m0 = beg; m0 < end; m0 += BWD_CHUNK) {
+                const int cnt = min(BWD_CHUNK, end - m0);
+                __syncthreads();
+                for (int r = tid; r < cnt; r += TILE) sev[r] = evs[m0 + r];
+                __syncthreads();
+                if (n == 0) continue;
+                // Four events at a time: their terms are formed in event order (the cursor only moves
+                // forward), then the four shared-memory updates are issued with all loads first when the
+                // four pre neurons differ (the usual case), so that they do not wait on one another. Every
+                // G[j][i] still receives its terms in event order.
+                int m = 0;
+                for (; m + 4 <= cnt; m += 4) {
+                    float v[4];
+                    int jj[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const Event e = sev[m + u];
+                        cur.advance_past(e.t);
+                        jj[u] = e.j - J0;
+                        v[u] = cur.valid() ? fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y)) : 0.0f;
+                    }
+                    const bool distinct = jj[0] != jj[1] && jj[0] != jj[2] && jj[0] != jj[3] && jj[1] != jj[2] &&
+                                          jj[1] != jj[3] && jj[2] != jj[3];
+                    if (distinct) {
+                        float g[4];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) g[u] = G[jj[u]][tid];
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            if (v[u] != 0.0f) G[jj[u]][tid] = g[u] + v[u];
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u)
+                            if (v[u] != 0.0f) G[jj[u]][tid] += v[u];
+                    }
+                }
+                for (; m < cnt; ++m) {
+                    const Event e = sev[m];
                     cur.advance_past(e.t);
-                    jj[u] = e.j - J0;
-                    v[u] = cur.valid() ? fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y)) : 0.0f;
+                    if (cur.valid()) G[e.j - J0][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
                 }
-                const bool distinct = jj[0] != jj[1] && jj[0] != jj[2] && jj[0] != jj[3] && jj[1] != jj[2] &&
-                                      jj[1] != jj[3] && jj[2] != jj[3];
-                if (distinct) {
-                    float g[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) g[u] = G[jj[u]][tid];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (v[u] != 0.0f) G[jj[u]][tid] = g[u] + v[u];
-                } else {
-#pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (v[u] != 0.0f) G[jj[u]][tid] += v[u];
-                }
-            }
-            for (; m < cnt; ++m) {
-                const Event e = sev[m];
-                cur.advance_past(e.t);
-                if (cur.valid()) G[e.j - J0][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
             }
         }
     }
