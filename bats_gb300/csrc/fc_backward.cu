@@ -509,8 +509,20 @@ __global__ void reduce_groups_kernel(const float* __restrict__ partial, long lon
                                      float divisor, float* __restrict__ out) {
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < per_group;
          q += (long long)gridDim.x * blockDim.x) {
+        // Loads four partials ahead of the (in-order) additions, so that they are in flight together.
         float acc = 0.0f;
-        for (int g = 0; g < groups; ++g) acc += partial[(long long)g * per_group + q];
+        int g = 0;
+        for (; g + 4 <= groups; g += 4) {
+            const float p0 = partial[(long long)g * per_group + q];
+            const float p1 = partial[(long long)(g + 1) * per_group + q];
+            const float p2 = partial[(long long)(g + 2) * per_group + q];
+            const float p3 = partial[(long long)(g + 3) * per_group + q];
+            acc += p0;
+            acc += p1;
+            acc += p2;
+            acc += p3;
+        }
+        for (; g < groups; ++g) acc += partial[(long long)g * per_group + q];
         out[q] = acc / divisor;
     }
 }
@@ -886,7 +898,8 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
         tiles = (n_post + 127) / 128;
     }
     if (rc != BATS_OK) return rc;
-    dim3 g2((unsigned)std::min<long long>((ev_cap + 255) / 256, 64), batch);
+    // A few CTAs per sample, striding over its events (most samples have far fewer events than slots).
+    dim3 g2((unsigned)std::min<long long>((ev_cap + 255) / 256, 4), batch);
     bats::pre_err_scatter_kernel<<<g2, 256, 0, stream>>>(part, reinterpret_cast<const bats::Event*>(events), ev_slot,
                                                           ev_count, ev_cap, tiles, slots, tau_s, tau, pre_errors);
     BATS_CUDA(cudaGetLastError());
