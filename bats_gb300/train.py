@@ -218,7 +218,7 @@ class FCTrainStep:
                               force=force)
             self.fwd_algo[li] = algos[best]
             cands = {}
-            for parts in ((4, 8, 16, 32) if spec.n_neurons > 32 else (16, 32, 64, 128, 256)):
+            for parts in ((4, 8, 16, 32, 64, 128) if spec.n_neurons > 32 else (16, 32, 64, 128, 256)):
                 g = max(2, -(-B // parts))
                 if K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev, g) <= wsb:
                     cands[str(g)] = g
