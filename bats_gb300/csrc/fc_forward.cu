@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(TILE + 32)
 lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                       const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
                       int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
-                      float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status) {
+                      float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status, int pad) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using Smem = StreamSmem<TILE, SEV, STAGES>;
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
@@ -129,7 +129,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
     // +inf past each neuron's spikes. The warp's 32 neurons own contiguous rows of k_post slots, so the
     // warp fills them row by row with the lanes along the row (contiguous stores), not lane by neuron.
     const int i0 = tile0 + warp * 32;
-    const int rows = max(0, min(32, n_post - i0));
+    const int rows = pad ? max(0, min(32, n_post - i0)) : 0;
     const long long wbase = ((long long)s * n_post + i0) * k_post;
     for (int r = 0; r < rows; ++r) {
         const int nr = __shfl_sync(0xffffffffu, n, r);
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(WARPS * 32)
 lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                             const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
                             int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
-                            float* __restrict__ t_out, float* __restrict__ z_out) {
+                            float* __restrict__ t_out, float* __restrict__ z_out, int pad) {
     __shared__ float4 blk[WARPS][32];  // (w, es, e, -) of the block's events
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int s = blockIdx.y;
@@ -256,7 +256,7 @@ lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict_
         __syncwarp();
     }
     if (lane == 0) n_spikes[(long long)s * n_post + i] = n;
-    for (int q = n + lane; q < k_post; q += 32) {
+    for (int q = n + lane; pad && q < k_post; q += 32) {
         to[q] = BATS_INF;
         zo[q] = BATS_INF;
     }
@@ -265,11 +265,11 @@ lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict_
 template <int WARPS>
 static int launch_forward_lanes(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld,
                                 int batch, int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a,
-                                float* x, float* times, float* post_exp_tau, cudaStream_t stream) {
+                                float* x, float* times, float* post_exp_tau, int pad, cudaStream_t stream) {
     dim3 grid((n_post + WARPS - 1) / WARPS, batch);
     lif_fc_forward_lanes_kernel<WARPS><<<grid, WARPS * 32, 0, stream>>>(
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
-        post_exp_tau);
+        post_exp_tau, pad);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -277,13 +277,13 @@ static int launch_forward_lanes(const void* events, const int* ev_count, long lo
 template <int TILE, int SEV, int STAGES>
 static int launch_forward(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld, int batch,
                           int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a, float* x,
-                          float* times, float* post_exp_tau, int* status, cudaStream_t stream) {
+                          float* times, float* post_exp_tau, int* status, int pad, cudaStream_t stream) {
     const size_t smem = sizeof(StreamSmem<TILE, SEV, STAGES>);
     BATS_CUDA((cudaError_t)max_dynamic_smem_set((const void*)lif_fc_forward_kernel<TILE, SEV, STAGES>, (int)smem));
     dim3 grid((n_post + TILE - 1) / TILE, batch);
     lif_fc_forward_kernel<TILE, SEV, STAGES><<<grid, TILE + 32, smem, stream>>>(
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
-        post_exp_tau, status);
+        post_exp_tau, status, pad);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -309,6 +309,8 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
                            int algo, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0 && ld >= n_post && ld % 4 == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc: bad shape (ld must be >= n_post and a multiple of 4)");
+    const int pad = (algo & BATS_FWD_NO_PAD) ? 0 : 1;
+    algo &= ~BATS_FWD_NO_PAD;
     BATS_REQUIRE(algo >= BATS_FWD_AUTO && algo <= BATS_FWD_TILE64, BATS_ERR_BAD_SHAPE, "lif_forward_fc: unknown algo");
     if (batch == 0 || n_post == 0) return BATS_OK;
     BATS_REQUIRE(events && ev_count && weights_t && n_spikes && a && x && times && post_exp_tau, BATS_ERR_NULL,
@@ -319,22 +321,22 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
     if (algo == BATS_FWD_AUTO) algo = bats_lif_forward_fc_default_algo(batch, n_post, (int)(ev_cap < (1LL << 30) ? ev_cap : (1LL << 30)));
     if (algo == BATS_FWD_LANES)
         return bats::launch_forward_lanes<4>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
-                                             n_spikes, a, x, times, post_exp_tau, stream);
+                                             n_spikes, a, x, times, post_exp_tau, pad, stream);
     int* status = nullptr;
     BATS_CUDA((cudaError_t)bats::device_status(&status));
     if (algo == BATS_FWD_TILE64)
         return bats::launch_forward<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
-                                              n_spikes, a, x, times, post_exp_tau, status, stream);
+                                              n_spikes, a, x, times, post_exp_tau, status, pad, stream);
     if (n_post <= 32)
         return bats::launch_forward<32, 16, 8>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
-                                               n_spikes, a, x, times, post_exp_tau, status, stream);
+                                               n_spikes, a, x, times, post_exp_tau, status, pad, stream);
     if (n_post <= 64)
         return bats::launch_forward<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
-                                              n_spikes, a, x, times, post_exp_tau, status, stream);
+                                              n_spikes, a, x, times, post_exp_tau, status, pad, stream);
     // 8-event stages: half the shared memory of 16-event stages, so 7 CTAs (28 consumer warps) fit on an SM
     // instead of 4, and a replay after a possible crossing covers fewer events.
     return bats::launch_forward<128, 8, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
-                                          n_spikes, a, x, times, post_exp_tau, status, stream);
+                                          n_spikes, a, x, times, post_exp_tau, status, pad, stream);
 }
 
 extern "C" int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap) {

@@ -45,7 +45,8 @@ extern "C" int bats_serve_fc_batch(const int* h_indices, const float* h_times, c
         if (rc != BATS_OK) return rc;
         rc = bats_lif_forward_fc_algo(L.events, L.ev_count, (long long)L.n_pre * L.k_pre, L.weights_t, L.ld, batch,
                                       L.n_post, L.k_post, L.c, L.delta_theta_tau, L.tau, L.max_simulation,
-                                      L.n_spikes, L.a, L.x, L.times, L.post_exp_tau, L.algo, stream);
+                                      L.n_spikes, L.a, L.x, L.times, L.post_exp_tau,
+                                      l + 1 < n_layers ? (L.algo | BATS_FWD_NO_PAD) : L.algo, stream);
         if (rc != BATS_OK) return rc;
         pre = L.times;
     }

@@ -156,6 +156,7 @@ def get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron):
 
 
 FWD_AUTO, FWD_TILE, FWD_LANES, FWD_TILE64 = 0, 1, 2, 3
+FWD_NO_PAD = 0x100  # OR-ed into the algo: no +inf past the spike counts (outputs read only below them)
 
 
 def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: float, theta: float,

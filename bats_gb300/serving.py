@@ -247,7 +247,8 @@ class InferenceServer:
             if only is None or only == li:
                 call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.wt[li]),
                      self.wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt), float(tau32),
-                     float(np.float32(self.max_sim)), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), int(algos[li]), s)
+                     float(np.float32(self.max_sim)), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z),
+                     int(algos[li]) | (K.FWD_NO_PAD if li + 1 < len(self.specs) else 0), s)
             pre, pre_n = t, n
 
     @staticmethod

@@ -5,7 +5,8 @@ the exact backward with batch-mean weight gradients, and Adam updates of the wei
 transposed copies, with no host synchronisation and no allocation after construction, so that the
 whole step can be captured once as a CUDA graph and replayed (capture()). It computes the same
 arithmetic as the layer-by-layer API (Network + LIFLayer + SpikeCountClassLoss + AdamOptimizer +
-the caller's batch mean), only without materialising the per-sample gradients.
+the caller's batch mean), only without materialising the per-sample gradients. The spike trains of
+its hidden layers (self.out) hold valid times only below their spike counts (no +inf padding).
 """
 from __future__ import annotations
 
@@ -95,6 +96,14 @@ class FCTrainStep:
         self.launches = self._build_launches()
         self.launches_per_step = self._count_launches()
 
+    def _pad_flag(self, li: int) -> int:
+        """Hidden layers skip the +inf padding of their spike trains: everything that reads them (the next
+        layer's counted sort, the counted prep, the gradient and pre-error kernels) stays below the spike
+        counts. The output layer (read by the loss) and layers with K > 32 (whose prep scans the times)
+        keep it."""
+        last = li + 1 == len(self.specs)
+        return 0 if last or self.specs[li].max_n_spike > 32 else K.FWD_NO_PAD
+
     # -- the step as a fixed list of launches --------------------------------------------------------
     def _build_launches(self):
         """(name, fn(stream)) for every entry-point call of one step, in order. All pointers are fixed."""
@@ -121,7 +130,8 @@ class FCTrainStep:
             L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
                       call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
                            self.Wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt),
-                           float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o), self.fwd_algo[li],
+                           float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o),
+                           self.fwd_algo[li] | self._pad_flag(li),
                            s)))
             pre_times, pre_counts = t, n
         n_out = self.out[-1][0]

@@ -104,6 +104,10 @@ int bats_intensity_to_spike_times(const unsigned char* pixels, int batch, int n_
 #define BATS_FWD_TILE 1
 #define BATS_FWD_LANES 2
 #define BATS_FWD_TILE64 3 /* the tile kernel with 64-neuron tiles whatever N_post (more CTAs, less reuse) */
+/* OR-ed into `algo`: the slots past each neuron's spikes in times/post_exp_tau are left as they are instead of
+ * set to +inf, for outputs read only below the spike counts (bats_sort_events_counted,
+ * bats_backward_prep_counted, bats_weights_gradient, bats_pre_errors): the hidden layers of a train step. */
+#define BATS_FWD_NO_PAD 0x100
 int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap);
 int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
                              int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,

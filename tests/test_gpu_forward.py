@@ -261,3 +261,27 @@ def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
     if case == "long_narrow":
         ref = run_ref(t, n_in, W, *args)
         check_against(lanes, ref, None, what="lanes vs reference kernels")
+
+
+@pytest.mark.parametrize("algo", [K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64])
+def test_no_pad_flag_leaves_slots_past_counts(cuda, algo):
+    """BATS_FWD_NO_PAD: counts and every value below them are those of the padded forward, and the slots
+    past the counts keep what the buffers held (here a sentinel)."""
+    t, n_in = mnist_like_input(8, seed=4)
+    rng = np.random.default_rng(4)
+    W = rng.uniform(-1, 1, (200, 784)).astype(np.float32)
+    ev = K.sort_events(torch.tensor(t, device="cuda"), np.float32(0.13), np.float32(0.26))
+    wt = K.transpose_weights(torch.tensor(W, device="cuda"))
+    ref = K.lif_forward_fc(ev, wt, 200, 30, 0.13, 0.2, 0.2, 0.2, algo=algo)
+    outs = (torch.full((8, 200), -7, dtype=torch.int32, device="cuda"),
+            *(torch.full((8, 200, 30), 12345.0, device="cuda") for _ in range(4)))
+    got = K.lif_forward_fc(ev, wt, 200, 30, 0.13, 0.2, 0.2, 0.2, outs=outs, algo=algo | K.FWD_NO_PAD)
+    torch.cuda.synchronize()
+    n = ref[0].cpu().numpy()
+    assert np.array_equal(n, got[0].cpu().numpy())
+    assert n.sum() > 0 and (n < 30).any()
+    valid = leading_mask(n, 30)
+    for r, g in zip(ref[1:], got[1:]):
+        r, g = r.cpu().numpy(), g.cpu().numpy()
+        assert np.array_equal(r[valid].view(np.uint32), g[valid].view(np.uint32))
+        assert (g[~valid] == 12345.0).all()
