@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(TILE)
 bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__ boff, int n_buckets,
                          long long ev_cap, const float* __restrict__ post_t, const float2* __restrict__ tab,
                          const int* __restrict__ nvalid, int n_post, int k_post, int n_pre, int batch, int group,
-                         float* __restrict__ out) {
+                         float* __restrict__ out, int* __restrict__ flags) {
     constexpr int WARPS = TILE / 32;
     __shared__ float G[JC][TILE + 1];
     __shared__ Event sev[BWD_CHUNK];
@@ -420,6 +420,7 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
 
     const int s_begin = g * group;
     const int s_end = min(batch, s_begin + group);
+    bool worked = false;  // some sample had events in the bucket and a spike in the tile (CTA-uniform)
     for (int s0 = s_begin; s0 < s_end; s0 += 32) {
         // Window of up to 32 samples: their bucket ranges, and for each whether any neuron of the tile
         // spiked, are read at once (independent loads), so that samples with nothing to do cost nothing.
@@ -444,6 +445,7 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
             const int s = s0 + q;
             const int beg = s_beg[q], end = s_end_[q];
             if (beg >= end || !((any >> q) & 1u)) continue;
+            worked = true;
             const long long pn = (long long)s * n_post + (active ? i : 0);
             const int n = active ? nvalid[pn] : 0;
             const float* tp = post_t + pn * k_post;
@@ -495,6 +497,12 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
             }
         }
     }
+    if (flags) {
+        // A partial that is all zero is not written; the reduction skips it (adding +0 changes nothing:
+        // a partial is a sum of nonzero terms, never -0).
+        if (tid == 0) flags[((long long)g * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = worked ? 1 : 0;
+        if (!worked) return;
+    }
     __syncthreads();
     const long long obase = (long long)g * n_post * n_pre;
     for (int q = tid; q < TILE * JC; q += TILE) {
@@ -505,24 +513,36 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
 }
 
 // Sum of per-group partial gradients in a fixed order, divided by `divisor` (1 or the batch).
+// With `flags` (one per group, pre bucket and post tile of the gradient kernel's grid; 0 = that partial tile
+// is all zero and was not written), only the written partials are added.
 __global__ void reduce_groups_kernel(const float* __restrict__ partial, long long per_group, int groups,
-                                     float divisor, float* __restrict__ out) {
+                                     float divisor, float* __restrict__ out, const int* __restrict__ flags,
+                                     int n_pre, int tile, int jc, int tiles, int buckets) {
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < per_group;
          q += (long long)gridDim.x * blockDim.x) {
+        const int* fl = nullptr;
+        if (flags) {
+            const long long i = q / n_pre, j = q - i * n_pre;
+            fl = flags + (j / jc) * tiles + i / tile;
+        }
+        const long long fstride = (long long)tiles * buckets;
         // Loads four partials ahead of the (in-order) additions, so that they are in flight together.
         float acc = 0.0f;
         int g = 0;
         for (; g + 4 <= groups; g += 4) {
-            const float p0 = partial[(long long)g * per_group + q];
-            const float p1 = partial[(long long)(g + 1) * per_group + q];
-            const float p2 = partial[(long long)(g + 2) * per_group + q];
-            const float p3 = partial[(long long)(g + 3) * per_group + q];
-            acc += p0;
-            acc += p1;
-            acc += p2;
-            acc += p3;
+            const bool f0 = !fl || fl[g * fstride], f1 = !fl || fl[(g + 1) * fstride];
+            const bool f2 = !fl || fl[(g + 2) * fstride], f3 = !fl || fl[(g + 3) * fstride];
+            const float p0 = f0 ? partial[(long long)g * per_group + q] : 0.0f;
+            const float p1 = f1 ? partial[(long long)(g + 1) * per_group + q] : 0.0f;
+            const float p2 = f2 ? partial[(long long)(g + 2) * per_group + q] : 0.0f;
+            const float p3 = f3 ? partial[(long long)(g + 3) * per_group + q] : 0.0f;
+            if (f0) acc += p0;
+            if (f1) acc += p1;
+            if (f2) acc += p2;
+            if (f3) acc += p3;
         }
-        for (; g < groups; ++g) acc += partial[(long long)g * per_group + q];
+        for (; g < groups; ++g)
+            if (!fl || fl[g * fstride]) acc += partial[(long long)g * per_group + q];
         out[q] = acc / divisor;
     }
 }
@@ -767,21 +787,31 @@ extern "C" int bats_backward_prep_counted(const float* post_times, const int* n_
     return BATS_OK;
 }
 
+static int grad_tile_for(int n_post) { return n_post <= 32 ? 32 : (n_post <= 64 ? 64 : 128); }
+
+// Partials (groups, n_post, n_pre) floats, then (256-byte aligned) one int flag per partial tile.
+static size_t grad_partials_bytes(long long groups, int n_post, int n_pre) {
+    return ((size_t)groups * n_post * n_pre * sizeof(float) + 255) & ~(size_t)255;
+}
+
 extern "C" size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, int n_pre, int group) {
     if (group <= 1 || group >= batch) return 0;
     const long long groups = (batch + group - 1) / group;
-    return (size_t)groups * n_post * n_pre * sizeof(float);
+    const int tile = grad_tile_for(n_post);
+    const long long tiles = (n_post + tile - 1) / tile, buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
+    return grad_partials_bytes(groups, n_post, n_pre) + (size_t)groups * tiles * buckets * sizeof(int);
 }
 
 template <int TILE>
 static void launch_grad(const void* events, const int* ev_count, const void* ev_b, const int* boff, int n_buckets,
                         long long ev_cap, const float* post_times, const void* tables, const int* nvalid, int batch,
-                        int n_post, int k_post, int n_pre, int group, int groups, float* out, cudaStream_t stream) {
+                        int n_post, int k_post, int n_pre, int group, int groups, float* out, int* flags,
+                        cudaStream_t stream) {
     dim3 grid((n_post + TILE - 1) / TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
     if (ev_b) {
         bats::bwd_grad_bucketed_kernel<TILE, GRAD_JC><<<grid, TILE, 0, stream>>>(
             reinterpret_cast<const bats::Event*>(ev_b), boff, n_buckets, ev_cap, post_times,
-            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out);
+            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out, flags);
     } else {
         bats::bwd_grad_kernel<TILE, GRAD_JC><<<grid, TILE, 0, stream>>>(
             reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
@@ -802,25 +832,30 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
     const int n_buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
     const int groups = group == 1 ? batch : (batch + group - 1) / group;
     float* part = grad;
+    int* flags = nullptr;  // all-zero partial tiles are skipped (bucketed kernel, partials in the workspace)
     if (group > 1 && groups > 1) {
         BATS_REQUIRE(workspace && workspace_bytes >= bats_weights_gradient_workspace_bytes(batch, n_post, n_pre, group),
                      BATS_ERR_WORKSPACE, "weights_gradient: workspace too small");
         part = reinterpret_cast<float*>(workspace);
+        if (events_bucketed)
+            flags = reinterpret_cast<int*>(static_cast<char*>(workspace) + grad_partials_bytes(groups, n_post, n_pre));
     }
-    if (n_post <= 32)
+    const int tile = grad_tile_for(n_post);
+    if (tile == 32)
         launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables, nvalid,
-                        batch, n_post, k_post, n_pre, group, groups, part, stream);
-    else if (n_post <= 64)
+                        batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
+    else if (tile == 64)
         launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables, nvalid,
-                        batch, n_post, k_post, n_pre, group, groups, part, stream);
+                        batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
     else
         launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables,
-                         nvalid, batch, n_post, k_post, n_pre, group, groups, part, stream);
+                         nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
     BATS_CUDA(cudaGetLastError());
     if (group == 1) return BATS_OK;  // per-sample gradient (B, N_post, N_pre)
     const long long per = (long long)n_post * n_pre;
     const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
-    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, mean ? (float)batch : 1.0f, grad);
+    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, mean ? (float)batch : 1.0f, grad, flags,
+                                                       n_pre, tile, GRAD_JC, (n_post + tile - 1) / tile, n_buckets);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -969,7 +1004,8 @@ extern "C" int bats_weights_gradient_mean_noalloc(const void* events, const int*
         reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, part);
     BATS_CUDA(cudaGetLastError());
     const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
-    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, (float)batch, grad);
+    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, (float)batch, grad, nullptr, n_pre, 1, 1, 1,
+                                                       1);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

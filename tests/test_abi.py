@@ -70,6 +70,8 @@ def test_workspace_queries(lib):
     L = _lib.load()
     assert L.bats_sort_events_workspace_bytes(4, 10, 3) == 0  # fits in shared memory
     assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 4 * 30000 * 4
-    assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == 16 * 800 * 784 * 4
+    # 16 partial gradients, 256-byte aligned, then one flag per (partial, pre bucket of 64, post tile of 128)
+    parts = (16 * 800 * 784 * 4 + 255) // 256 * 256
+    assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == parts + 16 * 13 * 7 * 4
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 1) == 0
     assert L.bats_pre_errors_workspace_bytes(2, 100, 300) == 2 * 100 * 3 * 2 * 4
