@@ -122,6 +122,41 @@ def test_sort_events(cuda):
         np.testing.assert_allclose(e[s, :cnt[s], 2], np.exp(et / np.float32(0.1)), rtol=2e-6)
 
 
+@pytest.mark.parametrize("k", [1, 3])
+def test_sort_events_small_samples_with_ties(cuda, k):
+    """Small samples with many tied times: events, slots and counts equal the oracle's stable sort (ties
+    in slot order), and the bucketed copy is the time order grouped stably by pre-neuron bucket, with its
+    offsets; samples of 0, 1, 40, 150, 256 and 257 events."""
+    rng = np.random.default_rng(31)
+    B, N = 6, 300
+    t = np.full((B, N, k), np.inf, dtype=np.float32)
+    want = [150, 256, 257, 0, 1, 40]
+    for s, m in enumerate(want):
+        slots = rng.choice(N * k, size=m, replace=False)
+        vals = (rng.integers(0, 60, m) * 0.001).astype(np.float32)  # many ties
+        t[s].reshape(-1)[slots] = vals
+    ev = K.sort_events(torch.tensor(t, device="cuda"), 0.1, 0.2, bucket_width=64)
+    torch.cuda.synchronize()
+    e = ev.events.cpu().numpy()
+    sl = ev.slots.cpu().numpy()
+    cnt = ev.counts.cpu().numpy()
+    be = ev.bucketed.cpu().numpy()
+    bo = ev.bucket_offsets.cpu().numpy()
+    assert cnt.tolist() == want
+    for s in range(B):
+        et, ej, es = R.sort_events(t[s:s + 1])[0]
+        c = cnt[s]
+        assert np.array_equal(sl[s, :c], es)
+        assert np.array_equal(e[s, :c, 0], et.astype(np.float32))
+        assert np.array_equal(e[s, :c, 1].view(np.int32), ej)
+        bucket = ej // 64
+        order = np.argsort(bucket, kind="stable")
+        assert np.array_equal(be[s, :c].view(np.uint32), e[s, :c][order].view(np.uint32))
+        nb = bo.shape[1] - 1
+        assert np.array_equal(bo[s, :nb], np.searchsorted(bucket[order], np.arange(nb), side="left"))
+        assert bo[s, nb] == c
+
+
 def test_sort_events_large_sample_uses_global_path(cuda):
     """More valid slots than the shared-memory sort holds (4096)."""
     rng = np.random.default_rng(4)
