@@ -74,6 +74,9 @@ class Autotuner:
         times = {}
         for name, fn in candidates.items():
             fn()  # warm-up (module load, caches)
+            # A short spin kernel ahead of the timed launches keeps the GPU busy while the host enqueues
+            # them, so that the events time the kernels and not the host's launch calls (short kernels).
+            torch.cuda._sleep(1_000_000)
             start = torch.cuda.Event(enable_timing=True)
             end = torch.cuda.Event(enable_timing=True)
             start.record(stream)

@@ -514,36 +514,36 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
 
 // Sum of per-group partial gradients in a fixed order, divided by `divisor` (1 or the batch).
 // With `flags` (one per group, pre bucket and post tile of the gradient kernel's grid; 0 = that partial tile
-// is all zero and was not written), only the written partials are added.
-__global__ void reduce_groups_kernel(const float* __restrict__ partial, long long per_group, int groups,
+// is all zero and was not written), only the written partials are added. Grid (column blocks, row blocks):
+// rows are post neurons, columns pre neurons, so the tile and bucket of an element need no division.
+__global__ void reduce_groups_kernel(const float* __restrict__ partial, int n_rows, int n_cols, int groups,
                                      float divisor, float* __restrict__ out, const int* __restrict__ flags,
-                                     int n_pre, int tile, int jc, int tiles, int buckets) {
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < per_group;
-         q += (long long)gridDim.x * blockDim.x) {
-        const int* fl = nullptr;
-        if (flags) {
-            const long long i = q / n_pre, j = q - i * n_pre;
-            fl = flags + (j / jc) * tiles + i / tile;
+                                     int tile_shift, int jc_shift, int tiles, int buckets) {
+    const long long per_group = (long long)n_rows * n_cols;
+    const long long fstride = (long long)tiles * buckets;
+    for (int i = blockIdx.y; i < n_rows; i += gridDim.y) {
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n_cols; j += gridDim.x * blockDim.x) {
+            const long long q = (long long)i * n_cols + j;
+            const int* fl = flags ? flags + (j >> jc_shift) * tiles + (i >> tile_shift) : nullptr;
+            // Loads four partials ahead of the (in-order) additions, so that they are in flight together.
+            float acc = 0.0f;
+            int g = 0;
+            for (; g + 4 <= groups; g += 4) {
+                const bool f0 = !fl || fl[g * fstride], f1 = !fl || fl[(g + 1) * fstride];
+                const bool f2 = !fl || fl[(g + 2) * fstride], f3 = !fl || fl[(g + 3) * fstride];
+                const float p0 = f0 ? partial[(long long)g * per_group + q] : 0.0f;
+                const float p1 = f1 ? partial[(long long)(g + 1) * per_group + q] : 0.0f;
+                const float p2 = f2 ? partial[(long long)(g + 2) * per_group + q] : 0.0f;
+                const float p3 = f3 ? partial[(long long)(g + 3) * per_group + q] : 0.0f;
+                if (f0) acc += p0;
+                if (f1) acc += p1;
+                if (f2) acc += p2;
+                if (f3) acc += p3;
+            }
+            for (; g < groups; ++g)
+                if (!fl || fl[g * fstride]) acc += partial[(long long)g * per_group + q];
+            out[q] = acc / divisor;
         }
-        const long long fstride = (long long)tiles * buckets;
-        // Loads four partials ahead of the (in-order) additions, so that they are in flight together.
-        float acc = 0.0f;
-        int g = 0;
-        for (; g + 4 <= groups; g += 4) {
-            const bool f0 = !fl || fl[g * fstride], f1 = !fl || fl[(g + 1) * fstride];
-            const bool f2 = !fl || fl[(g + 2) * fstride], f3 = !fl || fl[(g + 3) * fstride];
-            const float p0 = f0 ? partial[(long long)g * per_group + q] : 0.0f;
-            const float p1 = f1 ? partial[(long long)(g + 1) * per_group + q] : 0.0f;
-            const float p2 = f2 ? partial[(long long)(g + 2) * per_group + q] : 0.0f;
-            const float p3 = f3 ? partial[(long long)(g + 3) * per_group + q] : 0.0f;
-            if (f0) acc += p0;
-            if (f1) acc += p1;
-            if (f2) acc += p2;
-            if (f3) acc += p3;
-        }
-        for (; g < groups; ++g)
-            if (!fl || fl[g * fstride]) acc += partial[(long long)g * per_group + q];
-        out[q] = acc / divisor;
     }
 }
 
@@ -789,6 +789,18 @@ extern "C" int bats_backward_prep_counted(const float* post_times, const int* n_
 
 static int grad_tile_for(int n_post) { return n_post <= 32 ? 32 : (n_post <= 64 ? 64 : 128); }
 
+static int log2_pow2(int v) { return 31 - __builtin_clz((unsigned)v); }
+
+// Sum of the group partials (groups, n_post, n_pre) into out, ~8 CTAs of 256 threads per SM.
+static void launch_reduce(const float* part, int n_post, int n_pre, int groups, float divisor, float* out,
+                          const int* flags, int tile, int tiles, int buckets, cudaStream_t stream) {
+    const int gx = (n_pre + 255) / 256;
+    const int gy = (int)std::min<long long>(n_post, std::max<long long>(1, 152LL * 8 / gx));
+    bats::reduce_groups_kernel<<<dim3(gx, gy), 256, 0, stream>>>(part, n_post, n_pre, groups, divisor, out, flags,
+                                                                 log2_pow2(tile), log2_pow2(GRAD_JC), tiles,
+                                                                 buckets);
+}
+
 // Partials (groups, n_post, n_pre) floats, then (256-byte aligned) one int flag per partial tile.
 static size_t grad_partials_bytes(long long groups, int n_post, int n_pre) {
     return ((size_t)groups * n_post * n_pre * sizeof(float) + 255) & ~(size_t)255;
@@ -852,10 +864,8 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
                          nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
     BATS_CUDA(cudaGetLastError());
     if (group == 1) return BATS_OK;  // per-sample gradient (B, N_post, N_pre)
-    const long long per = (long long)n_post * n_pre;
-    const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
-    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, mean ? (float)batch : 1.0f, grad, flags,
-                                                       n_pre, tile, GRAD_JC, (n_post + tile - 1) / tile, n_buckets);
+    launch_reduce(part, n_post, n_pre, groups, mean ? (float)batch : 1.0f, grad, flags, tile,
+                  (n_post + tile - 1) / tile, n_buckets, stream);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -1003,9 +1013,7 @@ extern "C" int bats_weights_gradient_mean_noalloc(const void* events, const int*
         reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
         reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, part);
     BATS_CUDA(cudaGetLastError());
-    const int rb = (int)std::min<long long>((per + 255) / 256, 152LL * 8);
-    bats::reduce_groups_kernel<<<rb, 256, 0, stream>>>(part, per, groups, (float)batch, grad, nullptr, n_pre, 1, 1, 1,
-                                                       1);
+    launch_reduce(part, n_post, n_pre, groups, (float)batch, grad, nullptr, GRAD_TILE, 1, 1, stream);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
