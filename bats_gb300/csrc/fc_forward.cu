@@ -212,14 +212,15 @@ lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict_
         // 1. sequential chain; lanes past the block's end carry w = 0, which leaves a and b unchanged.
         my[lane] = make_float4(w, e4.z, e4.w, 0.0f);
         __syncwarp();
-        float am = 0.0f, bm = 0.0f, ca = a, cb = b;
+        // Lane l stops after event l: its state is the chain's l-th prefix, with no select per step.
+        float am = a, bm = b;
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
             const float4 q = my[k];
-            ca = fmaf(q.x, q.y, ca);
-            cb = fmaf(q.x, q.z, cb);
-            am = (lane == k) ? ca : am;
-            bm = (lane == k) ? cb : bm;
+            if (k <= lane) {
+                am = fmaf(q.x, q.y, am);
+                bm = fmaf(q.x, q.z, bm);
+            }
         }
         // 2. provable no-crossing tests of all lanes at once.
         unsigned cand = __ballot_sync(0xffffffffu, in && !no_crossing<false>(am, bm, e4.w, e_nx, sk));
