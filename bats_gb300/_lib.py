@@ -37,6 +37,9 @@ SIGNATURES = {
     "bats_lif_forward_fc_default_algo": (c_int, [c_int, c_int, c_int]),
     "bats_lif_forward_fc_algo": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float,
                                          c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp]),
+    "bats_lif_forward_fc_queue_workspace_bytes": (c_size, [c_int]),
+    "bats_lif_forward_fc_queue": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float,
+                                          c_float, c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_size, c_vp]),
     "bats_intensity_to_spike_times": (c_int, [c_vp, c_int, c_int, ctypes.c_double, ctypes.c_double, c_vp, c_vp,
                                               c_vp]),
     "bats_nadam_step": (c_int, [c_vp, c_vp, c_vp, c_ll, c_float, c_float, c_float, c_float, ctypes.c_double,

@@ -16,6 +16,7 @@
 // test on each intermediate state; only if some event may cross does it replay the stage from its
 // saved state with the exact solver. The accumulation is the same FMA sequence either way, so the
 // results are those of the reference's one-event-at-a-time loop.
+#include <algorithm>
 #include <cmath>
 #include <limits>
 #include "common.cuh"
@@ -24,31 +25,18 @@
 
 namespace bats {
 
+// Consumer warps' part of one work item (sample s, post neurons tile0 .. tile0 + TILE - 1): thread = post
+// neuron. The item's event stages are stages k0 .. k0 + ceil(E / SEV) - 1 of the CTA's ring (k0 = 0 when the
+// CTA has one item). Returns false when a wait gave up (the CTA is aborting).
 template <int TILE, int SEV, int STAGES>
-__global__ void __launch_bounds__(TILE + 32)
-lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
-                      const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
-                      int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
-                      float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status, int pad) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    using Smem = StreamSmem<TILE, SEV, STAGES>;
-    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
-    constexpr int CONSUMER_WARPS = TILE / 32;
+__device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>& sm, int k0, int s, int tile0, int E,
+                                                  int n_post, int k_post, const SolveConst& sk,
+                                                  int* __restrict__ n_spikes, float* __restrict__ a_out,
+                                                  float* __restrict__ x_out, float* __restrict__ t_out,
+                                                  float* __restrict__ z_out, int* status, int pad) {
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
-    const int s = blockIdx.y;
-    const int tile0 = blockIdx.x * TILE;
-    const int E = ev_count[s];
     const int n_stages = (E + SEV - 1) / SEV;
-    const Event* evs = ev + (long long)s * ev_cap;
-    stream_init(sm, CONSUMER_WARPS);
-    __syncthreads();
-    if (warp == CONSUMER_WARPS) {
-        stream_produce(sm, evs, E, wt, ld, tile0, n_stages, lane, status);
-        return;
-    }
-
-    // ---- consumer warps: thread = post neuron ----
     const int i = tile0 + tid;
     const bool active = i < n_post;
     const long long obase = ((long long)s * n_post + (active ? i : 0)) * k_post;
@@ -60,8 +48,9 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
     int n = 0;
     bool done = !active;
     for (int k = 0; k < n_stages; ++k) {
-        const int slot = k % STAGES;
-        if (!stream_acquire(sm, k, status)) return;
+        const int kg = k0 + k;  // the stage's place in the CTA's ring
+        const int slot = kg % STAGES;
+        if (!stream_acquire(sm, kg, status)) return false;
         const int m0 = k * SEV;
         const int cnt = min(SEV, E - m0);
         const Event* se = sm.evs[slot];
@@ -123,7 +112,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
                 }
             }
         }
-        stream_release(sm, k);
+        stream_release(sm, kg);
     }
     if (active) n_spikes[(long long)s * n_post + i] = n;
     // +inf past each neuron's spikes. The warp's 32 neurons own contiguous rows of k_post slots, so the
@@ -138,6 +127,168 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
             z_out[wbase + (long long)r * k_post + q] = BATS_INF;
         }
     }
+    return true;
+}
+
+template <int TILE, int SEV, int STAGES>
+__global__ void __launch_bounds__(TILE + 32)
+lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
+                      const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
+                      int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
+                      float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status, int pad) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    using Smem = StreamSmem<TILE, SEV, STAGES>;
+    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+    constexpr int CONSUMER_WARPS = TILE / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int s = blockIdx.y;
+    const int tile0 = blockIdx.x * TILE;
+    const int E = ev_count[s];
+    const int n_stages = (E + SEV - 1) / SEV;
+    const Event* evs = ev + (long long)s * ev_cap;
+    stream_init(sm, CONSUMER_WARPS);
+    __syncthreads();
+    if (warp == CONSUMER_WARPS) {
+        stream_produce(sm, evs, E, wt, ld, tile0, n_stages, lane, status);
+        return;
+    }
+    forward_tile_item(sm, 0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out, x_out, t_out, z_out, status, pad);
+}
+
+// Persistent variant over a work queue, for batches whose samples carry very different numbers of events.
+// A work item is (sample, post-neuron tile); the items are numbered in the order of `order` (samples by
+// descending event count, from work_order_kernel), the tiles of a sample next to each other, and a grid of
+// as many CTAs as fit on the GPU at once takes them from a global counter (`head`, zero at launch) until
+// none is left: the longest samples start first and the short ones fill the end, instead of the block
+// scheduler's fixed index order leaving a long sample for last. The producer warp claims the next item
+// and starts streaming its stages while the consumers finish the current one (the ring's stage count runs
+// on across items), so no CTA start-up or pipeline fill sits between items. Items reach the consumers
+// through a two-slot mailbox with its own full/empty mbarriers. Each item computes exactly what the
+// one-item-per-CTA kernel computes for it, so results are bit-identical to lif_fc_forward_kernel's.
+struct WorkItem {
+    int s;      // sample, < 0: no work left
+    int tile0;  // first post neuron of the tile
+    int E;      // events of the sample
+    int unused;
+};
+struct ItemMailbox {
+    uint64_t full[2];   // the producer has written item[q] (one arrival)
+    uint64_t empty[2];  // every consumer warp has read item[q] (one arrival per warp)
+    WorkItem item[2];
+};
+
+template <typename Smem>
+__host__ __device__ constexpr size_t mailbox_offset() {
+    return (sizeof(Smem) + 15) / 16 * 16;
+}
+
+template <int TILE, int SEV, int STAGES>
+__global__ void __launch_bounds__(TILE + 32)
+lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
+                            const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
+                            int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
+                            float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status, int pad,
+                            const int* __restrict__ order, int* __restrict__ head, int n_tiles, int n_items) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    using Smem = StreamSmem<TILE, SEV, STAGES>;
+    Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
+    ItemMailbox& box = *reinterpret_cast<ItemMailbox*>(smem_raw + mailbox_offset<Smem>());
+    constexpr int CONSUMER_WARPS = TILE / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(&box.full[q], 1);
+            mbar_init(&box.empty[q], CONSUMER_WARPS);
+        }
+    }
+    stream_init(sm, CONSUMER_WARPS);  // thread 0: the stage barriers, then the barrier-init fence
+    __syncthreads();
+    if (warp == CONSUMER_WARPS) {
+        int issued = 0;  // stages issued by this CTA so far
+        for (int it = 0;; ++it) {
+            int item = 0;
+            if (lane == 0) item = atomicAdd(head, 1);
+            item = __shfl_sync(0xffffffffu, item, 0);
+            WorkItem w = {-1, 0, 0, 0};
+            if (item < n_items) {
+                const int r = item / n_tiles;
+                w.s = __ldg(order + r);
+                w.tile0 = (item - r * n_tiles) * TILE;
+                w.E = __ldg(ev_count + w.s);
+            }
+            const int q = it & 1;
+            const bool ok = mbar_wait(&box.empty[q], ((it >> 1) & 1) ^ 1, &sm.abort, status);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            if (lane == 0) {
+                box.item[q] = w;
+                mbar_arrive(&box.full[q]);  // release: the item is visible to the consumers' acquiring wait
+            }
+            if (w.s < 0) break;
+            const int n_stages = (w.E + SEV - 1) / SEV;
+            const int done = stream_produce_at(sm, ev + (long long)w.s * ev_cap, w.E, wt, ld, w.tile0, n_stages,
+                                               issued, lane, status);
+            issued += done;
+            if (done < n_stages) break;
+        }
+        if (sm.abort) stream_drain(sm, issued);
+        return;
+    }
+    int k0 = 0;  // the current item's first stage in the ring
+    for (int it = 0;; ++it) {
+        const int q = it & 1;
+        const bool ok = mbar_wait(&box.full[q], (it >> 1) & 1, &sm.abort, status);
+        if (!__all_sync(0xffffffffu, ok)) return;
+        const volatile int* vi = reinterpret_cast<const volatile int*>(&box.item[q]);
+        const int s = vi[0], tile0 = vi[1], E = vi[2];
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&box.empty[q]);
+        if (s < 0) return;
+        if (!forward_tile_item(sm, k0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out, x_out, t_out, z_out, status,
+                               pad))
+            return;
+        k0 += (E + SEV - 1) / SEV;
+    }
+}
+
+// Longest-first order of the samples for lif_fc_forward_queue_kernel, and the reset of its queue head. The
+// samples are ranked by descending event count in 512 logarithmic classes (16 per octave: the exponent and
+// top four mantissa bits of the float count + 1); the order inside a class is whatever the atomics give,
+// which changes only the schedule, never a result. One CTA of 1024 threads.
+__device__ __forceinline__ int count_class(int c) {
+    const int key = (int)(__float_as_uint((float)(c + 1)) >> 19) - (127 << 4);  // increasing in c, >= 0
+    return 511 - min(511, max(0, key));
+}
+
+__global__ void __launch_bounds__(1024) work_order_kernel(const int* __restrict__ ev_count, int batch,
+                                                          int* __restrict__ head, int* __restrict__ order) {
+    __shared__ int off[512];
+    __shared__ int warp_sum[16];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < 512) off[tid] = 0;
+    if (tid == 0) *head = 0;
+    __syncthreads();
+    for (int s = tid; s < batch; s += blockDim.x) atomicAdd(&off[count_class(ev_count[s])], 1);
+    __syncthreads();
+    // Exclusive scan of the 512 class sizes: 16 warps of 32 classes, then the warp totals.
+    int v = 0, incl = 0;
+    if (tid < 512) {
+        v = off[tid];
+        incl = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += u;
+        }
+        if (lane == 31) warp_sum[warp] = incl;
+    }
+    __syncthreads();
+    if (tid < 512) {
+        int base = 0;
+        for (int w = 0; w < warp; ++w) base += warp_sum[w];
+        off[tid] = base + incl - v;
+    }
+    __syncthreads();
+    for (int s = tid; s < batch; s += blockDim.x) order[atomicAdd(&off[count_class(ev_count[s])], 1)] = s;
 }
 
 // Event-parallel variant for layers with little neuron parallelism (few post neurons, or a small
@@ -289,6 +440,36 @@ static int launch_forward(const void* events, const int* ev_count, long long ev_
     return BATS_OK;
 }
 
+// Work-queue launch: the order kernel, then a grid of as many CTAs of the persistent kernel as are resident
+// at once on this GPU (at most one per work item).
+template <int TILE, int SEV, int STAGES>
+static int launch_forward_queue(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld,
+                                int batch, int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a,
+                                float* x, float* times, float* post_exp_tau, int* status, int pad, int* order,
+                                int* head, cudaStream_t stream) {
+    using Smem = StreamSmem<TILE, SEV, STAGES>;
+    const size_t smem = mailbox_offset<Smem>() + sizeof(ItemMailbox);
+    const void* kern = (const void*)lif_fc_forward_queue_kernel<TILE, SEV, STAGES>;
+    BATS_CUDA((cudaError_t)max_dynamic_smem_set(kern, (int)smem));
+    int dev = 0, n_sm = 0, per_sm = 0;
+    BATS_CUDA(cudaGetDevice(&dev));
+    BATS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    BATS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lif_fc_forward_queue_kernel<TILE, SEV, STAGES>,
+                                                            TILE + 32, smem));
+    const int n_tiles = (n_post + TILE - 1) / TILE;
+    BATS_REQUIRE((long long)batch * n_tiles < (1LL << 31), BATS_ERR_BAD_SHAPE,
+                 "lif_forward_fc_queue: batch * post-neuron tiles must stay below 2^31");
+    const int n_items = batch * n_tiles;
+    const int grid = (int)std::min<long long>(n_items, (long long)std::max(1, per_sm) * std::max(1, n_sm));
+    work_order_kernel<<<1, 1024, 0, stream>>>(ev_count, batch, head, order);
+    BATS_CUDA(cudaGetLastError());
+    lif_fc_forward_queue_kernel<TILE, SEV, STAGES><<<grid, TILE + 32, smem, stream>>>(
+        reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
+        post_exp_tau, status, pad, order, head, n_tiles, n_items);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
+}
+
 SolveConst make_solve_const(float c, float dtt, float tau, float max_sim) {
     SolveConst k;
     k.c = c;
@@ -363,4 +544,44 @@ extern "C" int bats_lif_forward_fc_algo(const void* events, const int* ev_count,
                                         cudaStream_t stream) {
     return forward_fc_impl(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, c, delta_theta_tau, tau,
                            max_simulation, n_spikes, a, x, times, post_exp_tau, algo, stream);
+}
+
+extern "C" size_t bats_lif_forward_fc_queue_workspace_bytes(int batch) {
+    // The queue head (own 256-byte line), then the sample order.
+    return 256 + ((size_t)(batch > 0 ? batch : 0) * sizeof(int) + 255) / 256 * 256;
+}
+
+extern "C" int bats_lif_forward_fc_queue(const void* events, const int* ev_count, long long ev_cap,
+                                         const float* weights_t, int ld, int batch, int n_post, int k_post, float c,
+                                         float delta_theta_tau, float tau, float max_simulation, int* n_spikes,
+                                         float* a, float* x, float* times, float* post_exp_tau, int algo,
+                                         void* workspace, size_t workspace_bytes, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0 && ld >= n_post && ld % 4 == 0, BATS_ERR_BAD_SHAPE,
+                 "lif_forward_fc_queue: bad shape (ld must be >= n_post and a multiple of 4)");
+    const int pad = (algo & BATS_FWD_NO_PAD) ? 0 : 1;
+    algo &= ~BATS_FWD_NO_PAD;
+    BATS_REQUIRE(algo == BATS_FWD_AUTO || algo == BATS_FWD_TILE || algo == BATS_FWD_TILE64, BATS_ERR_BAD_SHAPE,
+                 "lif_forward_fc_queue: algo must be BATS_FWD_AUTO, BATS_FWD_TILE or BATS_FWD_TILE64");
+    if (batch == 0 || n_post == 0) return BATS_OK;
+    BATS_REQUIRE(events && ev_count && weights_t && n_spikes && a && x && times && post_exp_tau && workspace,
+                 BATS_ERR_NULL, "lif_forward_fc_queue: null pointer");
+    BATS_REQUIRE(((uintptr_t)weights_t & 15) == 0 && ((uintptr_t)events & 15) == 0, BATS_ERR_BAD_SHAPE,
+                 "lif_forward_fc_queue: weights_t and events must be 16-byte aligned");
+    BATS_REQUIRE(((uintptr_t)workspace & 15) == 0 && workspace_bytes >= bats_lif_forward_fc_queue_workspace_bytes(batch),
+                 BATS_ERR_WORKSPACE, "lif_forward_fc_queue: workspace too small or not 16-byte aligned");
+    const bats::SolveConst sk = bats::make_solve_const(c, delta_theta_tau, tau, max_simulation);
+    int* status = nullptr;
+    BATS_CUDA((cudaError_t)bats::device_status(&status));
+    int* head = reinterpret_cast<int*>(workspace);
+    int* order = reinterpret_cast<int*>(reinterpret_cast<char*>(workspace) + 256);
+    if (algo == BATS_FWD_TILE64 || (n_post > 32 && n_post <= 64))
+        return bats::launch_forward_queue<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post,
+                                                    sk, n_spikes, a, x, times, post_exp_tau, status, pad, order, head,
+                                                    stream);
+    if (n_post <= 32)
+        return bats::launch_forward_queue<32, 16, 8>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post,
+                                                    sk, n_spikes, a, x, times, post_exp_tau, status, pad, order, head,
+                                                    stream);
+    return bats::launch_forward_queue<128, 8, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+                                                n_spikes, a, x, times, post_exp_tau, status, pad, order, head, stream);
 }

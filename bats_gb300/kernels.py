@@ -157,6 +157,33 @@ def get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron):
 
 FWD_AUTO, FWD_TILE, FWD_LANES, FWD_TILE64 = 0, 1, 2, 3
 FWD_NO_PAD = 0x100  # OR-ed into the algo: no +inf past the spike counts (outputs read only below them)
+# Python-side choices that route to bats_lif_forward_fc_queue (one persistent launch over a work queue of
+# (sample, tile) items, longest samples first), with the tile width of FWD_TILE or FWD_TILE64.
+FWD_QUEUE, FWD_QUEUE64 = 4, 5
+
+
+def is_queue_algo(algo: int) -> bool:
+    return (algo & ~FWD_NO_PAD) in (FWD_QUEUE, FWD_QUEUE64)
+
+
+def queue_workspace_bytes(batch: int) -> int:
+    return call_size("bats_lif_forward_fc_queue_workspace_bytes", int(batch))
+
+
+def forward_fc_call(events: Events, weights_t, n_post: int, k_post: int, c, dtt, tau32, max_simulation, outs,
+                    algo: int, stream: int, workspace=None, workspace_bytes: int = 0):
+    """One FC forward launch through the C ABI: bats_lif_forward_fc_queue for FWD_QUEUE / FWD_QUEUE64 (with the
+    given workspace), bats_lif_forward_fc_algo otherwise."""
+    n, a, x, t, z = outs
+    common = (ptr(events.events), ptr(events.counts), events.cap, ptr(weights_t), weights_t.shape[1], events.batch,
+              n_post, k_post, float(c), float(dtt), float(tau32), float(np.float32(max_simulation)), ptr(n), ptr(a),
+              ptr(x), ptr(t), ptr(z))
+    if is_queue_algo(algo):
+        tile = FWD_TILE64 if (algo & ~FWD_NO_PAD) == FWD_QUEUE64 else FWD_TILE
+        call("bats_lif_forward_fc_queue", *common, tile | (algo & FWD_NO_PAD), workspace, int(workspace_bytes),
+             stream)
+    else:
+        call("bats_lif_forward_fc_algo", *common, int(algo), stream)
 
 
 def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: float, theta: float,
@@ -164,18 +191,20 @@ def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: f
     """FC LIF forward (replaces get_spike_weights + compute_spike_times,
     bats/CudaKernels/Wrappers/Inference/compute_spike_times.py:11-32). Returns n, a, x, times, post_exp_tau.
     algo: FWD_TILE (CTA per neuron tile and sample), FWD_LANES (warp per neuron and sample, 32 events in
-    parallel) or FWD_AUTO; all give identical results."""
+    parallel), FWD_QUEUE / FWD_QUEUE64 (persistent CTAs over a longest-first work queue) or FWD_AUTO; all give
+    identical results."""
     B = events.batch
     tau32, c, dtt = lif_constants(tau_s, theta, delta_theta)
     dev = events.events.device
     if outs is None:
         outs = (torch.empty((B, n_post), dtype=I32, device=dev),
                 *(torch.empty((B, n_post, k_post), dtype=F32, device=dev) for _ in range(4)))
-    n, a, x, t, z = outs
-    call("bats_lif_forward_fc_algo", ptr(events.events), ptr(events.counts), events.cap, ptr(weights_t),
-         weights_t.shape[1], B, n_post, k_post, float(c), float(dtt), float(tau32), float(np.float32(max_simulation)),
-         ptr(n), ptr(a), ptr(x), ptr(t), ptr(z), int(algo), stream_ptr())
-    return n, a, x, t, z
+    ws = None
+    if is_queue_algo(algo):
+        ws = torch.empty(queue_workspace_bytes(B), dtype=torch.uint8, device=dev)
+    forward_fc_call(events, weights_t, n_post, k_post, c, dtt, tau32, max_simulation, outs, algo, stream_ptr(),
+                    ptr(ws), 0 if ws is None else ws.numel())
+    return tuple(outs)
 
 
 def conv_forward(events: Events, filters, pre_shape, k_post: int, tau_s: float, theta: float, delta_theta: float,

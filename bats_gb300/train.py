@@ -80,6 +80,7 @@ class FCTrainStep:
             grp = max(2, self.grad_group or K.default_group(B, spec.n_neurons, n_prev))
             self.groups.append(grp)
             ws = max(ws, K.call_size("bats_sort_events_workspace_bytes", B, n_prev, k_prev),
+                     K.queue_workspace_bytes(B),
                      K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev, grp),
                      K.call_size("bats_pre_errors_workspace_bytes", B, n_prev * k_prev, spec.n_neurons))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
@@ -94,7 +95,6 @@ class FCTrainStep:
         self.h_loss = torch.empty((B,), dtype=f32, pin_memory=True)
         self.fwd_algo = [K.FWD_AUTO] * len(self.specs)
         self.launches = self._build_launches()
-        self.launches_per_step = self._count_launches()
 
     def _pad_flag(self, li: int) -> int:
         """Hidden layers skip the +inf padding of their spike trains: everything that reads them (the next
@@ -128,11 +128,8 @@ class FCTrainStep:
                     ptr(ev.bucket_offsets), K.BUCKET_WIDTH, ws, wsb, s)))
             n, a, x, t, z = self.out[li]
             L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
-                      call("bats_lif_forward_fc_algo", ptr(ev.events), ptr(ev.counts), ev.cap, ptr(self.Wt[li]),
-                           self.Wt[li].shape[1], B, spec.n_neurons, spec.max_n_spike, float(c), float(dtt),
-                           float(tau32), float(np.float32(self.max_sim)), *(ptr(v) for v in o),
-                           self.fwd_algo[li] | self._pad_flag(li),
-                           s)))
+                      K.forward_fc_call(ev, self.Wt[li], spec.n_neurons, spec.max_n_spike, c, dtt, tau32,
+                                        self.max_sim, o, self.fwd_algo[li] | self._pad_flag(li), s, ws, wsb)))
             pre_times, pre_counts = t, n
         n_out = self.out[-1][0]
         L.append(("loss", lambda s: call("bats_spike_count_loss", ptr(n_out), 0, None, ptr(self.labels),
@@ -182,8 +179,14 @@ class FCTrainStep:
     KERNELS_PER_CALL = {"sort": 1, "forward": 1, "loss": 1, "prep": 1, "grad": 2, "pre_err": 3, "powers": 1,
                         "adam": 1}
 
+    @property
+    def launches_per_step(self) -> int:
+        """Kernels launched by one step with the current variant choices."""
+        return self._count_launches()
+
     def _count_launches(self):
-        return sum(self.KERNELS_PER_CALL[name.split(".")[-1]] for name, _ in self.launches)
+        n = sum(self.KERNELS_PER_CALL[name.split(".")[-1]] for name, _ in self.launches)
+        return n + sum(1 for a in self.fwd_algo if K.is_queue_algo(a))  # the queue's order kernel
 
     def step(self) -> None:
         """One training step on the device-resident inputs (in_times, labels), launched eagerly."""
@@ -221,9 +224,10 @@ class FCTrainStep:
                 fwd[f"{tag}.forward"](s)
                 self.fwd_algo[li] = saved
 
-            algos = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES}
+            algos = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES, "queue": K.FWD_QUEUE}
             if spec.n_neurons > 64:
                 algos["tile64"] = K.FWD_TILE64
+                algos["queue64"] = K.FWD_QUEUE64
             best = tuner.pick("fc_forward", shape, {k: (lambda a=a: run_fwd(a)) for k, a in algos.items()},
                               force=force)
             self.fwd_algo[li] = algos[best]
@@ -243,6 +247,9 @@ class FCTrainStep:
                                 force=force)
                 self.groups[li] = cands[bg]
             choice[tag] = {"forward": best, "grad_group": self.groups[li]}
+            fwd_ms = tuner.timings.get(tuner.key("fc_forward", *shape))
+            if fwd_ms:  # timed now (not taken from the cache): every candidate's time, for the record
+                choice[tag]["forward_ms"] = {k: round(v, 4) for k, v in fwd_ms.items()}
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
         torch.cuda.synchronize()
         self.tuned = choice

@@ -114,6 +114,23 @@ int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long 
                              float max_simulation, int* n_spikes, float* a, float* x, float* times,
                              float* post_exp_tau, int algo, cudaStream_t stream);
 
+/* The FC forward as one persistent launch over a work queue, for batches whose samples carry very different
+ * numbers of events. A first kernel ranks the samples by descending event count (in the workspace, which also
+ * holds the queue head it resets); then as many CTAs as fit on the GPU at once take (sample, post-neuron tile)
+ * items from the queue, longest samples first, each producer warp streaming its next item while the consumers
+ * finish the current one. Outputs, arguments and results are those of bats_lif_forward_fc_algo (bit-identical);
+ * algo is BATS_FWD_AUTO or BATS_FWD_TILE (tile width by n_post) or BATS_FWD_TILE64, optionally OR-ed with
+ * BATS_FWD_NO_PAD. The workspace (16-byte aligned, bats_lif_forward_fc_queue_workspace_bytes(batch) bytes) must
+ * not be used by another launch until this one ends. Replaces the same reference wrappers as
+ * bats_lif_forward_fc (get_spike_weights.py:9-18, compute_spike_times.py:11-32); the reference runs one thread
+ * per (sample, neuron) with no scheduling of its own. */
+size_t bats_lif_forward_fc_queue_workspace_bytes(int batch);
+int bats_lif_forward_fc_queue(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
+                              int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,
+                              float max_simulation, int* n_spikes, float* a, float* x, float* times,
+                              float* post_exp_tau, int algo, void* workspace, size_t workspace_bytes,
+                              cudaStream_t stream);
+
 /* Convolutional LIF forward on a (X, Y, C) input with (C_out, fx, fy, C) filters, valid, stride 1.
  * Replaces compute_spike_times_conv (bats/CudaKernels/Wrappers/Inference/compute_spike_times_conv.py:11-35). */
 int bats_conv_forward(const void* events, const int* ev_count, long long ev_cap, const float* weights, int batch,

@@ -10,6 +10,7 @@ import pytest
 import torch
 
 from bats_gb300 import kernels as K
+from bats_gb300._lib import BatsError, check_device_status, ptr, stream_ptr
 from oracle import bats_ref64 as R
 from oracle import refkern
 from tests._helpers import (conditioned_reference, count_mismatches, grazing_mask, leading_mask, mnist_like_input,
@@ -249,7 +250,7 @@ def _both_algos(t, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
     ev = K.sort_events(tt, np.float32(tau_s), np.float32(2 * tau_s))
     wt = K.transpose_weights(torch.tensor(W, device="cuda"))
     outs = []
-    for algo in (K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64):
+    for algo in (K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64, K.FWD_QUEUE, K.FWD_QUEUE64):
         o = K.lif_forward_fc(ev, wt, W.shape[0], K_post, tau_s, theta, dtheta, max_sim, algo=algo)
         outs.append([v.cpu().numpy() for v in o])
     return outs
@@ -267,8 +268,8 @@ def _assert_identical(p, q, what):
 
 @pytest.mark.parametrize("case", ["small", "mnist_active", "long_narrow", "long_wide", "cap_and_cut"])
 def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
-    """The warp-per-neuron forward (32 events per step, FWD_LANES) and the 64-neuron-tile variant are
-    bit-identical to the tile kernel on
+    """The warp-per-neuron forward (32 events per step, FWD_LANES), the 64-neuron-tile variant and the
+    persistent work-queue kernel (both tile widths) are bit-identical to the tile kernel on
     short and long event streams, narrow and wide layers, a full spike buffer and a max_simulation cut; on
     a long stream it also matches the reference kernels."""
     rng = np.random.default_rng(5)
@@ -289,16 +290,18 @@ def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
         t, n_in = multi_spike_input(3, 50, 6, 0.2, seed=6, p_silent=0.0)
         W = np.abs(rng.normal(0, 1, (40, 50))).astype(np.float32)
         args = (0.1, 0.05, 0.05, 4, 0.12)
-    tile, lanes, tile64 = _both_algos(t, W, *args)
+    tile, lanes, tile64, queue, queue64 = _both_algos(t, W, *args)
     assert tile[0].sum() > 0, "the case should spike"
     _assert_identical(tile, lanes, case)
     _assert_identical(tile, tile64, case + " (64-neuron tiles)")
+    _assert_identical(tile, queue, case + " (work queue)")
+    _assert_identical(tile, queue64, case + " (work queue, 64-neuron tiles)")
     if case == "long_narrow":
         ref = run_ref(t, n_in, W, *args)
         check_against(lanes, ref, None, what="lanes vs reference kernels")
 
 
-@pytest.mark.parametrize("algo", [K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64])
+@pytest.mark.parametrize("algo", [K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64, K.FWD_QUEUE])
 def test_no_pad_flag_leaves_slots_past_counts(cuda, algo):
     """BATS_FWD_NO_PAD: counts and every value below them are those of the padded forward, and the slots
     past the counts keep what the buffers held (here a sentinel)."""
@@ -320,3 +323,66 @@ def test_no_pad_flag_leaves_slots_past_counts(cuda, algo):
         r, g = r.cpu().numpy(), g.cpu().numpy()
         assert np.array_equal(r[valid].view(np.uint32), g[valid].view(np.uint32))
         assert (g[~valid] == 12345.0).all()
+
+
+def uneven_input(batch, n_in, median, hi, t_max, seed, p_empty=0.05):
+    """Samples with lognormal event counts (median `median`, at most `hi`), some of them empty, channels
+    uniform over n_in, times U(0, t_max): spike trains (B, n_in, K_in), K_in the largest per-channel count."""
+    rng = np.random.default_rng(seed)
+    counts = np.clip(np.round(rng.lognormal(np.log(median), 1.0, batch)), 1, hi).astype(np.int64)
+    counts[rng.random(batch) < p_empty] = 0
+    chans = [rng.integers(0, n_in, c) for c in counts]
+    k_in = max(1, max(int(np.bincount(ch, minlength=n_in).max()) if len(ch) else 0 for ch in chans))
+    t = np.full((batch, n_in, k_in), np.inf, dtype=np.float32)
+    for q, ch in enumerate(chans):
+        for j in np.unique(ch):
+            m = int((ch == j).sum())
+            t[q, j, :m] = np.sort(rng.uniform(0, t_max, m))
+    return t, counts
+
+
+@pytest.mark.parametrize("n_post", [20, 50, 300])
+def test_work_queue_forward_on_uneven_batch(cuda, n_post):
+    """The persistent work-queue forward on a batch whose samples carry 0 to 600 events (lognormal, some
+    empty) is bit-identical to the one-CTA-per-item tile kernel, padded and unpadded, and again on a second
+    call with the same workspace (the order kernel resets the queue head): tile widths 32, 64 and 128 with a
+    partial last tile, K = 8 so that some neurons fill their spike buffer."""
+    t, counts = uneven_input(333, 256, 40, 600, 0.05, seed=9)
+    assert (counts == 0).any() and counts.max() > 300
+    rng = np.random.default_rng(10)
+    W = rng.uniform(-0.5, 1.5, (n_post, 256)).astype(np.float32)
+    ev = K.sort_events(torch.tensor(t, device="cuda"), np.float32(0.13), np.float32(0.26))
+    wt = K.transpose_weights(torch.tensor(W, device="cuda"))
+    args = (n_post, 8, 0.13, 0.2, 0.2, 0.2)
+    tile = [v.cpu().numpy() for v in K.lif_forward_fc(ev, wt, *args, algo=K.FWD_TILE)]
+    assert tile[0].sum() > 0 and (tile[0] == 8).any(), "the case should spike, some neurons up to K"
+    ws = torch.empty(K.queue_workspace_bytes(333), dtype=torch.uint8, device="cuda")
+    outs = (torch.empty((333, n_post), dtype=torch.int32, device="cuda"),
+            *(torch.empty((333, n_post, 8), device="cuda") for _ in range(4)))
+    tau32, c, dtt = K.lif_constants(0.13, 0.2, 0.2)
+    for rep in range(2):
+        for o in outs:
+            o.fill_(-1)
+        K.forward_fc_call(ev, wt, n_post, 8, c, dtt, tau32, 0.2, outs, K.FWD_QUEUE, stream_ptr(), ptr(ws),
+                          ws.numel())
+        _assert_identical(tile, [v.cpu().numpy() for v in outs], f"work queue, call {rep + 1}")
+    K.forward_fc_call(ev, wt, n_post, 8, c, dtt, tau32, 0.2, outs, K.FWD_QUEUE | K.FWD_NO_PAD, stream_ptr(),
+                      ptr(ws), ws.numel())
+    n = outs[0].cpu().numpy()
+    assert np.array_equal(n, tile[0])
+    valid = leading_mask(n, 8)
+    for i in range(1, 5):
+        assert np.array_equal(outs[i].cpu().numpy()[valid].view(np.uint32), tile[i][valid].view(np.uint32))
+    check_device_status()
+
+
+def test_work_queue_forward_rejects_small_workspace(cuda):
+    t, _ = mnist_like_input(4, seed=1)
+    ev = K.sort_events(torch.tensor(t, device="cuda"), np.float32(0.13), np.float32(0.26))
+    wt = K.transpose_weights(torch.tensor(np.ones((8, 784), np.float32), device="cuda"))
+    outs = (torch.empty((4, 8), dtype=torch.int32, device="cuda"), *(torch.empty((4, 8, 4), device="cuda")
+                                                                      for _ in range(4)))
+    ws = torch.empty(16, dtype=torch.uint8, device="cuda")
+    tau32, c, dtt = K.lif_constants(0.13, 1.0, 1.0)
+    with pytest.raises(BatsError):
+        K.forward_fc_call(ev, wt, 8, 4, c, dtt, tau32, 0.2, outs, K.FWD_QUEUE, stream_ptr(), ptr(ws), ws.numel())

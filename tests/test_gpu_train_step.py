@@ -14,6 +14,7 @@ import pytest
 import torch
 
 from bats_gb300 import Network, SpikeCountClassLoss
+from bats_gb300 import kernels as KN
 from bats_gb300.Layers import InputLayer, LIFLayer
 from bats_gb300.Optimizers import AdamOptimizer
 from bats_gb300.autotune import Autotuner
@@ -126,3 +127,26 @@ def test_train_host_pipeline_matches_step_host(cuda):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), f"loss of step {q}"
     for wa, wb in zip(a.W, b.W):
         assert torch.equal(wa, wb)
+
+
+def test_work_queue_forward_step_equals_tile_step_under_graph_capture(cuda):
+    """Every layer's forward on the persistent work-queue kernel (order kernel + queue kernel, captured in the
+    step's CUDA graph and replayed) gives the weights of the tile-kernel step bit for bit over 3 steps, on a
+    batch of uneven samples."""
+    t, n, ws, labels = case(B=48, seed=5)
+    keep = np.random.default_rng(6).random(t.shape[:2]) < np.linspace(0.05, 1.0, 48)[:, None]
+    t = np.where(keep[:, :, None], t, np.inf).astype(np.float32)  # 5 % to 100 % of the events per sample
+    tile = make_step(t, ws, labels)
+    tile.fwd_algo = [KN.FWD_TILE] * len(tile.fwd_algo)
+    queue = make_step(t, ws, labels)
+    queue.fwd_algo = [KN.FWD_QUEUE] * len(queue.fwd_algo)
+    assert queue.launches_per_step == tile.launches_per_step + len(queue.fwd_algo)
+    assert queue.try_capture(), queue.capture_error  # one eager step, then the capture
+    tile.step()
+    for _ in range(2):
+        tile.step()
+        queue.replay()
+    torch.cuda.synchronize()
+    assert int(queue.out[0][0].sum()) > 0
+    for a, b in zip(tile.W, queue.W):
+        assert torch.equal(a, b)
