@@ -339,7 +339,117 @@ def profile_one_step(workload):
     print(json.dumps({"profiled_step": workload, "launches": [n for n, _ in ts.launches]}))
 
 
-def plain_api_rate(variant, steps, flush):
+def profile_kernels():
+    """Every kernel of the library on the workloads' own shapes: each entry-point call runs once as a warm-up,
+    then once more inside a named NVTX range under "census", for one ncu pass over all of them
+    (ncu --nvtx --nvtx-include "census/" ...). The calls: the active 784-800-800-10 train step (batch 256,
+    forward variants tile / work queue / lanes on layers 1 / 2 / 3), the same step through the drop-in layer
+    API (per-sample gradients, Adam deltas), the conv train step (batch 128), and one call of each other
+    entry point: pre-exponentials, the intensity encoder, event-list conversion of a 16-request serving
+    batch, the TTFS and spike-time losses, untiled Adam, NAdam, both synaptic-scaling regularizers,
+    transpose, add_deltas, the generic backward prep (reset errors, factors), the conv backward for filters
+    too large for shared memory, and the allocation-free gradient."""
+    import ctypes
+
+    import torch
+    from bats_gb300 import _lib
+    from bats_gb300 import kernels as K
+    from bats_gb300._lib import stream_ptr
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(21)
+    dev = "cuda"
+    calls = []
+
+    ts = build_train_step("active")
+    ts.fwd_algo = [K.FWD_TILE, K.FWD_QUEUE, K.FWD_LANES]
+    for name, fn in ts.launches:
+        calls.append((f"step.{name}", lambda fn=fn: fn(stream_ptr())))
+    calls.append(("api_step", plain_api_step("active")))
+    conv_step, _, _ = conv_network()
+    calls.append(("conv_step", conv_step))
+
+    tau = 2 * TAU_S
+    tau32, c, dtt = K.lif_constants(TAU_S, 0.2, 0.2)
+    calls.append(("pre_exps", lambda: K.compute_pre_exps(ts.in_times, TAU_S, tau)))
+    px = torch.tensor(rng.integers(0, 256, (B, SIZES[0])).astype(np.uint8), device=dev)
+    calls.append(("intensity_to_spike_times", lambda: K.intensity_to_spike_times(px)))
+    n_ev = np.exp(rng.uniform(np.log(50), np.log(5000), 16)).astype(np.int64)
+    idx = np.full((16, int(n_ev.max())), -1, np.int32)
+    tms = np.zeros(idx.shape, np.float32)
+    for q, m in enumerate(n_ev):
+        idx[q, :m] = rng.integers(0, 700, m)
+        tms[q, :m] = np.sort(rng.uniform(0, 0.2, m))
+    idx_d, tms_d = torch.tensor(idx, device=dev), torch.tensor(tms, device=dev)
+    calls.append(("events_to_trains", lambda: K.convert_to_spike_per_neuron(idx_d, tms_d, 700)))
+    out_t = ts.out[-1][3]
+    targets = torch.full(out_t.shape, float("inf"), device=dev)
+    calls.append(("ttfs_softmax_cross_entropy", lambda: K.ttfs_softmax_cross_entropy(out_t, ts.labels, tau)))
+    calls.append(("spike_time_loss", lambda: K.spike_time_loss(out_t, targets, 2)))
+    g = ts.grad[0]
+    m1, v1, m2, v2 = (torch.zeros_like(g) for _ in range(4))
+    d1, d2 = torch.empty_like(g), torch.empty_like(g)
+    calls.append(("adam_step", lambda: K.adam_step(g, m1, v1, 0.9, 0.999, 1e-8, LR, 0.9, 0.999, delta=d1)))
+    calls.append(("nadam_step", lambda: K.nadam_step(g, m2, v2, 0.9, 0.999, 1e-8, LR, 0.9, 0.999, d2)))
+    gps = torch.zeros((64, SIZES[1], SIZES[0]), device=dev)
+    ratios = torch.tensor(rng.uniform(0, 1, 64).astype(np.float32), device=dev)
+    labels_f = torch.tensor(rng.integers(0, SIZES[1], 64).astype(np.float32), device=dev)
+    calls.append(("weights_synaptic_scaling", lambda: K.apply_weights_synaptic_scaling(
+        ts.W[0], ratios, ts.out[0][0][:64].contiguous(), gps, 0.5, 0.1)))
+    calls.append(("label_weights_synaptic_scaling", lambda: K.apply_label_weights_synaptic_scaling(
+        ts.W[0], labels_f, ts.out[0][0][:64].contiguous(), gps, 0.1)))
+    calls.append(("transpose", lambda: K.transpose_weights(ts.W[0])))
+    w_copy = ts.W[0].clone()
+    calls.append(("add_deltas", lambda: K.add_deltas(w_copy, d1)))
+    errs = torch.tensor(rng.uniform(-1, 1, (B, SIZES[1], K_SPIKE)).astype(np.float32), device=dev)
+    t1, a1, x1, z1 = (o.clone() for o in ts.out[0][1:])  # the padded first hidden layer after a step
+    calls.append(("propagate_recurrent_errors", lambda: K.propagate_recurrent_errors(x1, z1, errs, dtt)))
+    calls.append(("compute_factors", lambda: K.compute_factors(t1, a1, c, x1, z1, tau32)))
+    # A conv layer whose per-sample filter gradient (128 x 5 x 5 x 15 floats) exceeds shared memory.
+    ct = np.full((32, 12 * 12 * 15, 4), np.inf, np.float32)
+    nf = rng.integers(0, 5, ct.shape[:2])
+    for q in range(4):
+        ct[:, :, q] = np.where(q < nf, rng.uniform(0.01 * q, 0.01 * (q + 1), ct.shape[:2]), np.inf)
+    cev = K.sort_events(torch.tensor(ct, device=dev), np.float32(TAU_S), np.float32(tau), bucketed=False)
+    cw = torch.tensor(rng.uniform(0, 0.2, (128, 5, 5, 15)).astype(np.float32), device=dev)
+    co = K.conv_forward(cev, cw, (12, 12, 15), 10, TAU_S, 0.3, 0.3, MAX_SIM)
+    ctc, ccc, cdc = K.lif_constants(TAU_S, 0.3, 0.3)
+    cerr = torch.tensor(rng.uniform(-1, 1, co[3].shape).astype(np.float32), device=dev)
+    ctabs = K.backward_prep(co[3], co[1], co[2], co[4], cerr, ccc, ctc, cdc)
+    calls.append(("conv_backward_large_filters", lambda: K.conv_backward(cev, cw, (12, 12, 15), co[3], ctabs, TAU_S,
+                                                                          tau)))
+    na_out = torch.empty((SIZES[1], SIZES[0]), device=dev)
+    lib = _lib.load()
+
+    def noalloc():
+        ev, tb = ts.ev[0], ts.tabs[0]
+        st = lib.bats_weights_gradient_mean_noalloc(
+            ev.events.data_ptr(), ev.counts.data_ptr(), ev.cap, ts.out[0][3].data_ptr(), tb.tables.data_ptr(),
+            tb.nvalid.data_ptr(), B, SIZES[1], K_SPIKE, SIZES[0], 32, na_out.data_ptr(),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if st != 0:
+            raise RuntimeError(lib.bats_last_error().decode())
+    calls.append(("weights_gradient_mean_noalloc", noalloc))
+
+    for _, fn in calls:  # warm-up: module load, first-call set-up
+        fn()
+    torch.cuda.synchronize()
+    flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    flush_l2(flush)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("census")
+    for name, fn in calls:
+        torch.cuda.nvtx.range_push(name)
+        fn()
+        torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    _lib.check_device_status()
+    print(json.dumps({"profiled": "census", "calls": [n for n, _ in calls]}))
+
+
+def plain_api_step(variant):
+    """One train step of the 784-800-800-10 network through the drop-in layer API (per-sample gradients, the
+    caller's batch mean, AdamOptimizer deltas applied by the network), as a no-argument function."""
     import torch
     from bats_gb300 import Network, SpikeCountClassLoss
     from bats_gb300.Layers import InputLayer, LIFLayer
@@ -369,6 +479,11 @@ def plain_api_rate(variant, steps, flush):
         d = opt.step([None if x is None else x.mean(0) for x in g])
         net.apply_deltas(d)
 
+    return step
+
+
+def plain_api_rate(variant, steps, flush):
+    step = plain_api_step(variant)
     ms, _ = time_steps(step, steps, 1, flush)
     return {"value": B * steps / (ms / 1e3), "unit": "samples/s", "steps": steps,
             "what": "Network/LIFLayer/SpikeCountClassLoss/AdamOptimizer drop-in API, per-sample gradients"}
@@ -473,12 +588,12 @@ def conv_weights(seed=3):
             rng.uniform(-1, 1, (300, 640)).astype(np.float32), rng.uniform(-1, 1, (10, 300)).astype(np.float32)]
 
 
-def conv_bench(steps: int = 5):
+def conv_network():
     """The convolutional network of the reference's MNIST conv experiment (experiments/mnist/train_conv.py:
     conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> FC 300 -> 10, thresholds 0.04 / 0.8 / 0.6 / 0.3 with
     delta_theta = theta, tau_s 0.13, weights U(-1, 1)), max_n_spike 10 in every layer, batch 128, on
     synthetic MNIST-shaped single-spike input; full train step (forward, spike-count loss, exact backward,
-    Adam) through the drop-in layer API, and the same step on the reference's own CUDA kernels."""
+    Adam) through the drop-in layer API. Returns (step, layers, inputs (t, n, labels))."""
     import torch
     from bats_gb300 import Network, SpikeCountClassLoss
     from bats_gb300.Layers import ConvInputLayer, ConvLIFLayer, LIFLayer, PoolingLayer
@@ -520,6 +635,15 @@ def conv_bench(steps: int = 5):
         g = net.backward(err)
         net.apply_deltas(opt.step([None if x is None else x.mean(0) for x in g]))
 
+    return step, layers, (t, n, labels)
+
+
+def conv_bench(steps: int = 5):
+    """The conv network's train step (conv_network) timed, next to the same step on the reference's own CUDA
+    kernels."""
+    import torch
+    Bc = 128
+    step, layers, (t, n, labels) = conv_network()
     flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ms, _ = time_steps(step, steps, 3, flush)
     spikes = [int(L.spike_trains[1].sum().item()) for L in layers]
@@ -629,6 +753,8 @@ def main():
     ap.add_argument("--workload", default="all", choices=["all", "literal", "active", "serving", "conv", "batching"],
                     help="all (default): every measurement; otherwise only that one (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline (profiling runs)")
+    ap.add_argument("--profile-kernels", action="store_true",
+                    help="run every kernel of the library once inside NVTX ranges under \"census\" (for ncu)")
     ap.add_argument("--profile-step", action="store_true",
                     help="with --workload literal|active|batching: set up and autotune the step, then run one "
                          "eager step with an NVTX range named after every launch (for ncu --nvtx-include)")
@@ -652,6 +778,9 @@ def main():
 
     if args.profile_step:
         profile_one_step(args.workload)
+        return
+    if args.profile_kernels:
+        profile_kernels()
         return
 
     # CPU baseline first (spawned workers, before any GPU context exists in this process).
