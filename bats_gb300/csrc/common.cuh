@@ -102,6 +102,36 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_start, flo
     return usable && (level1 || right_of_window || left_of_window);
 }
 
+// Screen of a run of consecutive events (FC layer, tau = 2 tau_s): true when the reference solver provably
+// accepts no crossing after any event of the run, given the run's states (a_u, b_u) only through
+// amin = min_u a_u and bmax = max_u b_u, and e_first = exp(t/tau) of the run's first event.
+// With x = exp(t/tau), the crossing condition c x^2 - b x + a = 0 reads V(x) = b/x - a/x^2 = c. For
+// x >= X0 = e_first (1 - 2^-17) every state satisfies V_u(x) <= max(bmax, 0)/X0 + max(-amin, 0)/X0^2,
+// a bound that decreases in x. If it lies below c (1 - 2^-20), then for each state either
+//   * the maximum of V_u over x > 0 is below c (1 - 2^-20), so b_u^2 < 4 a_u c (1 - 2^-20) (or a_u <= 0 or
+//     b_u <= 0, whose roots the reference rejects by sign, as in no_crossing), and the reference's
+//     discriminant, fl(b^2) - 4ac with fl(b^2) <= b^2 (1 + 2^-24), is negative; or
+//   * V_u reaches c only left of X0 (V_u is unimodal), so both roots lie below e_first (1 - 2^-17): the
+//     reference's root z (within 2^-21 of the smaller root), after __logf, gives a time before the event,
+//     which it rejects — the margin of the left-of-window test of no_crossing.
+// The test is evaluated multiplied through by X0^2 > 0: fma(max(bmax, 0), X0, max(-amin, 0)) < c' X0 X0 with
+// c' = c (1 - 2^-19), whose roundings (a few units of 2^-24) stay inside the 2^-20 margin; the same margin
+// covers the reference's fl(b^2) in place of b^2 (a 2^-24 change of b moves V by at most 2^-24 c right of
+// X0, where b/x < c). As for no_crossing, the run must start before 8 tau (X0 < 2981) and every |a_u| must
+// be at least 2^-60 (amag = min_u |a_u|), so that the discriminant's rounding is relative. fminf/fmaxf
+// skip NaN, so the run's last state (a_last, b_last) must be finite: a non-finite state stays non-finite
+// through the later events of the run, and the reference turns it into a NaN spike. No division or square
+// root.
+__device__ __forceinline__ bool stage_no_crossing(float amin, float bmax, float amag, float a_last, float b_last,
+                                                  float e_first, const SolveConst& k) {
+    const float x0 = e_first * (1.0f - 0x1p-17f);
+    const float lhs = fmaf(fmaxf(bmax, 0.0f), x0, fmaxf(-amin, 0.0f));
+    const float rhs = (k.c * (1.0f - 0x1p-19f)) * x0 * x0;
+    return k.fast && k.c >= 0x1p-40f && k.c <= 0x1p40f && x0 > 0.0f && x0 < 2981.0f && amag >= 0x1p-60f &&
+           fabsf(a_last) <= 0x1p120f &&
+           fabsf(b_last) <= 0x1p120f && lhs < rhs;
+}
+
 // Threshold-crossing solver of the current-based LIF neuron after an input event.
 //
 // The neuron state is a = sum w*exp(t_i/tau_s), b = sum w*exp(t_i/tau) - (dtheta/tau)*sum z_k,

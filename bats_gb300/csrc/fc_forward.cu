@@ -28,7 +28,11 @@ namespace bats {
 // Consumer warps' part of one work item (sample s, post neurons tile0 .. tile0 + TILE - 1): thread = post
 // neuron. The item's event stages are stages k0 .. k0 + ceil(E / SEV) - 1 of the CTA's ring (k0 = 0 when the
 // CTA has one item). Returns false when a wait gave up (the CTA is aborting).
-template <int TILE, int SEV, int STAGES>
+// SCREEN: every full stage first runs only the accumulation, tracking the smallest a and |a| and the largest
+// b of its states, and skips the per-event tests when stage_no_crossing rules out a crossing after any of
+// its events (quiet neurons: one test per stage instead of one per event); otherwise the stage is
+// evaluated as without SCREEN. The FMA sequence is the same either way, so results are bit-identical.
+template <int TILE, int SEV, int STAGES, bool SCREEN = false>
 __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>& sm, int k0, int s, int tile0, int E,
                                                   int n_post, int k_post, const SolveConst& sk,
                                                   int* __restrict__ n_spikes, float* __restrict__ a_out,
@@ -60,7 +64,27 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
             // stage overlap; events past the sample's end (last stage) leave the state unchanged.
             float aa = a, bb = b;
             unsigned cand = 0u;
-            if (m0 + SEV < E) {
+            bool screened = false;
+            if (SCREEN && m0 + SEV < E) {
+                float amin = BATS_INF, bmax = -BATS_INF, amag = BATS_INF;
+#pragma unroll
+                for (int u = 0; u < SEV; ++u) {
+                    const float w = sm.rows[slot][u][tid];
+                    aa = fmaf(w, se[u].es, aa);
+                    bb = fmaf(w, se[u].e, bb);
+                    amin = fminf(amin, aa);
+                    amag = fminf(amag, fabsf(aa));
+                    bmax = fmaxf(bmax, bb);
+                }
+                screened = stage_no_crossing(amin, bmax, amag, aa, bb, se[0].e, sk);
+                if (!screened) {
+                    aa = a;
+                    bb = b;
+                }
+            }
+            if (screened) {
+                // no event of the stage can cross: aa, bb hold the state after the stage
+            } else if (m0 + SEV < E) {
                 // A full stage followed by more events (every stage but the last): no bounds to select on.
 #pragma unroll
                 for (int u = 0; u < SEV; ++u) {
@@ -130,7 +154,7 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
     return true;
 }
 
-template <int TILE, int SEV, int STAGES>
+template <int TILE, int SEV, int STAGES, bool SCREEN>
 __global__ void __launch_bounds__(TILE + 32)
 lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                       const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
@@ -152,7 +176,8 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
         stream_produce(sm, evs, E, wt, ld, tile0, n_stages, lane, status);
         return;
     }
-    forward_tile_item(sm, 0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out, x_out, t_out, z_out, status, pad);
+    forward_tile_item<TILE, SEV, STAGES, SCREEN>(sm, 0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out, x_out, t_out,
+                                                z_out, status, pad);
 }
 
 // Persistent variant over a work queue, for batches whose samples carry very different numbers of events.
@@ -182,7 +207,7 @@ __host__ __device__ constexpr size_t mailbox_offset() {
     return (sizeof(Smem) + 15) / 16 * 16;
 }
 
-template <int TILE, int SEV, int STAGES>
+template <int TILE, int SEV, int STAGES, bool SCREEN>
 __global__ void __launch_bounds__(TILE + 32)
 lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                             const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
@@ -243,8 +268,8 @@ lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict_
         __syncwarp();
         if (lane == 0) mbar_arrive(&box.empty[q]);
         if (s < 0) return;
-        if (!forward_tile_item(sm, k0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out, x_out, t_out, z_out, status,
-                               pad))
+        if (!forward_tile_item<TILE, SEV, STAGES, SCREEN>(sm, k0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out,
+                                                         x_out, t_out, z_out, status, pad))
             return;
         k0 += (E + SEV - 1) / SEV;
     }
@@ -426,14 +451,15 @@ static int launch_forward_lanes(const void* events, const int* ev_count, long lo
     return BATS_OK;
 }
 
-template <int TILE, int SEV, int STAGES>
+template <int TILE, int SEV, int STAGES, bool SCREEN>
 static int launch_forward(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld, int batch,
                           int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a, float* x,
                           float* times, float* post_exp_tau, int* status, int pad, cudaStream_t stream) {
     const size_t smem = sizeof(StreamSmem<TILE, SEV, STAGES>);
-    BATS_CUDA((cudaError_t)max_dynamic_smem_set((const void*)lif_fc_forward_kernel<TILE, SEV, STAGES>, (int)smem));
+    BATS_CUDA((cudaError_t)max_dynamic_smem_set((const void*)lif_fc_forward_kernel<TILE, SEV, STAGES, SCREEN>,
+                                                (int)smem));
     dim3 grid((n_post + TILE - 1) / TILE, batch);
-    lif_fc_forward_kernel<TILE, SEV, STAGES><<<grid, TILE + 32, smem, stream>>>(
+    lif_fc_forward_kernel<TILE, SEV, STAGES, SCREEN><<<grid, TILE + 32, smem, stream>>>(
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
         post_exp_tau, status, pad);
     BATS_CUDA(cudaGetLastError());
@@ -442,20 +468,20 @@ static int launch_forward(const void* events, const int* ev_count, long long ev_
 
 // Work-queue launch: the order kernel, then a grid of as many CTAs of the persistent kernel as are resident
 // at once on this GPU (at most one per work item).
-template <int TILE, int SEV, int STAGES>
+template <int TILE, int SEV, int STAGES, bool SCREEN>
 static int launch_forward_queue(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld,
                                 int batch, int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a,
                                 float* x, float* times, float* post_exp_tau, int* status, int pad, int* order,
                                 int* head, cudaStream_t stream) {
     using Smem = StreamSmem<TILE, SEV, STAGES>;
     const size_t smem = mailbox_offset<Smem>() + sizeof(ItemMailbox);
-    const void* kern = (const void*)lif_fc_forward_queue_kernel<TILE, SEV, STAGES>;
+    const void* kern = (const void*)lif_fc_forward_queue_kernel<TILE, SEV, STAGES, SCREEN>;
     BATS_CUDA((cudaError_t)max_dynamic_smem_set(kern, (int)smem));
     int dev = 0, n_sm = 0, per_sm = 0;
     BATS_CUDA(cudaGetDevice(&dev));
     BATS_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
-    BATS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lif_fc_forward_queue_kernel<TILE, SEV, STAGES>,
-                                                            TILE + 32, smem));
+    BATS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, lif_fc_forward_queue_kernel<TILE, SEV, STAGES, SCREEN>, TILE + 32, smem));
     const int n_tiles = (n_post + TILE - 1) / TILE;
     BATS_REQUIRE((long long)batch * n_tiles < (1LL << 31), BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc_queue: batch * post-neuron tiles must stay below 2^31");
@@ -463,11 +489,22 @@ static int launch_forward_queue(const void* events, const int* ev_count, long lo
     const int grid = (int)std::min<long long>(n_items, (long long)std::max(1, per_sm) * std::max(1, n_sm));
     work_order_kernel<<<1, 1024, 0, stream>>>(ev_count, batch, head, order);
     BATS_CUDA(cudaGetLastError());
-    lif_fc_forward_queue_kernel<TILE, SEV, STAGES><<<grid, TILE + 32, smem, stream>>>(
+    lif_fc_forward_queue_kernel<TILE, SEV, STAGES, SCREEN><<<grid, TILE + 32, smem, stream>>>(
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
         post_exp_tau, status, pad, order, head, n_tiles, n_items);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
+}
+
+// The stage-screen choice (a run-time flag) mapped onto the kernel template.
+template <int TILE, int SEV, int STAGES, typename... Args>
+static int launch_tile(bool screen, Args... args) {
+    return screen ? launch_forward<TILE, SEV, STAGES, true>(args...) : launch_forward<TILE, SEV, STAGES, false>(args...);
+}
+template <int TILE, int SEV, int STAGES, typename... Args>
+static int launch_queue(bool screen, Args... args) {
+    return screen ? launch_forward_queue<TILE, SEV, STAGES, true>(args...)
+                  : launch_forward_queue<TILE, SEV, STAGES, false>(args...);
 }
 
 SolveConst make_solve_const(float c, float dtt, float tau, float max_sim) {
@@ -492,7 +529,8 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0 && ld >= n_post && ld % 4 == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc: bad shape (ld must be >= n_post and a multiple of 4)");
     const int pad = (algo & BATS_FWD_NO_PAD) ? 0 : 1;
-    algo &= ~BATS_FWD_NO_PAD;
+    const bool screen = (algo & BATS_FWD_STAGE_SCREEN) != 0;
+    algo &= ~(BATS_FWD_NO_PAD | BATS_FWD_STAGE_SCREEN);
     BATS_REQUIRE(algo >= BATS_FWD_AUTO && algo <= BATS_FWD_TILE64, BATS_ERR_BAD_SHAPE, "lif_forward_fc: unknown algo");
     if (batch == 0 || n_post == 0) return BATS_OK;
     BATS_REQUIRE(events && ev_count && weights_t && n_spikes && a && x && times && post_exp_tau, BATS_ERR_NULL,
@@ -507,17 +545,17 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
     int* status = nullptr;
     BATS_CUDA((cudaError_t)bats::device_status(&status));
     if (algo == BATS_FWD_TILE64)
-        return bats::launch_forward<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+        return bats::launch_tile<64, 16, 6>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                               n_spikes, a, x, times, post_exp_tau, status, pad, stream);
     if (n_post <= 32)
-        return bats::launch_forward<32, 16, 8>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+        return bats::launch_tile<32, 16, 8>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                                n_spikes, a, x, times, post_exp_tau, status, pad, stream);
     if (n_post <= 64)
-        return bats::launch_forward<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+        return bats::launch_tile<64, 16, 6>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                               n_spikes, a, x, times, post_exp_tau, status, pad, stream);
     // 8-event stages: half the shared memory of 16-event stages, so 7 CTAs (28 consumer warps) fit on an SM
     // instead of 4, and a replay after a possible crossing covers fewer events.
-    return bats::launch_forward<128, 8, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+    return bats::launch_tile<128, 8, 6>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                           n_spikes, a, x, times, post_exp_tau, status, pad, stream);
 }
 
@@ -559,7 +597,8 @@ extern "C" int bats_lif_forward_fc_queue(const void* events, const int* ev_count
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0 && ld >= n_post && ld % 4 == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc_queue: bad shape (ld must be >= n_post and a multiple of 4)");
     const int pad = (algo & BATS_FWD_NO_PAD) ? 0 : 1;
-    algo &= ~BATS_FWD_NO_PAD;
+    const bool screen = (algo & BATS_FWD_STAGE_SCREEN) != 0;
+    algo &= ~(BATS_FWD_NO_PAD | BATS_FWD_STAGE_SCREEN);
     BATS_REQUIRE(algo == BATS_FWD_AUTO || algo == BATS_FWD_TILE || algo == BATS_FWD_TILE64, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc_queue: algo must be BATS_FWD_AUTO, BATS_FWD_TILE or BATS_FWD_TILE64");
     if (batch == 0 || n_post == 0) return BATS_OK;
@@ -575,13 +614,13 @@ extern "C" int bats_lif_forward_fc_queue(const void* events, const int* ev_count
     int* head = reinterpret_cast<int*>(workspace);
     int* order = reinterpret_cast<int*>(reinterpret_cast<char*>(workspace) + 256);
     if (algo == BATS_FWD_TILE64 || (n_post > 32 && n_post <= 64))
-        return bats::launch_forward_queue<64, 16, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post,
+        return bats::launch_queue<64, 16, 6>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post,
                                                     sk, n_spikes, a, x, times, post_exp_tau, status, pad, order, head,
                                                     stream);
     if (n_post <= 32)
-        return bats::launch_forward_queue<32, 16, 8>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post,
+        return bats::launch_queue<32, 16, 8>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post,
                                                     sk, n_spikes, a, x, times, post_exp_tau, status, pad, order, head,
                                                     stream);
-    return bats::launch_forward_queue<128, 8, 6>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
+    return bats::launch_queue<128, 8, 6>(screen, events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                                 n_spikes, a, x, times, post_exp_tau, status, pad, order, head, stream);
 }

@@ -14,61 +14,128 @@
 namespace bats {
 
 constexpr int CONV_WARPS = 4;
+// Per-sample neuron counts are kept in shared memory up to this many neurons (with the event windows below,
+// 48 KB in all, no opt-in needed); larger layers keep them in the output counts array.
+constexpr int CONV_SMEM_NEURONS = 8000;  // 32 000 B of counts + 16 400 B of windows <= 48 KB
+constexpr int CONV_WINDOW = 1024;  // events per shared-memory window (two windows: double buffering)
 
+// One CTA per sample. The sample's events are staged through shared memory in windows of CONV_WINDOW
+// (indices and times, coalesced loads by warps 1..3, one window ahead of the ranking). Warp 0 ranks each
+// window's events in order of appearance, 32 at a time (events of the same neuron ranked by
+// __match_any_sync), writing each spike into its slot, with the per-neuron counts in shared memory when
+// SMEM_COUNTS: a 32-event step then waits on shared memory only. Finally all warps set the slots past each
+// neuron's count to +inf (row by row, contiguous stores) and write the counts.
+template <bool SMEM_COUNTS>
 __global__ void __launch_bounds__(CONV_WARPS * 32)
 events_to_trains_kernel(const int* __restrict__ indices, const float* __restrict__ times,
                         const int* __restrict__ offsets, int batch, int max_events, int n_neurons, int k_cap,
                         float* __restrict__ out_times, int* __restrict__ out_counts, int* __restrict__ overflow) {
-    const int lane = threadIdx.x & 31;
-    const int s = blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);
-    if (s >= batch) return;
+    extern __shared__ int s_cnt[];
+    __shared__ int w_idx[2][CONV_WINDOW];
+    __shared__ float w_t[2][CONV_WINDOW];
+    __shared__ int s_stop;  // the sample ended (negative or out-of-range index) inside the current window
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int s = blockIdx.x;
     const long long tb = (long long)s * n_neurons * k_cap;
-    int* cnt = out_counts + (long long)s * n_neurons;
-    for (long long q = lane; q < (long long)n_neurons * k_cap; q += 32) out_times[tb + q] = BATS_INF;
-    for (int q = lane; q < n_neurons; q += 32) cnt[q] = 0;
-    __syncwarp();
+    int* cnt = SMEM_COUNTS ? s_cnt : out_counts + (long long)s * n_neurons;
+    for (int q = tid; q < n_neurons; q += blockDim.x) cnt[q] = 0;
     // Padded rows (B, max_events), or with offsets the events offsets[s] .. offsets[s + 1] of a flat list.
     const long long first = offsets ? (long long)offsets[s] : (long long)s * max_events;
     const int n_ev = offsets ? offsets[s + 1] - offsets[s] : max_events;
     const int* idx = indices + first;
     const float* tm = times + first;
-    int dropped = 0;
-    for (int m0 = 0; m0 < n_ev; m0 += 32) {
-        const int m = m0 + lane;
-        int j = m < n_ev ? idx[m] : -1;
-        // The sample ends at its first negative index.
-        const unsigned neg = __ballot_sync(0xffffffffu, j < 0 || j >= n_neurons);
-        const int stop = neg ? __ffs(neg) - 1 : 32;
-        const bool valid = lane < stop;
-        if (!valid) j = -1 - lane;  // distinct keys so that invalid lanes never match
-        const unsigned peers = __match_any_sync(0xffffffffu, j);
-        const int rank = __popc(peers & lanemask_lt());
-        int base = 0;
-        if (valid && rank == 0) base = cnt[j];
-        base = __shfl_sync(0xffffffffu, base, __ffs(peers) - 1);
-        if (valid) {
-            const int slot = base + rank;
-            if (slot < k_cap)
-                out_times[tb + (long long)j * k_cap + slot] = tm[m];
-            else
-                ++dropped;
-            if (rank == 0) cnt[j] = min(base + __popc(peers), k_cap);
-        }
-        __syncwarp();
-        if (stop < 32) break;
+    const int n_win = (n_ev + CONV_WINDOW - 1) / CONV_WINDOW;
+    // Window 0, loaded by every thread.
+    for (int q = tid; q < min(n_ev, CONV_WINDOW); q += blockDim.x) {
+        w_idx[0][q] = idx[q];
+        w_t[0][q] = tm[q];
     }
-    for (int o = 16; o >= 1; o >>= 1) dropped += __shfl_xor_sync(0xffffffffu, dropped, o);
-    if (lane == 0 && dropped && overflow) atomicAdd(overflow, dropped);
+    if (tid == 0) s_stop = 0;
+    __syncthreads();
+    int dropped = 0;
+    for (int w = 0; w < n_win; ++w) {
+        const int buf = w & 1;
+        const int m_base = w * CONV_WINDOW;
+        const int cnt_w = min(CONV_WINDOW, n_ev - m_base);
+        if (warp == 0) {
+            for (int m0 = 0; m0 < cnt_w; m0 += 32) {
+                const int m = m0 + lane;
+                int j = m < cnt_w ? w_idx[buf][m] : -1;
+                const float t = m < cnt_w ? w_t[buf][m] : 0.0f;
+                // The sample ends at its first negative (or out-of-range) index.
+                const unsigned neg = __ballot_sync(0xffffffffu, j < 0 || j >= n_neurons);
+                const int stop = neg ? __ffs(neg) - 1 : 32;
+                const bool valid = lane < stop;
+                if (!valid) j = -1 - lane;  // distinct keys so that invalid lanes never match
+                const unsigned peers = __match_any_sync(0xffffffffu, j);
+                const int rank = __popc(peers & lanemask_lt());
+                int base = 0;
+                if (valid && rank == 0) base = cnt[j];
+                base = __shfl_sync(0xffffffffu, base, __ffs(peers) - 1);
+                if (valid) {
+                    const int slot = base + rank;
+                    if (slot < k_cap)
+                        out_times[tb + (long long)j * k_cap + slot] = t;
+                    else
+                        ++dropped;
+                    if (rank == 0) cnt[j] = min(base + __popc(peers), k_cap);
+                }
+                __syncwarp();
+                if (stop < 32) {
+                    if (lane == 0) s_stop = 1;
+                    break;
+                }
+            }
+        } else if (w + 1 < n_win) {
+            // Warps 1..3: the next window into the other buffer.
+            const int nb = m_base + CONV_WINDOW;
+            const int cnt_n = min(CONV_WINDOW, n_ev - nb);
+            for (int q = tid - 32; q < cnt_n; q += blockDim.x - 32) {
+                w_idx[buf ^ 1][q] = idx[nb + q];
+                w_t[buf ^ 1][q] = tm[nb + q];
+            }
+        }
+        __syncthreads();
+        if (s_stop) break;
+    }
+    if (warp == 0) {
+        for (int o = 16; o >= 1; o >>= 1) dropped += __shfl_xor_sync(0xffffffffu, dropped, o);
+        if (lane == 0 && dropped && overflow) atomicAdd(overflow, dropped);
+    }
+    // +inf past each neuron's spikes; the ranking above wrote only the slots below the counts.
+    for (int j = warp; j < n_neurons; j += CONV_WARPS) {
+        float* row = out_times + tb + (long long)j * k_cap;
+        for (int k = cnt[j] + lane; k < k_cap; k += 32) row[k] = BATS_INF;
+    }
+    if (SMEM_COUNTS)
+        for (int q = tid; q < n_neurons; q += blockDim.x) out_counts[(long long)s * n_neurons + q] = cnt[q];
+}
+
+static int launch_events_to_trains(const int* indices, const float* times, const int* offsets, int batch,
+                                   int max_events, int n_neurons, int k_cap, float* out_times, int* out_counts,
+                                   int* overflow, cudaStream_t stream) {
+    if (n_neurons <= CONV_SMEM_NEURONS)
+        events_to_trains_kernel<true><<<batch, CONV_WARPS * 32, (size_t)n_neurons * sizeof(int), stream>>>(
+            indices, times, offsets, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+    else
+        events_to_trains_kernel<false><<<batch, CONV_WARPS * 32, 0, stream>>>(
+            indices, times, offsets, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
 }
 
 // Largest per-neuron spike count of each sample (the K the reference derives on the host).
+// Warp per sample; the counts live in a warp-private slice of shared memory when SMEM_COUNTS (else in the
+// caller's scratch).
+template <bool SMEM_COUNTS>
 __global__ void __launch_bounds__(CONV_WARPS * 32)
 max_per_neuron_kernel(const int* __restrict__ indices, int batch, int max_events, int n_neurons,
                       int* __restrict__ scratch_counts, int* __restrict__ out_max) {
+    extern __shared__ int s_cnt[];
     const int lane = threadIdx.x & 31;
     const int s = blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);
     if (s >= batch) return;
-    int* cnt = scratch_counts + (long long)s * n_neurons;
+    int* cnt = SMEM_COUNTS ? s_cnt + (threadIdx.x >> 5) * n_neurons : scratch_counts + (long long)s * n_neurons;
     for (int q = lane; q < n_neurons; q += 32) cnt[q] = 0;
     __syncwarp();
     const int* idx = indices + (long long)s * max_events;
@@ -106,11 +173,8 @@ extern "C" int bats_events_to_trains(const int* indices, const float* times, int
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(out_times && out_counts && (max_events == 0 || (indices && times)), BATS_ERR_NULL,
                  "events_to_trains: null pointer");
-    const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
-    bats::events_to_trains_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
-        indices, times, nullptr, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
-    BATS_CUDA(cudaGetLastError());
-    return BATS_OK;
+    return bats::launch_events_to_trains(indices, times, nullptr, batch, max_events, n_neurons, k_cap, out_times,
+                                         out_counts, overflow, stream);
 }
 
 extern "C" int bats_events_to_trains_csr(const int* indices, const float* times, const int* offsets, int batch,
@@ -120,11 +184,8 @@ extern "C" int bats_events_to_trains_csr(const int* indices, const float* times,
     if (batch == 0 || n_neurons == 0) return BATS_OK;
     BATS_REQUIRE(indices && times && offsets && out_times && out_counts, BATS_ERR_NULL,
                  "events_to_trains_csr: null pointer");
-    const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
-    bats::events_to_trains_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
-        indices, times, offsets, batch, 0, n_neurons, k_cap, out_times, out_counts, overflow);
-    BATS_CUDA(cudaGetLastError());
-    return BATS_OK;
+    return bats::launch_events_to_trains(indices, times, offsets, batch, 0, n_neurons, k_cap, out_times, out_counts,
+                                         overflow, stream);
 }
 
 extern "C" int bats_events_max_per_neuron(const int* indices, int batch, int max_events, int n_neurons,
@@ -135,8 +196,13 @@ extern "C" int bats_events_max_per_neuron(const int* indices, int batch, int max
     BATS_REQUIRE(scratch_counts && out_max && (max_events == 0 || indices), BATS_ERR_NULL,
                  "events_max_per_neuron: null pointer");
     const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
-    bats::max_per_neuron_kernel<<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(indices, batch, max_events, n_neurons,
-                                                                              scratch_counts, out_max);
+    if (n_neurons * bats::CONV_WARPS <= 12288)  // 48 KB of warp-private counts
+        bats::max_per_neuron_kernel<true><<<blocks, bats::CONV_WARPS * 32,
+                                            (size_t)n_neurons * bats::CONV_WARPS * sizeof(int), stream>>>(
+            indices, batch, max_events, n_neurons, scratch_counts, out_max);
+    else
+        bats::max_per_neuron_kernel<false><<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
+            indices, batch, max_events, n_neurons, scratch_counts, out_max);
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -157,13 +157,14 @@ def get_sorted_spikes_indices(spike_times_per_neuron, n_spike_per_neuron):
 
 FWD_AUTO, FWD_TILE, FWD_LANES, FWD_TILE64 = 0, 1, 2, 3
 FWD_NO_PAD = 0x100  # OR-ed into the algo: no +inf past the spike counts (outputs read only below them)
+FWD_STAGE = 0x200  # OR-ed into a tile or queue algo: one no-crossing test per neuron and stage first (quiet layers)
 # Python-side choices that route to bats_lif_forward_fc_queue (one persistent launch over a work queue of
 # (sample, tile) items, longest samples first), with the tile width of FWD_TILE or FWD_TILE64.
 FWD_QUEUE, FWD_QUEUE64 = 4, 5
 
 
 def is_queue_algo(algo: int) -> bool:
-    return (algo & ~FWD_NO_PAD) in (FWD_QUEUE, FWD_QUEUE64)
+    return (algo & ~(FWD_NO_PAD | FWD_STAGE)) in (FWD_QUEUE, FWD_QUEUE64)
 
 
 def queue_workspace_bytes(batch: int) -> int:
@@ -179,9 +180,9 @@ def forward_fc_call(events: Events, weights_t, n_post: int, k_post: int, c, dtt,
               n_post, k_post, float(c), float(dtt), float(tau32), float(np.float32(max_simulation)), ptr(n), ptr(a),
               ptr(x), ptr(t), ptr(z))
     if is_queue_algo(algo):
-        tile = FWD_TILE64 if (algo & ~FWD_NO_PAD) == FWD_QUEUE64 else FWD_TILE
-        call("bats_lif_forward_fc_queue", *common, tile | (algo & FWD_NO_PAD), workspace, int(workspace_bytes),
-             stream)
+        tile = FWD_TILE64 if (algo & ~(FWD_NO_PAD | FWD_STAGE)) == FWD_QUEUE64 else FWD_TILE
+        call("bats_lif_forward_fc_queue", *common, tile | (algo & (FWD_NO_PAD | FWD_STAGE)), workspace,
+             int(workspace_bytes), stream)
     else:
         call("bats_lif_forward_fc_algo", *common, int(algo), stream)
 
@@ -191,8 +192,9 @@ def lif_forward_fc(events: Events, weights_t, n_post: int, k_post: int, tau_s: f
     """FC LIF forward (replaces get_spike_weights + compute_spike_times,
     bats/CudaKernels/Wrappers/Inference/compute_spike_times.py:11-32). Returns n, a, x, times, post_exp_tau.
     algo: FWD_TILE (CTA per neuron tile and sample), FWD_LANES (warp per neuron and sample, 32 events in
-    parallel), FWD_QUEUE / FWD_QUEUE64 (persistent CTAs over a longest-first work queue) or FWD_AUTO; all give
-    identical results."""
+    parallel), FWD_QUEUE / FWD_QUEUE64 (persistent CTAs over a longest-first work queue) or FWD_AUTO, the tile
+    and queue kinds optionally with FWD_STAGE (one no-crossing test per stage first); all give identical
+    results."""
     B = events.batch
     tau32, c, dtt = lif_constants(tau_s, theta, delta_theta)
     dev = events.events.device

@@ -284,7 +284,7 @@ class InferenceServer:
                         trial[li] = algo
                         self._layers(lane, b, trial, s, only=li)
 
-                    cands = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES}
+                    cands = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES, "tile_stage": K.FWD_TILE | K.FWD_STAGE}
                     if spec.n_neurons > 64:
                         cands["tile64"] = K.FWD_TILE64
                     best = tuner.pick("fc_forward", shape, {k: (lambda a=a: run(a)) for k, a in cands.items()})

@@ -224,7 +224,8 @@ class FCTrainStep:
                 fwd[f"{tag}.forward"](s)
                 self.fwd_algo[li] = saved
 
-            algos = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES, "queue": K.FWD_QUEUE}
+            algos = {"tile": K.FWD_TILE, "lanes": K.FWD_LANES, "queue": K.FWD_QUEUE,
+                     "tile_stage": K.FWD_TILE | K.FWD_STAGE, "queue_stage": K.FWD_QUEUE | K.FWD_STAGE}
             if spec.n_neurons > 64:
                 algos["tile64"] = K.FWD_TILE64
                 algos["queue64"] = K.FWD_QUEUE64

@@ -348,7 +348,8 @@ def profile_kernels():
     entry point: pre-exponentials, the intensity encoder, event-list conversion of a 16-request serving
     batch, the TTFS and spike-time losses, untiled Adam, NAdam, both synaptic-scaling regularizers,
     transpose, add_deltas, the generic backward prep (reset errors, factors), the conv backward for filters
-    too large for shared memory, and the allocation-free gradient."""
+    too large for shared memory, the allocation-free gradient, and one 16-request batch of the serving loop
+    (700-512-512-20 network, one foreign call: conversion, then per layer the sort and the forward)."""
     import ctypes
 
     import torch
@@ -429,6 +430,11 @@ def profile_kernels():
         if st != 0:
             raise RuntimeError(lib.bats_last_error().decode())
     calls.append(("weights_gradient_mean_noalloc", noalloc))
+    from bats_gb300.serving import InferenceServer, make_network, make_requests
+    sws, sspecs = make_network()
+    server = InferenceServer(sws, sspecs, 700, 5000, k_in=32, max_batch=16, max_lanes=1)
+    sreqs = make_requests(16, seed=7)
+    calls.append(("serve_batch_16", lambda: server.infer(sreqs)))
 
     for _, fn in calls:  # warm-up: module load, first-call set-up
         fn()
@@ -813,6 +819,7 @@ def main():
                    "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (512 MB write)",
                    "cuda_graph": lit["graph"]},
         "roofline": lit["roofline"], "e2e": lit["e2e"], "gpu_launches": lit["gpu_launches"], "clocks": lit["clocks"],
+        "autotuned": lit["autotuned"],
         "cpu_baseline": cb, "spikes_per_layer": lit["spikes_per_layer_last_step"], "kernels_ms": lit["kernels_ms"],
         "active": act, "serving": serving, "conv": conv, "batching": batching,
     }

@@ -108,6 +108,12 @@ int bats_intensity_to_spike_times(const unsigned char* pixels, int batch, int n_
  * set to +inf, for outputs read only below the spike counts (bats_sort_events_counted,
  * bats_backward_prep_counted, bats_weights_gradient, bats_pre_errors): the hidden layers of a train step. */
 #define BATS_FWD_NO_PAD 0x100
+/* OR-ed into `algo` (tile kernels, also those of bats_lif_forward_fc_queue; ignored by BATS_FWD_LANES): each
+ * full stage of events first runs the accumulation alone, with one test per neuron and stage that rules out a
+ * crossing after any of its events from the smallest a and the largest b of its states (the membrane bound
+ * b/x - a/x^2 < theta/tau from the stage's first event on); only stages that fail it get the per-event tests.
+ * Faster where most neurons stay far below threshold; results are bit-identical. */
+#define BATS_FWD_STAGE_SCREEN 0x200
 int bats_lif_forward_fc_default_algo(int batch, int n_post, int ev_cap);
 int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long ev_cap, const float* weights_t,
                              int ld, int batch, int n_post, int k_post, float c, float delta_theta_tau, float tau,
@@ -120,7 +126,7 @@ int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long 
  * items from the queue, longest samples first, each producer warp streaming its next item while the consumers
  * finish the current one. Outputs, arguments and results are those of bats_lif_forward_fc_algo (bit-identical);
  * algo is BATS_FWD_AUTO or BATS_FWD_TILE (tile width by n_post) or BATS_FWD_TILE64, optionally OR-ed with
- * BATS_FWD_NO_PAD. The workspace (16-byte aligned, bats_lif_forward_fc_queue_workspace_bytes(batch) bytes) must
+ * BATS_FWD_NO_PAD and BATS_FWD_STAGE_SCREEN. The workspace (16-byte aligned, bats_lif_forward_fc_queue_workspace_bytes(batch) bytes) must
  * not be used by another launch until this one ends. Replaces the same reference wrappers as
  * bats_lif_forward_fc (get_spike_weights.py:9-18, compute_spike_times.py:11-32); the reference runs one thread
  * per (sample, neuron) with no scheduling of its own. */
@@ -160,13 +166,14 @@ int bats_pool_forward(const int* n_spikes, const float* times, int batch, int X,
 int bats_events_to_trains(const int* indices, const float* times, int batch, int max_events, int n_neurons,
                           int k_cap, float* out_times, int* out_counts, int* overflow, cudaStream_t stream);
 
-/* Largest per-neuron spike count of each sample of an event list (the K of convert_to_spike_per_neuron,
- * Wrappers/Inference/convert_to_spike_per_neuron.py:11-18), using scratch_counts (B, N). */
 /* bats_events_to_trains over a flat event list: sample s owns events offsets[s] .. offsets[s + 1] - 1
  * (offsets: batch + 1 ints, device). No counterpart in the reference (its input is padded). */
 int bats_events_to_trains_csr(const int* indices, const float* times, const int* offsets, int batch, int n_neurons,
                               int k_cap, float* out_times, int* out_counts, int* overflow, cudaStream_t stream);
 
+/* Largest per-neuron spike count of each sample of an event list (the K of convert_to_spike_per_neuron,
+ * Wrappers/Inference/convert_to_spike_per_neuron.py:11-18). scratch_counts (B, N) holds the running counts
+ * when 4 * N ints do not fit the kernel's shared memory (N > 3072); it is left untouched otherwise. */
 int bats_events_max_per_neuron(const int* indices, int batch, int max_events, int n_neurons, int* scratch_counts,
                                int* out_max, cudaStream_t stream);
 

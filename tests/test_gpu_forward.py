@@ -250,7 +250,8 @@ def _both_algos(t, W, tau_s, theta, dtheta, K_post, max_sim=np.inf):
     ev = K.sort_events(tt, np.float32(tau_s), np.float32(2 * tau_s))
     wt = K.transpose_weights(torch.tensor(W, device="cuda"))
     outs = []
-    for algo in (K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64, K.FWD_QUEUE, K.FWD_QUEUE64):
+    for algo in (K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64, K.FWD_QUEUE, K.FWD_QUEUE64, K.FWD_TILE | K.FWD_STAGE,
+                 K.FWD_TILE64 | K.FWD_STAGE, K.FWD_QUEUE | K.FWD_STAGE):
         o = K.lif_forward_fc(ev, wt, W.shape[0], K_post, tau_s, theta, dtheta, max_sim, algo=algo)
         outs.append([v.cpu().numpy() for v in o])
     return outs
@@ -266,10 +267,12 @@ def _assert_identical(p, q, what):
         assert np.array_equal(p[i].view(np.uint32), q[i].view(np.uint32)), f"{what}: {name}"
 
 
-@pytest.mark.parametrize("case", ["small", "mnist_active", "long_narrow", "long_wide", "cap_and_cut"])
+@pytest.mark.parametrize("case", ["small", "mnist_active", "long_narrow", "long_wide", "cap_and_cut", "mnist_literal",
+                                  "quiet_and_spiking"])
 def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
-    """The warp-per-neuron forward (32 events per step, FWD_LANES), the 64-neuron-tile variant and the
-    persistent work-queue kernel (both tile widths) are bit-identical to the tile kernel on
+    """The warp-per-neuron forward (32 events per step, FWD_LANES), the 64-neuron-tile variant, the
+    persistent work-queue kernel (both tile widths) and the per-stage-screen variants (FWD_STAGE: tile, 64-neuron
+    tiles, queue) are bit-identical to the tile kernel on
     short and long event streams, narrow and wide layers, a full spike buffer and a max_simulation cut; on
     a long stream it also matches the reference kernels."""
     rng = np.random.default_rng(5)
@@ -286,22 +289,36 @@ def test_event_parallel_kernel_matches_tile_kernel(cuda, case):
         t, n_in = multi_spike_input(2, 700, 20, 0.2, seed=4, p_silent=0.1)
         W = ((rng.normal(0, 1, (n_post, 700)) + 1.5) / np.sqrt(700)).astype(np.float32)
         args = (0.13, 1.0, 1.0, 30, np.inf)
+    elif case == "mnist_literal":  # the hidden layer of the literal configuration: (almost) no neuron spikes
+        t, n_in = mnist_like_input(64, seed=7)
+        W = rng.normal(0, 1 / np.sqrt(784), (800, 784)).astype(np.float32)
+        args = (0.13, 1.0, 1.0, 30, 0.2)
+    elif case == "quiet_and_spiking":  # most stages pass the per-stage screen, some neurons spike late
+        t, n_in = multi_spike_input(8, 300, 4, 0.1, seed=8, p_silent=0.3)
+        W = ((rng.normal(0, 1, (200, 300)) + np.linspace(-0.5, 1.5, 200)[:, None]) / np.sqrt(300)).astype(np.float32)
+        args = (0.13, 1.0, 1.0, 30, np.inf)
     else:
         t, n_in = multi_spike_input(3, 50, 6, 0.2, seed=6, p_silent=0.0)
         W = np.abs(rng.normal(0, 1, (40, 50))).astype(np.float32)
         args = (0.1, 0.05, 0.05, 4, 0.12)
-    tile, lanes, tile64, queue, queue64 = _both_algos(t, W, *args)
-    assert tile[0].sum() > 0, "the case should spike"
+    tile, lanes, tile64, queue, queue64, stage, stage64, queue_stage = _both_algos(t, W, *args)
+    if case != "mnist_literal":
+        assert tile[0].sum() > 0, "the case should spike"
+    if case == "quiet_and_spiking":
+        assert 0 < (tile[0] > 0).mean() < 0.9, "some neurons should spike and others stay quiet"
     _assert_identical(tile, lanes, case)
     _assert_identical(tile, tile64, case + " (64-neuron tiles)")
     _assert_identical(tile, queue, case + " (work queue)")
     _assert_identical(tile, queue64, case + " (work queue, 64-neuron tiles)")
+    _assert_identical(tile, stage, case + " (per-stage screen)")
+    _assert_identical(tile, stage64, case + " (per-stage screen, 64-neuron tiles)")
+    _assert_identical(tile, queue_stage, case + " (work queue, per-stage screen)")
     if case == "long_narrow":
         ref = run_ref(t, n_in, W, *args)
         check_against(lanes, ref, None, what="lanes vs reference kernels")
 
 
-@pytest.mark.parametrize("algo", [K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64, K.FWD_QUEUE])
+@pytest.mark.parametrize("algo", [K.FWD_TILE, K.FWD_LANES, K.FWD_TILE64, K.FWD_QUEUE, K.FWD_TILE | K.FWD_STAGE])
 def test_no_pad_flag_leaves_slots_past_counts(cuda, algo):
     """BATS_FWD_NO_PAD: counts and every value below them are those of the padded forward, and the slots
     past the counts keep what the buffers held (here a sentinel)."""
@@ -360,11 +377,10 @@ def test_work_queue_forward_on_uneven_batch(cuda, n_post):
     outs = (torch.empty((333, n_post), dtype=torch.int32, device="cuda"),
             *(torch.empty((333, n_post, 8), device="cuda") for _ in range(4)))
     tau32, c, dtt = K.lif_constants(0.13, 0.2, 0.2)
-    for rep in range(2):
+    for rep, algo in enumerate((K.FWD_QUEUE, K.FWD_QUEUE, K.FWD_QUEUE | K.FWD_STAGE)):
         for o in outs:
             o.fill_(-1)
-        K.forward_fc_call(ev, wt, n_post, 8, c, dtt, tau32, 0.2, outs, K.FWD_QUEUE, stream_ptr(), ptr(ws),
-                          ws.numel())
+        K.forward_fc_call(ev, wt, n_post, 8, c, dtt, tau32, 0.2, outs, algo, stream_ptr(), ptr(ws), ws.numel())
         _assert_identical(tile, [v.cpu().numpy() for v in outs], f"work queue, call {rep + 1}")
     K.forward_fc_call(ev, wt, n_post, 8, c, dtt, tau32, 0.2, outs, K.FWD_QUEUE | K.FWD_NO_PAD, stream_ptr(),
                       ptr(ws), ws.numel())

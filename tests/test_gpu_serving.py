@@ -42,6 +42,44 @@ def test_event_list_conversion_known_answer(cuda):
     assert int(ovf) == int(np.maximum(en - 4, 0).sum())
 
 
+def test_event_list_conversion_multi_window(cuda):
+    """Samples longer than the conversion kernel's 1024-event shared-memory windows: ends inside the second
+    window, exactly at a window boundary, at the first event, and full rows; the flat (CSR) form with uneven
+    lengths; and a layer too wide for shared-memory counts (9000 neurons). All equal the oracle."""
+    from bats_gb300._lib import call, ptr, stream_ptr
+    rng = np.random.default_rng(4)
+    idx = rng.integers(0, 700, (5, 3500)).astype(np.int32)
+    idx[1, 1500:] = -1
+    idx[2, 1024:] = -1
+    idx[3, :] = -1
+    tm = np.sort(rng.uniform(0, 0.2, (5, 3500)), axis=1).astype(np.float32)
+    idx_d, tm_d = torch.tensor(idx, device="cuda"), torch.tensor(tm, device="cuda")
+    t, n = K.convert_to_spike_per_neuron(idx_d, tm_d, 700)
+    et, en = R.convert_to_spike_per_neuron(idx, tm, 700)
+    np.testing.assert_array_equal(n.cpu().numpy(), en)
+    np.testing.assert_array_equal(t.cpu().numpy(), et.astype(np.float32))
+    # Flat list: each sample's valid events back to back, offsets between them.
+    lens = [int((row >= 0).cumprod().sum()) for row in idx]
+    flat_i = np.concatenate([idx[q, :m] for q, m in enumerate(lens)]).astype(np.int32)
+    flat_t = np.concatenate([tm[q, :m] for q, m in enumerate(lens)]).astype(np.float32)
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    kc = int(en.max())
+    ct = torch.empty((5, 700, kc), device="cuda")
+    cn = torch.empty((5, 700), dtype=torch.int32, device="cuda")
+    fi, ft, fo = (torch.tensor(v, device="cuda") for v in (flat_i, flat_t, off))
+    call("bats_events_to_trains_csr", ptr(fi), ptr(ft), ptr(fo), 5, 700, kc, ptr(ct), ptr(cn), None, stream_ptr())
+    np.testing.assert_array_equal(cn.cpu().numpy(), en)
+    np.testing.assert_array_equal(ct.cpu().numpy(), et.astype(np.float32))
+    # Counts in global memory (more neurons than the shared-memory counts hold).
+    idx2 = rng.integers(0, 9000, (3, 2600)).astype(np.int32)
+    idx2[0, 2000:] = -1
+    tm2 = np.sort(rng.uniform(0, 0.2, (3, 2600)), axis=1).astype(np.float32)
+    t2, n2 = K.convert_to_spike_per_neuron(torch.tensor(idx2, device="cuda"), torch.tensor(tm2, device="cuda"), 9000)
+    et2, en2 = R.convert_to_spike_per_neuron(idx2, tm2, 9000)
+    np.testing.assert_array_equal(n2.cpu().numpy(), en2)
+    np.testing.assert_array_equal(t2.cpu().numpy(), et2.astype(np.float32))
+
+
 def test_same_result_alone_and_in_the_mix(cuda):
     ws, specs = net()
     server = InferenceServer(ws, specs, 700, 5000, k_in=32, max_batch=32, max_lanes=3)
