@@ -1,5 +1,6 @@
 // Error reporting and per-device launch attributes shared by the C-ABI entry points.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include "abi_util.h"
@@ -31,6 +32,21 @@ int max_dynamic_smem_set(const void* func, int bytes) {
     if (e != cudaSuccess) return (int)e;
     if (used < 64) cache[used++] = Entry{func, dev, bytes};
     return (int)cudaSuccess;
+}
+
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("BATS_GB300_PDL");
+        return v && v[0] == '1' && v[1] == '\0';
+    }();
+    return on;
+}
+
+int pdl_attribute(cudaLaunchAttribute* attr) {
+    if (!pdl_enabled()) return 0;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    return 1;
 }
 
 // Status word of bounded device-side waits: a kernel that gives up waiting ORs BATS_STATUS_TIMEOUT

@@ -16,6 +16,14 @@
 
 namespace bats {
 
+// First statement of every kernel (programmatic dependent launch): let the next kernel in the stream launch
+// its CTAs now (they wait in their own prologue), then wait until the grids this one depends on have
+// completed and their writes are visible. Both are no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_prologue() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // One pre-synaptic spike of one sample, sorted by time. 16 bytes so that a warp reads it as a
 // single broadcast vector load from shared memory.
 struct __align__(16) Event {

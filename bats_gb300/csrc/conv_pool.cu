@@ -40,6 +40,7 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
                                     int w_in_smem, int* __restrict__ n_spikes,
                                     float* __restrict__ a_out, float* __restrict__ x_out, float* __restrict__ t_out,
                                     float* __restrict__ z_out) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ConvEvent* sev = reinterpret_cast<ConvEvent*>(smem_raw);
     int* swarp = reinterpret_cast<int*>(sev + CONV_CHUNK);
@@ -139,6 +140,7 @@ __global__ void conv_backward_kernel(const Event* __restrict__ ev, const int* __
                                      const float* __restrict__ post_t, const float2* __restrict__ tab,
                                      const int* __restrict__ nvalid, int k_post, float tau_s, float tau,
                                      long long pre_slots, float* __restrict__ grad, float* __restrict__ pre_err) {
+    pdl_prologue();
     __shared__ float sred[32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -205,6 +207,7 @@ conv_backward_cluster_kernel(const Event* __restrict__ ev, const int* __restrict
                              const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
                              int search_top, float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
                              float* __restrict__ pre_err) {
+    pdl_prologue();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) float Gs[];  // taps * C
@@ -316,6 +319,7 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
                              const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
                              float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
                              float* __restrict__ pre_err) {
+    pdl_prologue();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) float Gs[];  // taps * C, then C spike counters
@@ -404,6 +408,7 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
 __global__ void pool_forward_kernel(const int* __restrict__ n_spikes, const float* __restrict__ times, int batch, int X,
                                     int Y, int C, int K, int* __restrict__ out_n, float* __restrict__ out_t,
                                     int* __restrict__ out_idx) {
+    pdl_prologue();
     const int Xo = X / 2, Yo = Y / 2;
     const long long n_out = (long long)Xo * Yo * C;
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -457,6 +462,7 @@ __global__ void pool_forward_kernel(const int* __restrict__ n_spikes, const floa
 
 __global__ void pool_backward_kernel(const float* __restrict__ errors, const int* __restrict__ idx, long long count,
                                      float* __restrict__ pre_err) {
+    pdl_prologue();
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
          q += (long long)gridDim.x * blockDim.x)
         pre_err[idx[q]] = errors[q];
@@ -496,10 +502,10 @@ extern "C" int bats_conv_forward(const void* events, const int* ev_count, long l
     const size_t smem = base_smem + (w_in_smem ? nw * sizeof(float) : 0);
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_forward_kernel, (int)smem));
     dim3 grid(tiles_x * tiles_y, batch);
-    bats::conv_forward_kernel<<<grid, threads, smem, stream>>>(
-        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, weights, X, Y, C, fx, fy, C_out, Xo, Yo, TX,
-        TY, tiles_y, k_post, bats::make_solve_const(c, delta_theta_tau, tau, max_simulation), w_in_smem, n_spikes, a, x,
-        times, post_exp_tau);
+    BATS_CUDA(bats::launch(bats::conv_forward_kernel, grid, threads, smem, stream,
+        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, weights, X, Y, C, fx, fy, C_out, Xo, Yo, TX, TY,
+        tiles_y, k_post, bats::make_solve_const(c, delta_theta_tau, tau, max_simulation), w_in_smem, n_spikes, a, x,
+        times, post_exp_tau));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -532,13 +538,13 @@ extern "C" int bats_conv_backward(const void* events, const int* ev_slot, const 
         cfg.blockDim = dim3(threads);
         cfg.dynamicSmemBytes = gbytes;
         cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = bats::CONV_BWD_CLUSTER;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = 1 + (unsigned)bats::pdl_attribute(attr + 1);
         BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_cluster_kernel,
                                      reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights,
                                      Y, C, fx, fy, C_out, Xo, Yo, post_times,
@@ -546,10 +552,10 @@ extern "C" int bats_conv_backward(const void* events, const int* ev_slot, const 
                                      pre_slots, grad_per_sample, pre_errors));
         return BATS_OK;
     }
-    bats::conv_backward_kernel<<<batch, threads, 0, stream>>>(
+    BATS_CUDA(bats::launch(bats::conv_backward_kernel, batch, threads, 0, stream,
         reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights, Y, C, fx, fy, C_out, Xo, Yo,
         post_times, reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots, grad_per_sample,
-        pre_errors);
+        pre_errors));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -580,13 +586,13 @@ extern "C" int bats_conv_backward_grouped(const void* events_bucketed, const int
     cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = bats::CONV_BWD_CLUSTER;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 1 + (unsigned)bats::pdl_attribute(attr + 1);
     BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_grouped_kernel,
                                  reinterpret_cast<const bats::Event*>(events_bucketed), bucket_offsets, X * Y, ev_cap,
                                  weights, Y, C, fx, fy, C_out, Xo, Yo, k_pre, post_times,
@@ -604,8 +610,8 @@ extern "C" int bats_pool_forward(const int* n_spikes, const float* times, int ba
     BATS_REQUIRE(n_spikes && times && out_n_spikes && out_times && out_indices, BATS_ERR_NULL,
                  "pool_forward: null pointer");
     const long long total = (long long)batch * (X / 2) * (Y / 2) * C;
-    bats::pool_forward_kernel<<<(unsigned)((total + 127) / 128), 128, 0, stream>>>(n_spikes, times, batch, X, Y, C, K,
-                                                                                 out_n_spikes, out_times, out_indices);
+    BATS_CUDA(bats::launch(bats::pool_forward_kernel, (unsigned)((total + 127) / 128), 128, 0, stream, n_spikes, times,
+        batch, X, Y, C, K, out_n_spikes, out_times, out_indices));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -621,7 +627,8 @@ extern "C" int bats_pool_backward(const float* errors, const int* indices, long 
     BATS_REQUIRE(errors && indices, BATS_ERR_NULL, "pool_backward: null pointer");
     long long b = (count + 255) / 256;
     if (b > 152 * 16) b = 152 * 16;
-    bats::pool_backward_kernel<<<(unsigned)b, 256, 0, stream>>>(errors, indices, count, pre_errors);
+    BATS_CUDA(bats::launch(bats::pool_backward_kernel, (unsigned)b, 256, 0, stream, errors, indices, count,
+        pre_errors));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -41,6 +41,7 @@ __global__ void bwd_prep_kernel(const float* __restrict__ t, const float* __rest
                                 float tau, float dtt, int do_recurrent, int do_factors,
                                 float* __restrict__ f1, float* __restrict__ f2, float2* __restrict__ tab,
                                 int* __restrict__ nvalid) {
+    pdl_prologue();
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= total) return;
     const long long base = idx * K;
@@ -102,6 +103,7 @@ bwd_prep_layer_kernel(const float* __restrict__ t, const float* __restrict__ a, 
                       const float* __restrict__ z, float* __restrict__ err, long long total, int K, float c, float tau,
                       float dtt, float* __restrict__ f1, float* __restrict__ f2, float2* __restrict__ tab,
                       int* __restrict__ nvalid) {
+    pdl_prologue();
     extern __shared__ float prep_smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* sT = prep_smem + warp * 5 * 32 * PREP_KS;
@@ -236,6 +238,7 @@ bwd_prep_counted_kernel(const float* __restrict__ t, const int* __restrict__ n_s
                         const float* __restrict__ x, const float* __restrict__ z, float* __restrict__ err,
                         long long total, int K, float c, float tau, float dtt, float2* __restrict__ tab,
                         int* __restrict__ nvalid) {
+    pdl_prologue();
     __shared__ PrepCompact sm_all[PREPC_WARPS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     PrepCompact& sm = sm_all[warp];
@@ -352,6 +355,7 @@ __global__ void __launch_bounds__(TILE)
 bwd_grad_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
                 const float* __restrict__ post_t, const float2* __restrict__ tab, const int* __restrict__ nvalid,
                 int n_post, int k_post, int n_pre, int batch, int group, float* __restrict__ out) {
+    pdl_prologue();
     __shared__ float G[JC][TILE + 1];
     __shared__ Event sev[BWD_CHUNK];
     const int tid = threadIdx.x;
@@ -405,6 +409,7 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
                          long long ev_cap, const float* __restrict__ post_t, const float2* __restrict__ tab,
                          const int* __restrict__ nvalid, int n_post, int k_post, int n_pre, int batch, int group,
                          float* __restrict__ out, int* __restrict__ flags) {
+    pdl_prologue();
     constexpr int WARPS = TILE / 32;
     __shared__ float G[JC][TILE + 1];
     __shared__ Event sev[BWD_CHUNK];
@@ -519,6 +524,7 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
 __global__ void reduce_groups_kernel(const float* __restrict__ partial, int n_rows, int n_cols, int groups,
                                      float divisor, float* __restrict__ out, const int* __restrict__ flags,
                                      int tile_shift, int jc_shift, int tiles, int buckets) {
+    pdl_prologue();
     const long long per_group = (long long)n_rows * n_cols;
     const long long fstride = (long long)tiles * buckets;
     for (int i = blockIdx.y; i < n_rows; i += gridDim.y) {
@@ -562,6 +568,7 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
                    const float* __restrict__ wt, int ld, const float* __restrict__ post_t,
                    const float2* __restrict__ tab, const int* __restrict__ nvalid, int n_post, int k_post,
                    float2* __restrict__ partial, int n_tiles, int* __restrict__ status) {
+    pdl_prologue();
     constexpr int WARPS = TILE / 32;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using Smem = StreamSmem<TILE, SEV, STAGES>;
@@ -664,6 +671,7 @@ bwd_pre_err_narrow_kernel(const Event* __restrict__ ev, const int* __restrict__ 
                           const float* __restrict__ post_t, const float2* __restrict__ tab,
                           const int* __restrict__ nvalid, int n_post, int k_post, long long slots_per_sample,
                           float tau_s, float tau, float* __restrict__ pre_err) {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float2* stab = reinterpret_cast<float2*>(smem_raw);
     float* st = reinterpret_cast<float*>(stab + n_post * (k_post + 1));
@@ -700,6 +708,7 @@ __global__ void pre_err_scatter_kernel(const float2* __restrict__ partial, const
                                        const int* __restrict__ ev_slot, const int* __restrict__ ev_count,
                                        long long ev_cap, int n_tiles, long long slots_per_sample, float tau_s,
                                        float tau, float* __restrict__ pre_err) {
+    pdl_prologue();
     const int s = blockIdx.y;
     const int E = ev_count[s];
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < E; m += gridDim.x * blockDim.x) {
@@ -736,9 +745,9 @@ extern "C" int bats_backward_prep(const float* post_times, const float* a, const
     BATS_REQUIRE(!tables || (f1 && f2), BATS_ERR_NULL, "backward_prep: tables need f1/f2");
     const int threads = 128;
     const int blocks = (int)((total + threads - 1) / threads);
-    bats::bwd_prep_kernel<<<blocks, threads, 0, stream>>>(post_times, a, x, post_exp_tau, errors, total, k_post, c,
-                                                         tau, delta_theta_tau, do_recurrent, do_factors, f1, f2,
-                                                         reinterpret_cast<float2*>(tables), nvalid);
+    BATS_CUDA(bats::launch(bats::bwd_prep_kernel, blocks, threads, 0, stream, post_times, a, x, post_exp_tau, errors,
+        total, k_post, c, tau, delta_theta_tau, do_recurrent, do_factors, f1, f2, reinterpret_cast<float2*>(tables),
+        nvalid));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -761,9 +770,9 @@ extern "C" int bats_backward_prep_layer(const float* post_times, const float* a,
     const int blocks = (int)((warps + bats::PREP_WARPS - 1) / bats::PREP_WARPS);
     const size_t smem = (size_t)bats::PREP_WARPS * 5 * 32 * bats::PREP_KS * sizeof(float);
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_prep_layer_kernel, (int)smem));
-    bats::bwd_prep_layer_kernel<<<blocks, bats::PREP_WARPS * 32, smem, stream>>>(
-        post_times, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau, f1, f2,
-        reinterpret_cast<float2*>(tables), nvalid);
+    BATS_CUDA(bats::launch(bats::bwd_prep_layer_kernel, blocks, bats::PREP_WARPS * 32, smem, stream, post_times, a, x,
+        post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau, f1, f2, reinterpret_cast<float2*>(tables),
+        nvalid));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -780,9 +789,9 @@ extern "C" int bats_backward_prep_counted(const float* post_times, const int* n_
                  "backward_prep_counted: null pointer");
     const long long warps = (total + 31) / 32;
     const int blocks = (int)((warps + bats::PREPC_WARPS - 1) / bats::PREPC_WARPS);
-    bats::bwd_prep_counted_kernel<<<blocks, bats::PREPC_WARPS * 32, 0, stream>>>(
-        post_times, n_spikes, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau,
-        reinterpret_cast<float2*>(tables), nvalid);
+    BATS_CUDA(bats::launch(bats::bwd_prep_counted_kernel, blocks, bats::PREPC_WARPS * 32, 0, stream, post_times,
+        n_spikes, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau, reinterpret_cast<float2*>(tables),
+        nvalid));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -792,13 +801,12 @@ static int grad_tile_for(int n_post) { return n_post <= 32 ? 32 : (n_post <= 64 
 static int log2_pow2(int v) { return 31 - __builtin_clz((unsigned)v); }
 
 // Sum of the group partials (groups, n_post, n_pre) into out, ~8 CTAs of 256 threads per SM.
-static void launch_reduce(const float* part, int n_post, int n_pre, int groups, float divisor, float* out,
-                          const int* flags, int tile, int tiles, int buckets, cudaStream_t stream) {
+static cudaError_t launch_reduce(const float* part, int n_post, int n_pre, int groups, float divisor, float* out,
+                                 const int* flags, int tile, int tiles, int buckets, cudaStream_t stream) {
     const int gx = (n_pre + 255) / 256;
     const int gy = (int)std::min<long long>(n_post, std::max<long long>(1, 152LL * 8 / gx));
-    bats::reduce_groups_kernel<<<dim3(gx, gy), 256, 0, stream>>>(part, n_post, n_pre, groups, divisor, out, flags,
-                                                                 log2_pow2(tile), log2_pow2(GRAD_JC), tiles,
-                                                                 buckets);
+    return bats::launch(bats::reduce_groups_kernel, dim3(gx, gy), 256, 0, stream, part, n_post, n_pre, groups, divisor,
+                        out, flags, log2_pow2(tile), log2_pow2(GRAD_JC), tiles, buckets);
 }
 
 // Partials (groups, n_post, n_pre) floats, then (256-byte aligned) one int flag per partial tile.
@@ -815,20 +823,19 @@ extern "C" size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, i
 }
 
 template <int TILE>
-static void launch_grad(const void* events, const int* ev_count, const void* ev_b, const int* boff, int n_buckets,
-                        long long ev_cap, const float* post_times, const void* tables, const int* nvalid, int batch,
-                        int n_post, int k_post, int n_pre, int group, int groups, float* out, int* flags,
-                        cudaStream_t stream) {
+static cudaError_t launch_grad(const void* events, const int* ev_count, const void* ev_b, const int* boff,
+                               int n_buckets, long long ev_cap, const float* post_times, const void* tables,
+                               const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, int groups,
+                               float* out, int* flags, cudaStream_t stream) {
     dim3 grid((n_post + TILE - 1) / TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
-    if (ev_b) {
-        bats::bwd_grad_bucketed_kernel<TILE, GRAD_JC><<<grid, TILE, 0, stream>>>(
-            reinterpret_cast<const bats::Event*>(ev_b), boff, n_buckets, ev_cap, post_times,
-            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out, flags);
-    } else {
-        bats::bwd_grad_kernel<TILE, GRAD_JC><<<grid, TILE, 0, stream>>>(
-            reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
-            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out);
-    }
+    if (ev_b)
+        return bats::launch(bats::bwd_grad_bucketed_kernel<TILE, GRAD_JC>, grid, TILE, 0, stream,
+                            reinterpret_cast<const bats::Event*>(ev_b), boff, n_buckets, ev_cap, post_times,
+                            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out,
+                            flags);
+    return bats::launch(bats::bwd_grad_kernel<TILE, GRAD_JC>, grid, TILE, 0, stream,
+                        reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
+                        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out);
 }
 
 extern "C" int bats_weights_gradient(const void* events, const int* ev_count, const void* events_bucketed,
@@ -854,19 +861,17 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
     }
     const int tile = grad_tile_for(n_post);
     if (tile == 32)
-        launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables, nvalid,
-                        batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
+        BATS_CUDA(launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
+                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
     else if (tile == 64)
-        launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables, nvalid,
-                        batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
+        BATS_CUDA(launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
+                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
     else
-        launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times, tables,
-                         nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream);
-    BATS_CUDA(cudaGetLastError());
+        BATS_CUDA(launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
+                                   tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
     if (group == 1) return BATS_OK;  // per-sample gradient (B, N_post, N_pre)
-    launch_reduce(part, n_post, n_pre, groups, mean ? (float)batch : 1.0f, grad, flags, tile,
-                  (n_post + tile - 1) / tile, n_buckets, stream);
-    BATS_CUDA(cudaGetLastError());
+    BATS_CUDA(launch_reduce(part, n_post, n_pre, groups, mean ? (float)batch : 1.0f, grad, flags, tile,
+                            (n_post + tile - 1) / tile, n_buckets, stream));
     return BATS_OK;
 }
 
@@ -887,9 +892,9 @@ static int launch_pre_err(const void* events, const int* ev_count, long long ev_
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_kernel<TILE, SEV, STAGES>,
                                                       (int)smem));
     dim3 grid(tiles, batch);
-    bats::bwd_pre_err_kernel<TILE, SEV, STAGES><<<grid, TILE + 32, smem, stream>>>(
+    BATS_CUDA(bats::launch(bats::bwd_pre_err_kernel<TILE, SEV, STAGES>, grid, TILE + 32, smem, stream,
         reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, wt, ld, post_times,
-        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, part, tiles, status);
+        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, part, tiles, status));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -916,9 +921,9 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
         BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::bwd_pre_err_narrow_kernel, (int)smem));
         // At most 8 CTAs per sample (each stages the sample's post data once); empty samples exit at once.
         dim3 grid((unsigned)std::min<long long>((ev_cap + 127) / 128, 8), batch);
-        bats::bwd_pre_err_narrow_kernel<<<grid, 128, smem, stream>>>(
+        BATS_CUDA(bats::launch(bats::bwd_pre_err_narrow_kernel, grid, 128, smem, stream,
             reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights_t, ld, post_times,
-            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, slots, tau_s, tau, pre_errors);
+            reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, slots, tau_s, tau, pre_errors));
         BATS_CUDA(cudaGetLastError());
         return BATS_OK;
     }
@@ -945,8 +950,8 @@ extern "C" int bats_pre_errors(const void* events, const int* ev_slot, const int
     if (rc != BATS_OK) return rc;
     // A few CTAs per sample, striding over its events (most samples have far fewer events than slots).
     dim3 g2((unsigned)std::min<long long>((ev_cap + 255) / 256, 4), batch);
-    bats::pre_err_scatter_kernel<<<g2, 256, 0, stream>>>(part, reinterpret_cast<const bats::Event*>(events), ev_slot,
-                                                          ev_count, ev_cap, tiles, slots, tau_s, tau, pre_errors);
+    BATS_CUDA(bats::launch(bats::pre_err_scatter_kernel, g2, 256, 0, stream, part,
+        reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, tiles, slots, tau_s, tau, pre_errors));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -1009,11 +1014,10 @@ extern "C" int bats_weights_gradient_mean_noalloc(const void* events, const int*
         BATS_CUDA((cudaError_t)noalloc_scratch_ptr(&part));
     }
     dim3 grid((n_post + GRAD_TILE - 1) / GRAD_TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
-    bats::bwd_grad_kernel<GRAD_TILE, GRAD_JC><<<grid, GRAD_TILE, 0, stream>>>(
+    BATS_CUDA(bats::launch(bats::bwd_grad_kernel<GRAD_TILE, GRAD_JC>, grid, GRAD_TILE, 0, stream,
         reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
-        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, part);
+        reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, part));
     BATS_CUDA(cudaGetLastError());
-    launch_reduce(part, n_post, n_pre, groups, (float)batch, grad, nullptr, GRAD_TILE, 1, 1, stream);
-    BATS_CUDA(cudaGetLastError());
+    BATS_CUDA(launch_reduce(part, n_post, n_pre, groups, (float)batch, grad, nullptr, GRAD_TILE, 1, 1, stream));
     return BATS_OK;
 }

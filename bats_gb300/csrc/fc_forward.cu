@@ -160,6 +160,7 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
                       const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
                       int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
                       float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status, int pad) {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using Smem = StreamSmem<TILE, SEV, STAGES>;
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
@@ -214,6 +215,7 @@ lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict_
                             int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
                             float* __restrict__ t_out, float* __restrict__ z_out, int* __restrict__ status, int pad,
                             const int* __restrict__ order, int* __restrict__ head, int n_tiles, int n_items) {
+    pdl_prologue();
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using Smem = StreamSmem<TILE, SEV, STAGES>;
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
@@ -286,6 +288,7 @@ __device__ __forceinline__ int count_class(int c) {
 
 __global__ void __launch_bounds__(1024) work_order_kernel(const int* __restrict__ ev_count, int batch,
                                                           int* __restrict__ head, int* __restrict__ order) {
+    pdl_prologue();
     __shared__ int off[512];
     __shared__ int warp_sum[16];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -337,6 +340,7 @@ lif_fc_forward_lanes_kernel(const Event* __restrict__ ev, const int* __restrict_
                             const float* __restrict__ wt, int ld, int n_post, int k_post, SolveConst sk,
                             int* __restrict__ n_spikes, float* __restrict__ a_out, float* __restrict__ x_out,
                             float* __restrict__ t_out, float* __restrict__ z_out, int pad) {
+    pdl_prologue();
     __shared__ float4 blk[WARPS][32];  // (w, es, e, -) of the block's events
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int s = blockIdx.y;
@@ -444,9 +448,9 @@ static int launch_forward_lanes(const void* events, const int* ev_count, long lo
                                 int batch, int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a,
                                 float* x, float* times, float* post_exp_tau, int pad, cudaStream_t stream) {
     dim3 grid((n_post + WARPS - 1) / WARPS, batch);
-    lif_fc_forward_lanes_kernel<WARPS><<<grid, WARPS * 32, 0, stream>>>(
+    BATS_CUDA(bats::launch(lif_fc_forward_lanes_kernel<WARPS>, grid, WARPS * 32, 0, stream,
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
-        post_exp_tau, pad);
+        post_exp_tau, pad));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -459,9 +463,9 @@ static int launch_forward(const void* events, const int* ev_count, long long ev_
     BATS_CUDA((cudaError_t)max_dynamic_smem_set((const void*)lif_fc_forward_kernel<TILE, SEV, STAGES, SCREEN>,
                                                 (int)smem));
     dim3 grid((n_post + TILE - 1) / TILE, batch);
-    lif_fc_forward_kernel<TILE, SEV, STAGES, SCREEN><<<grid, TILE + 32, smem, stream>>>(
+    BATS_CUDA(bats::launch(lif_fc_forward_kernel<TILE, SEV, STAGES, SCREEN>, grid, TILE + 32, smem, stream,
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
-        post_exp_tau, status, pad);
+        post_exp_tau, status, pad));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -487,11 +491,11 @@ static int launch_forward_queue(const void* events, const int* ev_count, long lo
                  "lif_forward_fc_queue: batch * post-neuron tiles must stay below 2^31");
     const int n_items = batch * n_tiles;
     const int grid = (int)std::min<long long>(n_items, (long long)std::max(1, per_sm) * std::max(1, n_sm));
-    work_order_kernel<<<1, 1024, 0, stream>>>(ev_count, batch, head, order);
+    BATS_CUDA(bats::launch(work_order_kernel, 1, 1024, 0, stream, ev_count, batch, head, order));
     BATS_CUDA(cudaGetLastError());
-    lif_fc_forward_queue_kernel<TILE, SEV, STAGES, SCREEN><<<grid, TILE + 32, smem, stream>>>(
+    BATS_CUDA(bats::launch(lif_fc_forward_queue_kernel<TILE, SEV, STAGES, SCREEN>, grid, TILE + 32, smem, stream,
         reinterpret_cast<const Event*>(events), ev_count, ev_cap, wt, ld, n_post, k_post, sk, n_spikes, a, x, times,
-        post_exp_tau, status, pad, order, head, n_tiles, n_items);
+        post_exp_tau, status, pad, order, head, n_tiles, n_items));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

@@ -30,6 +30,7 @@ __global__ void __launch_bounds__(CONV_WARPS * 32)
 events_to_trains_kernel(const int* __restrict__ indices, const float* __restrict__ times,
                         const int* __restrict__ offsets, int batch, int max_events, int n_neurons, int k_cap,
                         float* __restrict__ out_times, int* __restrict__ out_counts, int* __restrict__ overflow) {
+    pdl_prologue();
     extern __shared__ int s_cnt[];
     __shared__ int w_idx[2][CONV_WINDOW];
     __shared__ float w_t[2][CONV_WINDOW];
@@ -115,11 +116,11 @@ static int launch_events_to_trains(const int* indices, const float* times, const
                                    int max_events, int n_neurons, int k_cap, float* out_times, int* out_counts,
                                    int* overflow, cudaStream_t stream) {
     if (n_neurons <= CONV_SMEM_NEURONS)
-        events_to_trains_kernel<true><<<batch, CONV_WARPS * 32, (size_t)n_neurons * sizeof(int), stream>>>(
-            indices, times, offsets, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+        BATS_CUDA(bats::launch(events_to_trains_kernel<true>, batch, CONV_WARPS * 32, (size_t)n_neurons * sizeof(int),
+            stream, indices, times, offsets, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow));
     else
-        events_to_trains_kernel<false><<<batch, CONV_WARPS * 32, 0, stream>>>(
-            indices, times, offsets, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow);
+        BATS_CUDA(bats::launch(events_to_trains_kernel<false>, batch, CONV_WARPS * 32, 0, stream, indices, times,
+            offsets, batch, max_events, n_neurons, k_cap, out_times, out_counts, overflow));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -131,6 +132,7 @@ template <bool SMEM_COUNTS>
 __global__ void __launch_bounds__(CONV_WARPS * 32)
 max_per_neuron_kernel(const int* __restrict__ indices, int batch, int max_events, int n_neurons,
                       int* __restrict__ scratch_counts, int* __restrict__ out_max) {
+    pdl_prologue();
     extern __shared__ int s_cnt[];
     const int lane = threadIdx.x & 31;
     const int s = blockIdx.x * CONV_WARPS + (threadIdx.x >> 5);
@@ -197,12 +199,12 @@ extern "C" int bats_events_max_per_neuron(const int* indices, int batch, int max
                  "events_max_per_neuron: null pointer");
     const int blocks = (batch + bats::CONV_WARPS - 1) / bats::CONV_WARPS;
     if (n_neurons * bats::CONV_WARPS <= 12288)  // 48 KB of warp-private counts
-        bats::max_per_neuron_kernel<true><<<blocks, bats::CONV_WARPS * 32,
-                                            (size_t)n_neurons * bats::CONV_WARPS * sizeof(int), stream>>>(
-            indices, batch, max_events, n_neurons, scratch_counts, out_max);
+        BATS_CUDA(bats::launch(bats::max_per_neuron_kernel<true>, blocks, bats::CONV_WARPS * 32,
+            (size_t)n_neurons * bats::CONV_WARPS * sizeof(int), stream, indices, batch, max_events, n_neurons,
+            scratch_counts, out_max));
     else
-        bats::max_per_neuron_kernel<false><<<blocks, bats::CONV_WARPS * 32, 0, stream>>>(
-            indices, batch, max_events, n_neurons, scratch_counts, out_max);
+        BATS_CUDA(bats::launch(bats::max_per_neuron_kernel<false>, blocks, bats::CONV_WARPS * 32, 0, stream, indices,
+            batch, max_events, n_neurons, scratch_counts, out_max));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -214,6 +216,7 @@ namespace bats {
 __global__ void intensity_to_spike_times_kernel(const unsigned char* __restrict__ pixels, long long total,
                                                 double time_window, double max_value, float* __restrict__ times,
                                                 int* __restrict__ counts) {
+    pdl_prologue();
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
         const double t = time_window * (1.0 - ((double)pixels[q] / max_value));
@@ -232,8 +235,8 @@ extern "C" int bats_intensity_to_spike_times(const unsigned char* pixels, int ba
     if (total == 0) return BATS_OK;
     BATS_REQUIRE(pixels && times && counts, BATS_ERR_NULL, "intensity_to_spike_times: null pointer");
     const long long blocks = (total + 255) / 256;
-    bats::intensity_to_spike_times_kernel<<<(int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, stream>>>(
-        pixels, total, time_window, max_value, times, counts);
+    BATS_CUDA(bats::launch(bats::intensity_to_spike_times_kernel,
+        (int)(blocks < 152 * 16 ? blocks : 152 * 16), 256, 0, stream, pixels, total, time_window, max_value, times, counts));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

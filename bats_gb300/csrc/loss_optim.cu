@@ -11,6 +11,7 @@ namespace bats {
 
 __global__ void pre_exps_kernel(const float* __restrict__ t, long long n, float tau_s, float tau,
                                 float* __restrict__ es, float* __restrict__ e) {
+    pdl_prologue();
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const float v = t[q];
         es[q] = __expf(v / tau_s);
@@ -24,6 +25,7 @@ __global__ void spike_count_loss_kernel(const void* __restrict__ counts, int cou
                                         const float* __restrict__ targets, const int* __restrict__ labels,
                                         float target_true, float target_false, int batch, int n, int k,
                                         float* __restrict__ loss, float* __restrict__ errors) {
+    pdl_prologue();
     const int warps = blockDim.x >> 5;
     const int s = blockIdx.x * warps + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -58,6 +60,7 @@ __device__ __forceinline__ float nan_to_num_f(float v) {
 __global__ void ttfs_sce_kernel(const float* __restrict__ spikes, const int* __restrict__ labels, int batch, int n,
                                 int k, double tau_literal, float tau_f, float* __restrict__ loss,
                                 float* __restrict__ errors) {
+    pdl_prologue();
     const int warps = blockDim.x >> 5;
     const int s = blockIdx.x * warps + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -92,6 +95,7 @@ __global__ void ttfs_sce_kernel(const float* __restrict__ spikes, const int* __r
 // Targets are modified in place (inf -> 1.0) like the reference.
 __global__ void spike_time_loss_kernel(const float* __restrict__ spikes, float* __restrict__ targets, int batch, int n,
                                        int k, int mode, float* __restrict__ loss, float* __restrict__ errors) {
+    pdl_prologue();
     const int warps = blockDim.x >> 5;
     const int s = blockIdx.x * warps + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
@@ -128,6 +132,7 @@ __global__ void adam_kernel(const float* __restrict__ grad, float* __restrict__ 
                             float r1_hi, float r1_lo, float r2_hi, float r2_lo,
                             float lr, float eps, float* __restrict__ delta, float* __restrict__ w, float* __restrict__ wt, int n_post,
                             int n_pre, int ld) {
+    pdl_prologue();
     if (powers) {
         // State written by adam_powers_kernel: beta^t (double) and the reciprocal pairs of 1 - beta^t.
         bias1 = 1.0 - powers[0];
@@ -172,6 +177,7 @@ adam_tiled_kernel(const float* __restrict__ grad, float* __restrict__ m, float* 
                   const double* __restrict__ powers, float r1_hi, float r1_lo, float r2_hi, float r2_lo, float lr,
                   float eps, float* __restrict__ delta, float* __restrict__ w, float* __restrict__ wt, int n_post,
                   int n_pre, int ld) {
+    pdl_prologue();
     __shared__ float tile[32][33];
     if (powers) {
         bias1 = 1.0 - powers[0];
@@ -215,6 +221,7 @@ adam_tiled_kernel(const float* __restrict__ grad, float* __restrict__ m, float* 
 
 // beta_1^t, beta_2^t kept on the device so that a captured step can advance t without host input.
 __global__ void adam_powers_kernel(double* powers, float beta_1, float beta_2) {
+    pdl_prologue();
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         powers[0] *= (double)beta_1;
         powers[1] *= (double)beta_2;
@@ -227,6 +234,7 @@ __global__ void adam_powers_kernel(double* powers, float beta_1, float beta_2) {
 
 // out (cols, ld) = in (rows, cols) transposed, 32x32 shared-memory tiles.
 __global__ void transpose_kernel(const float* __restrict__ in, int rows, int cols, float* __restrict__ out, int ld) {
+    pdl_prologue();
     __shared__ float tile[32][33];
     const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
     for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
@@ -242,6 +250,7 @@ __global__ void transpose_kernel(const float* __restrict__ in, int rows, int col
 
 __global__ void add_inplace_kernel(float* __restrict__ w, const float* __restrict__ d, long long count,
                                    float* __restrict__ wt, int n_pre, int ld) {
+    pdl_prologue();
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
          q += (long long)gridDim.x * blockDim.x) {
         const float nw = w[q] + d[q];
@@ -264,7 +273,8 @@ extern "C" int bats_compute_pre_exps(const float* times, long long count, float 
     BATS_REQUIRE(count >= 0, BATS_ERR_BAD_SHAPE, "compute_pre_exps: bad shape");
     if (count == 0) return BATS_OK;
     BATS_REQUIRE(times && exp_tau_s && exp_tau, BATS_ERR_NULL, "compute_pre_exps: null pointer");
-    bats::pre_exps_kernel<<<grid_for(count, 256), 256, 0, stream>>>(times, count, tau_s, tau, exp_tau_s, exp_tau);
+    BATS_CUDA(bats::launch(bats::pre_exps_kernel, grid_for(count, 256), 256, 0, stream, times, count, tau_s, tau,
+        exp_tau_s, exp_tau));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -276,8 +286,8 @@ extern "C" int bats_spike_count_loss(const void* counts, int count_is_float, con
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(counts && (targets || labels), BATS_ERR_NULL, "spike_count_loss: null pointer");
     const int warps = 4;
-    bats::spike_count_loss_kernel<<<(batch + warps - 1) / warps, warps * 32, 0, stream>>>(
-        counts, count_is_float, targets, labels, target_true, target_false, batch, n, k, loss, errors);
+    BATS_CUDA(bats::launch(bats::spike_count_loss_kernel, (batch + warps - 1) / warps, warps * 32, 0, stream, counts,
+        count_is_float, targets, labels, target_true, target_false, batch, n, k, loss, errors));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -288,8 +298,8 @@ extern "C" int bats_ttfs_softmax_cross_entropy(const float* spikes, const int* l
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(spikes && labels, BATS_ERR_NULL, "ttfs_sce: null pointer");
     const int warps = 4;
-    bats::ttfs_sce_kernel<<<(batch + warps - 1) / warps, warps * 32, 0, stream>>>(spikes, labels, batch, n, k, tau,
-                                                                                   (float)tau, loss, errors);
+    BATS_CUDA(bats::launch(bats::ttfs_sce_kernel, (batch + warps - 1) / warps, warps * 32, 0, stream, spikes, labels,
+        batch, n, k, tau, (float)tau, loss, errors));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -301,8 +311,8 @@ extern "C" int bats_spike_time_loss(const float* spikes, float* targets, int bat
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(spikes && targets, BATS_ERR_NULL, "spike_time_loss: null pointer");
     const int warps = 4;
-    bats::spike_time_loss_kernel<<<(batch + warps - 1) / warps, warps * 32, 0, stream>>>(spikes, targets, batch, n, k,
-                                                                                          mode, loss, errors);
+    BATS_CUDA(bats::launch(bats::spike_time_loss_kernel, (batch + warps - 1) / warps, warps * 32, 0, stream, spikes,
+        targets, batch, n, k, mode, loss, errors));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -321,15 +331,13 @@ extern "C" int bats_adam_step(const float* grad, float* m, float* v, long long c
     bats::reciprocal_pair(bias_correction_2, r2h, r2l);
     if (weights && weights_t) {
         dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
-        bats::adam_tiled_kernel<<<grid, block, 0, stream>>>(
-            grad, m, v, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
-            bias_correction_1, bias_correction_2, nullptr, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta, weights,
-            weights_t, n_post, n_pre, ld);
+        BATS_CUDA(bats::launch(bats::adam_tiled_kernel, grid, block, 0, stream, grad, m, v, beta_1,
+            (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), bias_correction_1, bias_correction_2,
+            nullptr, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta, weights, weights_t, n_post, n_pre, ld));
     } else {
-        bats::adam_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
-            grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
-            bias_correction_1, bias_correction_2, nullptr, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta, weights,
-            weights_t, n_post, n_pre, ld);
+        BATS_CUDA(bats::launch(bats::adam_kernel, grid_for(count, 256), 256, 0, stream, grad, m, v, count, beta_1,
+            (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), bias_correction_1, bias_correction_2,
+            nullptr, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta, weights, weights_t, n_post, n_pre, ld));
     }
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
@@ -337,7 +345,7 @@ extern "C" int bats_adam_step(const float* grad, float* m, float* v, long long c
 
 extern "C" int bats_adam_powers_advance(double* powers, float beta_1, float beta_2, cudaStream_t stream) {
     BATS_REQUIRE(powers, BATS_ERR_NULL, "adam_powers_advance: null pointer");
-    bats::adam_powers_kernel<<<1, 32, 0, stream>>>(powers, beta_1, beta_2);
+    BATS_CUDA(bats::launch(bats::adam_powers_kernel, 1, 32, 0, stream, powers, beta_1, beta_2));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -353,14 +361,13 @@ extern "C" int bats_adam_step_device(const float* grad, float* m, float* v, long
                  "adam_step_device: transposed copy needs n_post*n_pre == count");
     if (weights_t) {
         dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
-        bats::adam_tiled_kernel<<<grid, block, 0, stream>>>(
-            grad, m, v, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0, 0.0,
-            powers, 0.0f, 0.0f, 0.0f, 0.0f, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre, ld);
+        BATS_CUDA(bats::launch(bats::adam_tiled_kernel, grid, block, 0, stream, grad, m, v, beta_1,
+            (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0, 0.0, powers, 0.0f, 0.0f, 0.0f,
+            0.0f, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre, ld));
     } else {
-        bats::adam_kernel<<<grid_for(count, 256), 256, 0, stream>>>(
-            grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0,
-            0.0, powers, 0.0f, 0.0f, 0.0f, 0.0f, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre,
-            ld);
+        BATS_CUDA(bats::launch(bats::adam_kernel, grid_for(count, 256), 256, 0, stream, grad, m, v, count, beta_1,
+            (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), 0.0, 0.0, powers, 0.0f, 0.0f, 0.0f,
+            0.0f, learning_rate, epsilon, nullptr, weights, weights_t, n_post, n_pre, ld));
     }
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
@@ -371,7 +378,7 @@ extern "C" int bats_transpose(const float* in, int rows, int cols, float* out, i
     if (rows == 0 || cols == 0) return BATS_OK;
     BATS_REQUIRE(in && out, BATS_ERR_NULL, "transpose: null pointer");
     dim3 grid((cols + 31) / 32, (rows + 31) / 32);
-    bats::transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(in, rows, cols, out, ld);
+    BATS_CUDA(bats::launch(bats::transpose_kernel, grid, dim3(32, 8), 0, stream, in, rows, cols, out, ld));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -382,7 +389,8 @@ extern "C" int bats_add_deltas(float* weights, const float* delta, long long cou
     if (count == 0) return BATS_OK;
     BATS_REQUIRE(weights && delta, BATS_ERR_NULL, "add_deltas: null pointer");
     BATS_REQUIRE(!weights_t || n_pre > 0, BATS_ERR_BAD_SHAPE, "add_deltas: n_pre");
-    bats::add_inplace_kernel<<<grid_for(count, 256), 256, 0, stream>>>(weights, delta, count, weights_t, n_pre, ld);
+    BATS_CUDA(bats::launch(bats::add_inplace_kernel, grid_for(count, 256), 256, 0, stream, weights, delta, count,
+        weights_t, n_pre, ld));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

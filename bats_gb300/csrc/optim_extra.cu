@@ -7,7 +7,7 @@
 // larger weights, by factor * |w|.
 #include <cmath>
 #include "abi_util.h"
-#include "disc.cuh"
+#include "common.cuh"
 
 namespace bats {
 
@@ -20,6 +20,7 @@ __global__ void nadam_kernel(const float* __restrict__ grad, float* __restrict__
                              long long count, float beta_1, float one_minus_beta_1, float beta_2,
                              float one_minus_beta_2, double bias1, double bias2, float bias1_f, float r1_hi,
                              float r1_lo, float r2_hi, float r2_lo, float lr, float eps, float* __restrict__ delta) {
+    pdl_prologue();
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count;
          q += (long long)gridDim.x * blockDim.x) {
         const float g = grad[q];
@@ -38,6 +39,7 @@ __global__ void nadam_kernel(const float* __restrict__ grad, float* __restrict__
 __global__ void weights_synaptic_scaling_kernel(const float* __restrict__ w, const float* __restrict__ silent_ratios,
                                                 const int* __restrict__ n_spikes, float* __restrict__ gradient,
                                                 int batch, int n_post, int n_pre, float threshold, float factor) {
+    pdl_prologue();
     const long long total = (long long)batch * n_post * n_pre;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
@@ -56,6 +58,7 @@ __global__ void weights_synaptic_scaling_kernel(const float* __restrict__ w, con
 __global__ void label_weights_synaptic_scaling_kernel(const float* __restrict__ w, const float* __restrict__ labels,
                                                       const int* __restrict__ n_spikes, float* __restrict__ gradient,
                                                       int batch, int n_post, int n_pre, float factor) {
+    pdl_prologue();
     const long long total = (long long)batch * n_pre;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
@@ -83,10 +86,9 @@ extern "C" int bats_nadam_step(const float* grad, float* m, float* v, long long 
     float r1h, r1l, r2h, r2l;
     bats::reciprocal_pair(bias_correction_1, r1h, r1l);
     bats::reciprocal_pair(bias_correction_2, r2h, r2l);
-    bats::nadam_kernel<<<bats::grid_for(count, 256), 256, 0, stream>>>(
-        grad, m, v, count, beta_1, (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2),
-        bias_correction_1, bias_correction_2, (float)bias_correction_1, r1h, r1l, r2h, r2l, learning_rate, epsilon,
-        delta);
+    BATS_CUDA(bats::launch(bats::nadam_kernel, bats::grid_for(count, 256), 256, 0, stream, grad, m, v, count, beta_1,
+        (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), bias_correction_1, bias_correction_2,
+        (float)bias_correction_1, r1h, r1l, r2h, r2l, learning_rate, epsilon, delta));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -99,8 +101,8 @@ extern "C" int bats_weights_synaptic_scaling(const float* weights, const float* 
     if (total == 0) return BATS_OK;
     BATS_REQUIRE(weights && silent_ratios && n_spikes && gradient, BATS_ERR_NULL,
                  "weights_synaptic_scaling: null pointer");
-    bats::weights_synaptic_scaling_kernel<<<bats::grid_for(total, 256), 256, 0, stream>>>(
-        weights, silent_ratios, n_spikes, gradient, batch, n_post, n_pre, threshold, factor);
+    BATS_CUDA(bats::launch(bats::weights_synaptic_scaling_kernel, bats::grid_for(total, 256), 256, 0, stream, weights,
+        silent_ratios, n_spikes, gradient, batch, n_post, n_pre, threshold, factor));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -114,8 +116,8 @@ extern "C" int bats_label_weights_synaptic_scaling(const float* weights, const f
     if (total == 0 || n_post == 0) return BATS_OK;
     BATS_REQUIRE(weights && labels && n_spikes && gradient, BATS_ERR_NULL,
                  "label_weights_synaptic_scaling: null pointer");
-    bats::label_weights_synaptic_scaling_kernel<<<bats::grid_for(total, 256), 256, 0, stream>>>(
-        weights, labels, n_spikes, gradient, batch, n_post, n_pre, factor);
+    BATS_CUDA(bats::launch(bats::label_weights_synaptic_scaling_kernel, bats::grid_for(total, 256), 256, 0, stream,
+        weights, labels, n_spikes, gradient, batch, n_post, n_pre, factor));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }

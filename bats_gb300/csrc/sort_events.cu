@@ -1,4 +1,7 @@
 // Per-sample time sort of all pre-synaptic spikes of a layer (one CTA per sample).
+// The sort runs in shared memory whenever the sample's items fit (up to 17408 items with 16-bit slot
+// values for batches of at most 152 samples, 7680 for larger ones), else in a per-sample slice of the
+// caller's workspace.
 //
 // Replaces get_sorted_spikes_indices + the three take_along_axis gathers + compute_pre_exps
 // (bats/CudaKernels/Wrappers/Inference/get_sorted_spikes_indices.py:7-17,
@@ -18,8 +21,17 @@ namespace bats {
 
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
-constexpr int SORT_SMEM_ITEMS = 4096;  // items sorted fully in shared memory
 constexpr int SORT_MAX_BUCKETS = 255;
+// Items held in shared memory (two key buffers and two value buffers): slot values are 16-bit when the
+// layer has at most 65536 slots (cap = n_pre * k_pre), else 32-bit. Batches of at most SORT_SMALL_BATCH
+// samples (no more CTAs than a GB300 has SMs: one CTA per SM costs no parallelism) get as many items as
+// 227 KB holds (SORT_SMEM_MAX_U16 / _U32); larger batches keep two CTAs per SM (SORT_SMEM_U16 / _U32 items,
+// 110 KB or 82 KB with the counters). Samples with more valid slots than that sort in global scratch.
+constexpr int SORT_SMALL_BATCH = 152;
+constexpr int SORT_SMEM_MAX_U16 = 17408;  // 12 B per item + the counters <= 227 KB
+constexpr int SORT_SMEM_MAX_U32 = 13312;  // 16 B per item
+constexpr int SORT_SMEM_U16 = 7680;
+constexpr int SORT_SMEM_U32 = 4096;
 
 struct SortShared {
     int hist[256];
@@ -93,19 +105,20 @@ __device__ __forceinline__ void scan_bins(SortShared& sh) {
 // One stable counting pass (digit < 256) of n (key, val) pairs from (ka, va) into (kb, vb), using the
 // bin bases already in sh.base. Items are ranked in rounds of SORT_THREADS in their current order;
 // inside a warp, items of equal digit are ranked by __match_any_sync, across warps by a per-digit scan.
-template <typename DigitFn>
-__device__ __forceinline__ void stable_pass(const uint32_t* ka, const uint32_t* va, uint32_t* kb, uint32_t* vb, int n,
+template <typename V, typename DigitFn>
+__device__ __forceinline__ void stable_pass(const uint32_t* ka, const V* va, uint32_t* kb, V* vb, int n,
                                             SortShared& sh, DigitFn digit) {
     const int tid = threadIdx.x, warp = tid >> 5;
     for (int r0 = 0; r0 < n; r0 += SORT_THREADS) {
         const int i = r0 + tid;
         const bool valid = i < n;
-        uint32_t key = 0, val = 0;
+        uint32_t key = 0;
+        V val = 0;
         int d = 256;
         if (valid) {
             key = ka[i];
             val = va[i];
-            d = digit(key, val);
+            d = digit(key, (uint32_t)val);
         }
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int rank = __popc(peers & lanemask_lt());
@@ -164,16 +177,19 @@ struct BucketDigit {
     __device__ int operator()(uint32_t, uint32_t slot) const { return (int)slot / div; }
 };
 
+// V: type of the slot values (uint16_t when n_slots <= 65536). smem_cap: items held in shared memory.
+template <typename V>
 __global__ void __launch_bounds__(SORT_THREADS)
 sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_counts, int n_slots, int k_pre,
                    float tau_s, float tau,
                    const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out,
                    int* __restrict__ slot_out, int* __restrict__ ev_count, Event* __restrict__ ev_bucketed,
-                   int* __restrict__ bucket_off, int bucket_width, int n_buckets, long long cap,
-                   uint32_t* __restrict__ scratch) {
+                   int* __restrict__ bucket_off, int bucket_width, int n_buckets, long long cap, int smem_cap,
+                   unsigned char* __restrict__ scratch) {
+    pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortShared& sh = *reinterpret_cast<SortShared*>(smem_raw);
-    uint32_t* smem_items = reinterpret_cast<uint32_t*>(smem_raw + sizeof(SortShared));
+    unsigned char* smem_items = smem_raw + sizeof(SortShared);
 
     const int s = blockIdx.x;
     const int tid = threadIdx.x;
@@ -226,17 +242,17 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
         return;
     }
 
-    uint32_t *ka, *va, *kb, *vb;
-    if (n <= SORT_SMEM_ITEMS) {
-        ka = smem_items;
-        va = ka + SORT_SMEM_ITEMS;
-        kb = va + SORT_SMEM_ITEMS;
-        vb = kb + SORT_SMEM_ITEMS;
-    } else {
-        ka = scratch + (long long)s * 4 * cap;
-        va = ka + cap;
-        kb = va + cap;
-        vb = kb + cap;
+    // Two key and two value buffers: in shared memory when the sample's items fit, else in this sample's
+    // part of the global scratch (cap items each).
+    uint32_t *ka, *kb;
+    V *va, *vb;
+    {
+        const long long room = n <= smem_cap ? smem_cap : cap;
+        unsigned char* base = n <= smem_cap ? smem_items : scratch + (long long)s * cap * (8 + 2 * sizeof(V));
+        ka = reinterpret_cast<uint32_t*>(base);
+        kb = ka + room;
+        va = reinterpret_cast<V*>(kb + room);
+        vb = va + room;
     }
 
     // Compaction in slot order (stable).
@@ -254,7 +270,7 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
                 const float t = tsrc[slot0 + q];
                 if (t < BATS_INF) {
                     ka[pos] = float_to_key(t);
-                    va[pos] = (uint32_t)(slot0 + q);
+                    va[pos] = (V)(slot0 + q);
                     ++pos;
                 }
             }
@@ -281,7 +297,7 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
             for (int u = 0; u < 4; ++u) {
                 if (vv[u] < BATS_INF) {
                     ka[pos] = float_to_key(vv[u]);
-                    va[pos] = (uint32_t)(4 * q + u);
+                    va[pos] = (V)(4 * q + u);
                     ++pos;
                 }
             }
@@ -298,7 +314,7 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
             const int pos = block_exclusive_flag_scan(f, sh, tot);
             if (f) {
                 ka[base + pos] = float_to_key(t);
-                va[base + pos] = (uint32_t)slot;
+                va[base + pos] = (V)slot;
             }
             base += tot;
         }
@@ -315,13 +331,13 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
         scan_bins(sh);
         stable_pass(ka, va, kb, vb, n, sh, TimeDigit{shift});
         uint32_t* t0 = ka; ka = kb; kb = t0;
-        t0 = va; va = vb; vb = t0;
+        V* t1 = va; va = vb; vb = t1;
     }
 
     Event* eo = ev_out + (long long)s * cap;
     int* so = slot_out ? slot_out + (long long)s * cap : nullptr;
     for (int m = tid; m < n; m += SORT_THREADS) {
-        eo[m] = make_event(ka[m], va[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
+        eo[m] = make_event(ka[m], (uint32_t)va[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
         if (so) so[m] = (int)va[m];
     }
     if (tid == 0) ev_count[s] = n;
@@ -341,7 +357,7 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
         stable_pass(ka, va, kb, vb, n, sh, BucketDigit{div});
         Event* be = ev_bucketed + (long long)s * cap;
         for (int m = tid; m < n; m += SORT_THREADS)
-            be[m] = make_event(kb[m], vb[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
+            be[m] = make_event(kb[m], (uint32_t)vb[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
     }
 }
 
@@ -349,12 +365,25 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
 
 // ---------------------------------------------------------------------------------------------
 // C-ABI launchers (declared in include/bats_gb300.h).
+#include <algorithm>
 #include "abi_util.h"
+
+// Shared-memory items and value width for a batch of samples with cap slots each (see SORT_SMALL_BATCH).
+static void sort_plan(int batch, long long cap, int* smem_cap, bool* u16) {
+    *u16 = cap <= 65536;
+    const bool small = batch <= bats::SORT_SMALL_BATCH;
+    const int room = *u16 ? (small ? bats::SORT_SMEM_MAX_U16 : bats::SORT_SMEM_U16)
+                          : (small ? bats::SORT_SMEM_MAX_U32 : bats::SORT_SMEM_U32);
+    *smem_cap = (int)std::min<long long>(room, (cap + 31) / 32 * 32);
+}
 
 extern "C" size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_pre) {
     const long long cap = (long long)n_pre * k_pre;
-    if (cap <= bats::SORT_SMEM_ITEMS) return 0;
-    return (size_t)batch * 4 * cap * sizeof(uint32_t);
+    int smem_cap;
+    bool u16;
+    sort_plan(batch, cap, &smem_cap, &u16);
+    if (cap <= smem_cap) return 0;
+    return (size_t)(batch > 0 ? batch : 0) * (size_t)cap * (u16 ? 12 : 16);
 }
 
 static int sort_events_impl(const float* pre_times, const int* pre_counts, int batch, int n_pre, int k_pre,
@@ -377,13 +406,24 @@ static int sort_events_impl(const float* pre_times, const int* pre_counts, int b
     const size_t need = bats_sort_events_workspace_bytes(batch, n_pre, k_pre);
     BATS_REQUIRE(workspace_bytes >= need && (need == 0 || workspace), BATS_ERR_WORKSPACE,
                  "sort_events: workspace too small");
-    const size_t smem = sizeof(bats::SortShared) + 4 * bats::SORT_SMEM_ITEMS * sizeof(uint32_t);
-    BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel, (int)smem));
-    bats::sort_events_kernel<<<batch, bats::SORT_THREADS, smem, stream>>>(
-        pre_times, pre_counts, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out,
-        ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets, cap,
-        reinterpret_cast<uint32_t*>(workspace));
-    BATS_CUDA(cudaGetLastError());
+    int smem_cap;
+    bool u16;
+    sort_plan(batch, cap, &smem_cap, &u16);
+    const size_t smem = sizeof(bats::SortShared) + (size_t)smem_cap * (8 + 2 * (u16 ? 2 : 4));
+    unsigned char* scratch = reinterpret_cast<unsigned char*>(workspace);
+    if (u16) {
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel<uint16_t>, (int)smem));
+        BATS_CUDA(bats::launch(bats::sort_events_kernel<uint16_t>, batch, bats::SORT_THREADS, smem, stream, pre_times,
+            pre_counts, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out),
+            slot_out, ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets,
+            cap, smem_cap, scratch));
+    } else {
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel<uint32_t>, (int)smem));
+        BATS_CUDA(bats::launch(bats::sort_events_kernel<uint32_t>, batch, bats::SORT_THREADS, smem, stream, pre_times,
+            pre_counts, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out),
+            slot_out, ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets,
+            cap, smem_cap, scratch));
+    }
     return BATS_OK;
 }
 

@@ -69,7 +69,12 @@ def test_workspace_queries(lib):
     from bats_gb300 import _lib
     L = _lib.load()
     assert L.bats_sort_events_workspace_bytes(4, 10, 3) == 0  # fits in shared memory
-    assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 4 * 30000 * 4
+    assert L.bats_sort_events_workspace_bytes(4, 512, 30) == 0  # 15360 slots: the whole layer in shared memory
+    assert L.bats_sort_events_workspace_bytes(256, 512, 30) == 256 * 15360 * 12  # large batch: 7680 items
+    assert L.bats_sort_events_workspace_bytes(256, 256, 30) == 0
+    # two 4-byte key and two 2-byte slot buffers per slot when the slots fit 16 bits, 4-byte slots above
+    assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 30000 * 12
+    assert L.bats_sort_events_workspace_bytes(2, 4000, 20) == 2 * 80000 * 16
     # 16 partial gradients, 256-byte aligned, then one flag per (partial, pre bucket of 64, post tile of 128)
     parts = (16 * 800 * 784 * 4 + 255) // 256 * 256
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == parts + 16 * 13 * 7 * 4

@@ -158,19 +158,39 @@ def test_sort_events_small_samples_with_ties(cuda, k):
         assert bo[s, nb] == c
 
 
-def test_sort_events_large_sample_uses_global_path(cuda):
-    """More valid slots than the shared-memory sort holds (4096)."""
+@pytest.mark.parametrize("shape,fill", [((2, 1000, 6), (6000, 3000)), ((2, 512, 30), (15360, 4000)),
+                                        ((2, 1000, 20), (20000, 5000)), ((2, 5000, 14), (70000, 3000)),
+                                        ((2, 1000, 16), (16000, 13000)), ((160, 512, 30), (15360, 7000)),
+                                        ((160, 4000, 20), (80000, 4000))])
+def test_sort_events_large_sample_uses_global_path(cuda, shape, fill):
+    """Samples of every size class of the sort. Small batches (<= 152 samples): up to 17408 items in shared
+    memory with 16-bit slot values (layers of at most 65536 slots), 13312 with 32-bit values; larger
+    batches: 7680 and 4096. Samples above that sort in the global workspace. Events and slots equal the
+    oracle's sort; the bucketed copy is each bucket's events in time order. The samples not listed in
+    `fill` hold 37 spikes."""
     rng = np.random.default_rng(4)
-    t = rng.uniform(0, 1, (2, 1000, 6)).astype(np.float32)
-    t[1, :, 3:] = np.inf
+    B, N, Kp = shape
+    t = np.full(shape, np.inf, np.float32)
+    fill = tuple(fill) + (37,) * (B - len(fill))
+    for s, m in enumerate(fill):  # the first m slots of the sample (in slot order) hold spikes
+        flat = np.sort(rng.uniform(0, 1, (N, Kp)), axis=1).astype(np.float32).reshape(-1)
+        flat[m:] = np.inf
+        t[s] = flat.reshape(N, Kp)
     ev = K.sort_events(torch.tensor(t, device="cuda"), 0.1, 0.2)
     cnt = ev.counts.cpu().numpy()
-    assert cnt.tolist() == [6000, 3000]
-    e = ev.events.cpu().numpy()
-    for s in range(2):
+    assert cnt.tolist() == list(fill)
+    e, slots_d = ev.events.cpu().numpy(), ev.slots.cpu().numpy()
+    be, bo = ev.bucketed.cpu().numpy(), ev.bucket_offsets.cpu().numpy()
+    for s in range(min(B, 3)):
         et, ej, slots = R.sort_events(t[s:s + 1])[0]
-        assert np.array_equal(e[s, :cnt[s], 0], et.astype(np.float32))
-        assert np.array_equal(ev.slots.cpu().numpy()[s, :cnt[s]], slots)
+        c = cnt[s]
+        assert np.array_equal(e[s, :c, 0], et.astype(np.float32))
+        assert np.array_equal(slots_d[s, :c], slots)
+        bucket = (slots // Kp) // K.BUCKET_WIDTH
+        order = np.argsort(bucket, kind="stable")
+        assert np.array_equal(be[s, :c].view(np.uint32), e[s, :c][order].view(np.uint32))
+        nb = bo.shape[1] - 1
+        assert np.array_equal(bo[s, :nb], np.searchsorted(bucket[order], np.arange(nb), side="left"))
 
 
 def _events_equal(p, q, what):

@@ -9,6 +9,10 @@ batch-mean gradient and Adam.
 * Replaying the captured CUDA graph gives the eager step's result bit for bit, and the autotuned step
   (other kernel variants and gradient groups) agrees with the untuned one within the same tolerance.
 """
+import os
+import subprocess
+import sys
+
 import numpy as np
 import pytest
 import torch
@@ -150,3 +154,41 @@ def test_work_queue_forward_step_equals_tile_step_under_graph_capture(cuda):
     assert int(queue.out[0][0].sum()) > 0
     for a, b in zip(tile.W, queue.W):
         assert torch.equal(a, b)
+
+
+_CHILD_STEP_SCRIPT = """
+import sys
+import numpy as np
+import torch
+sys.path.insert(0, {root!r})
+from tests.test_gpu_train_step import case, make_step
+t, n, ws, labels = case(seed=9)
+ts = make_step(t, ws, labels)
+assert ts.try_capture(), ts.capture_error
+for _ in range(2):
+    ts.replay()
+torch.cuda.synchronize()
+np.savez({out!r}, *[w.cpu().numpy() for w in ts.W])
+"""
+
+
+def test_programmatic_dependent_launch_keeps_results(cuda, tmp_path):
+    """With BATS_GB300_PDL=1 every kernel is launched with programmatic stream serialization (its successor's
+    CTAs start while it drains and wait in their prologue). The graph-replayed train step gives bit-identical
+    weights with it (child process: the setting is read once per process) and in plain stream order."""
+    if os.environ.get("BATS_GB300_PDL") == "1":
+        pytest.skip("this process already runs with programmatic dependent launch")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = str(tmp_path / "pdl.npz")
+    env = dict(os.environ, BATS_GB300_PDL="1")
+    subprocess.run([sys.executable, "-c", _CHILD_STEP_SCRIPT.format(root=root, out=out)], env=env, check=True,
+                   timeout=600)
+    t, n, ws, labels = case(seed=9)
+    ts = make_step(t, ws, labels)
+    assert ts.try_capture(), ts.capture_error
+    for _ in range(2):
+        ts.replay()
+    torch.cuda.synchronize()
+    pdl = np.load(out)
+    for q, w in enumerate(ts.W):
+        assert np.array_equal(w.cpu().numpy().view(np.uint32), pdl[f"arr_{q}"].view(np.uint32)), f"layer {q}"
