@@ -66,6 +66,9 @@ SIGNATURES = {
     "bats_weights_gradient_workspace_bytes": (c_size, [c_int, c_int, c_int, c_int]),
     "bats_weights_gradient": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
                                       c_int, c_int, c_vp, c_vp, c_size, c_vp]),
+    "bats_weights_gradient_adam": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
+                                           c_int, c_vp, c_vp, c_vp, c_float, c_float, c_float, c_float, c_vp, c_vp,
+                                           c_vp, c_int, c_vp, c_size, c_vp]),
     "bats_weights_gradient_noalloc_capacity": (c_ll, []),
     "bats_weights_gradient_mean_noalloc": (c_int, [c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
                                                    c_int, c_vp, c_vp]),

@@ -553,6 +553,75 @@ __global__ void reduce_groups_kernel(const float* __restrict__ partial, int n_ro
     }
 }
 
+// Batch-mean weight gradient from the group partials, fused with the Adam update of the weights: CTA per
+// 32 x 32 tile of the (n_post, n_pre) matrix (block 32 x 8, four rows per thread), as the tiled Adam kernel.
+// Per element, the written partials are summed in group order and divided by the batch exactly as
+// reduce_groups_kernel does, and the Adam update is adam_tiled_kernel's (the bias corrections from the
+// device-side powers); the new weights are also written transposed (through shared memory) into wt, and the
+// gradient into grad_out when given. Results are bit-identical to bats_weights_gradient followed by
+// bats_adam_step_device, without the gradient's round trip through memory and one launch fewer.
+__global__ void __launch_bounds__(256)
+reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restrict__ flags, int groups,
+                         int tile_shift, int jc_shift, int tiles, int buckets, float divisor,
+                         float* __restrict__ grad_out, float* __restrict__ m, float* __restrict__ v, float beta_1,
+                         float one_minus_beta_1, float beta_2, float one_minus_beta_2,
+                         const double* __restrict__ powers, float lr, float eps, float* __restrict__ w,
+                         float* __restrict__ wt, int n_post, int n_pre, int ld) {
+    pdl_prologue();
+    __shared__ float tile[32][33];
+    const double bias1 = 1.0 - powers[0];
+    const double bias2 = 1.0 - powers[1];
+    const float4 rp = *reinterpret_cast<const float4*>(powers + 2);
+    const long long per_group = (long long)n_post * n_pre;
+    const long long fstride = (long long)tiles * buckets;
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int j = j0 + tx;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int i = i0 + ty + 8 * r;
+        if (i < n_post && j < n_pre) {
+            const long long q = (long long)i * n_pre + j;
+            const int* fl = flags ? flags + (j >> jc_shift) * tiles + (i >> tile_shift) : nullptr;
+            float acc = 0.0f;
+            int gg = 0;
+            for (; gg + 4 <= groups; gg += 4) {
+                const bool f0 = !fl || fl[gg * fstride], f1 = !fl || fl[(gg + 1) * fstride];
+                const bool f2 = !fl || fl[(gg + 2) * fstride], f3 = !fl || fl[(gg + 3) * fstride];
+                const float p0 = f0 ? partial[(long long)gg * per_group + q] : 0.0f;
+                const float p1 = f1 ? partial[(long long)(gg + 1) * per_group + q] : 0.0f;
+                const float p2 = f2 ? partial[(long long)(gg + 2) * per_group + q] : 0.0f;
+                const float p3 = f3 ? partial[(long long)(gg + 3) * per_group + q] : 0.0f;
+                if (f0) acc += p0;
+                if (f1) acc += p1;
+                if (f2) acc += p2;
+                if (f3) acc += p3;
+            }
+            for (; gg < groups; ++gg)
+                if (!fl || fl[gg * fstride]) acc += partial[(long long)gg * per_group + q];
+            const float g = acc / divisor;
+            if (grad_out) grad_out[q] = g;
+            const float nm = beta_1 * m[q] + one_minus_beta_1 * g;
+            const float nv = beta_2 * v[q] + one_minus_beta_2 * g * g;
+            m[q] = nm;
+            v[q] = nv;
+            const float m_hat = quotient_f64_to_f32(nm, rp.x, rp.y, bias1);
+            const float v_hat = quotient_f64_to_f32(nv, rp.z, rp.w, bias2);
+            const float d = -(lr * m_hat / (sqrtf(v_hat) + eps));
+            const float nw = w[q] + d;
+            w[q] = nw;
+            tile[ty + 8 * r][tx] = nw;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int jj = j0 + ty + 8 * r;  // row of wt
+        const int ii = i0 + tx;          // column of wt
+        if (jj < n_pre && ii < n_post) wt[(long long)jj * ld + ii] = tile[tx][ty + 8 * r];
+    }
+}
+
 // Errors of the pre-synaptic spikes. Grid (post tiles, B), TILE consumer threads (one per post
 // neuron) + one producer warp. As in the forward kernel, the producer streams the sample's events and
 // their weight-row segments wt[j, tile] into shared-memory stages with bulk copies; a stage holds SEV
@@ -872,6 +941,50 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
     if (group == 1) return BATS_OK;  // per-sample gradient (B, N_post, N_pre)
     BATS_CUDA(launch_reduce(part, n_post, n_pre, groups, mean ? (float)batch : 1.0f, grad, flags, tile,
                             (n_post + tile - 1) / tile, n_buckets, stream));
+    return BATS_OK;
+}
+
+extern "C" int bats_weights_gradient_adam(const void* events, const int* ev_count, const void* events_bucketed,
+                                          const int* bucket_offsets, long long ev_cap, const float* post_times,
+                                          const void* tables, const int* nvalid, int batch, int n_post, int k_post,
+                                          int n_pre, int group, float* grad, float* m, float* v, float beta_1,
+                                          float beta_2, float epsilon, float learning_rate, const double* powers,
+                                          float* weights, float* weights_t, int ld, void* workspace,
+                                          size_t workspace_bytes, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 2 && ld >= n_post,
+                 BATS_ERR_BAD_SHAPE, "weights_gradient_adam: bad shape (group >= 2, ld >= n_post)");
+    if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
+    BATS_REQUIRE(post_times && tables && nvalid && m && v && powers && weights && weights_t &&
+                     ((events && ev_count) || (events_bucketed && bucket_offsets)),
+                 BATS_ERR_NULL, "weights_gradient_adam: null pointer");
+    const int n_buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
+    const int groups = (batch + group - 1) / group;
+    float* part = grad;
+    int* flags = nullptr;
+    if (groups > 1) {
+        BATS_REQUIRE(workspace && workspace_bytes >= bats_weights_gradient_workspace_bytes(batch, n_post, n_pre, group),
+                     BATS_ERR_WORKSPACE, "weights_gradient_adam: workspace too small");
+        part = reinterpret_cast<float*>(workspace);
+        if (events_bucketed)
+            flags = reinterpret_cast<int*>(static_cast<char*>(workspace) + grad_partials_bytes(groups, n_post, n_pre));
+    } else {
+        BATS_REQUIRE(grad, BATS_ERR_NULL, "weights_gradient_adam: one group (group >= batch) needs grad");
+    }
+    const int tile = grad_tile_for(n_post);
+    if (tile == 32)
+        BATS_CUDA(launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
+                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+    else if (tile == 64)
+        BATS_CUDA(launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
+                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+    else
+        BATS_CUDA(launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
+                                   tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+    dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
+    BATS_CUDA(bats::launch(bats::reduce_adam_tiled_kernel, grid, block, 0, stream, part, flags, groups,
+        log2_pow2(tile), log2_pow2(GRAD_JC), (n_post + tile - 1) / tile, n_buckets, (float)batch, grad, m, v, beta_1,
+        (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), powers, learning_rate, epsilon, weights,
+        weights_t, n_post, n_pre, ld));
     return BATS_OK;
 }
 

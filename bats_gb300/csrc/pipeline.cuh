@@ -113,71 +113,6 @@ __device__ __forceinline__ void stream_init(StreamSmem<TILE, SEV, STAGES>& sm, i
     }
 }
 
-// Producer warp body. Never returns with copies in flight into shared memory. Lane u issues the row
-// copy of the stage's event u (SEV <= 32); the event indices of the next stage are loaded while the
-// producer waits for a free slot, so that no global-load latency sits between two stages.
-template <int TILE, int SEV, int STAGES>
-__device__ __forceinline__ void stream_produce(StreamSmem<TILE, SEV, STAGES>& sm, const Event* __restrict__ evs, int E,
-                                               const float* __restrict__ wt, int ld, int tile0, int n_stages,
-                                               int lane, int* status) {
-    static_assert(SEV <= 32, "one event per producer lane");
-    const uint32_t row_bytes = (uint32_t)min(TILE, ld - tile0) * 4u;
-    int issued = 0;
-    int j_next = (lane < SEV && lane < E) ? __ldg(&evs[lane].j) : 0;
-    for (int k = 0; k < n_stages; ++k) {
-        const int slot = k % STAGES;
-        const int j = j_next;
-        const int m1 = (k + 1) * SEV + lane;
-        j_next = (lane < SEV && m1 < E) ? __ldg(&evs[m1].j) : 0;
-        const bool ok = mbar_wait(&sm.empty[slot], ((k / STAGES) & 1) ^ 1, &sm.abort, status);
-        if (!__all_sync(0xffffffffu, ok)) break;
-        const int m0 = k * SEV;
-        const int cnt = min(SEV, E - m0);
-        const int cnt_ev = min(SEV + 1, E - m0);
-        if (lane == 0) mbar_arrive_expect_tx(&sm.full[slot], (uint32_t)cnt_ev * 16u + (uint32_t)cnt * row_bytes);
-        __syncwarp();
-        if (lane == 0) bulk_copy_g2s(&sm.evs[slot][0], evs + m0, (uint32_t)cnt_ev * 16u, &sm.full[slot]);
-        if (lane < cnt) bulk_copy_g2s(&sm.rows[slot][lane][0], wt + (long long)j * ld + tile0, row_bytes, &sm.full[slot]);
-        issued = k + 1;
-    }
-    if (sm.abort) {
-        for (int k = max(0, issued - STAGES); k < issued; ++k) {
-            volatile int dummy = 0;
-            mbar_wait(&sm.full[k % STAGES], (k / STAGES) & 1, &dummy, nullptr);
-        }
-    }
-}
-
-// Producer of one work item of a persistent kernel: the item's stages are stages k0 .. k0 + n_stages - 1
-// of the CTA's ring, which earlier items have cycled through (so slot and phase follow the running stage
-// count). Returns the number of stages whose copies were issued: n_stages, or fewer when a wait gave up
-// (the CTA abort flag is then raised and the caller drains with stream_drain).
-template <int TILE, int SEV, int STAGES>
-__device__ __forceinline__ int stream_produce_at(StreamSmem<TILE, SEV, STAGES>& sm, const Event* __restrict__ evs,
-                                                 int E, const float* __restrict__ wt, int ld, int tile0,
-                                                 int n_stages, int k0, int lane, int* status) {
-    static_assert(SEV <= 32, "one event per producer lane");
-    const uint32_t row_bytes = (uint32_t)min(TILE, ld - tile0) * 4u;
-    int j_next = (lane < SEV && lane < E) ? __ldg(&evs[lane].j) : 0;
-    for (int k = 0; k < n_stages; ++k) {
-        const int kg = k0 + k;
-        const int slot = kg % STAGES;
-        const int j = j_next;
-        const int m1 = (k + 1) * SEV + lane;
-        j_next = (lane < SEV && m1 < E) ? __ldg(&evs[m1].j) : 0;
-        const bool ok = mbar_wait(&sm.empty[slot], ((kg / STAGES) & 1) ^ 1, &sm.abort, status);
-        if (!__all_sync(0xffffffffu, ok)) return k;
-        const int m0 = k * SEV;
-        const int cnt = min(SEV, E - m0);
-        const int cnt_ev = min(SEV + 1, E - m0);
-        if (lane == 0) mbar_arrive_expect_tx(&sm.full[slot], (uint32_t)cnt_ev * 16u + (uint32_t)cnt * row_bytes);
-        __syncwarp();
-        if (lane == 0) bulk_copy_g2s(&sm.evs[slot][0], evs + m0, (uint32_t)cnt_ev * 16u, &sm.full[slot]);
-        if (lane < cnt) bulk_copy_g2s(&sm.rows[slot][lane][0], wt + (long long)j * ld + tile0, row_bytes, &sm.full[slot]);
-    }
-    return n_stages;
-}
-
 // After an abort: bounded waits for the copies of the last STAGES issued stages (of `issued` in all), so
 // that no bulk copy into shared memory is in flight when the CTA exits.
 template <int TILE, int SEV, int STAGES>
@@ -186,6 +121,64 @@ __device__ __forceinline__ void stream_drain(StreamSmem<TILE, SEV, STAGES>& sm, 
         volatile int dummy = 0;
         mbar_wait(&sm.full[k % STAGES], (k / STAGES) & 1, &dummy, nullptr);
     }
+}
+
+// Stages of pre-neuron indices the producer loads ahead. Its loop issues a stage in far less time than a
+// global load takes, so with one stage of look-ahead every stage waited for its load; eight stages cover it.
+constexpr int STREAM_PREFETCH = 8;
+
+// Producer of stages k0 .. k0 + n_stages - 1 of the ring (k0 = 0: one work item per CTA; persistent kernels
+// continue the running stage count of earlier items, so slot and phase follow it). Lane u issues the row
+// copy of the stage's event u (SEV <= 32); the pre-neuron indices of the next STREAM_PREFETCH stages are in
+// flight in registers (a ring indexed statically by unrolling). Returns the number of stages whose copies
+// were issued: n_stages, or fewer when a wait gave up (the CTA abort flag is then raised; drain with
+// stream_drain).
+template <int TILE, int SEV, int STAGES>
+__device__ __forceinline__ int stream_produce_at(StreamSmem<TILE, SEV, STAGES>& sm, const Event* __restrict__ evs,
+                                                 int E, const float* __restrict__ wt, int ld, int tile0,
+                                                 int n_stages, int k0, int lane, int* status) {
+    static_assert(SEV <= 32, "one event per producer lane");
+    constexpr int D = STREAM_PREFETCH;
+    const uint32_t row_bytes = (uint32_t)min(TILE, ld - tile0) * 4u;
+    int jr[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const int m = d * SEV + lane;
+        jr[d] = (lane < SEV && m < E) ? __ldg(&evs[m].j) : 0;
+    }
+    for (int kb = 0; kb < n_stages; kb += D) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int k = kb + d;
+            if (k >= n_stages) break;
+            const int kg = k0 + k;
+            const int slot = kg % STAGES;
+            const int j = jr[d];
+            const int m_ahead = (k + D) * SEV + lane;
+            jr[d] = (lane < SEV && m_ahead < E) ? __ldg(&evs[m_ahead].j) : 0;
+            const bool ok = mbar_wait(&sm.empty[slot], ((kg / STAGES) & 1) ^ 1, &sm.abort, status);
+            if (!__all_sync(0xffffffffu, ok)) return k;
+            const int m0 = k * SEV;
+            const int cnt = min(SEV, E - m0);
+            const int cnt_ev = min(SEV + 1, E - m0);
+            if (lane == 0)
+                mbar_arrive_expect_tx(&sm.full[slot], (uint32_t)cnt_ev * 16u + (uint32_t)cnt * row_bytes);
+            __syncwarp();
+            if (lane == 0) bulk_copy_g2s(&sm.evs[slot][0], evs + m0, (uint32_t)cnt_ev * 16u, &sm.full[slot]);
+            if (lane < cnt)
+                bulk_copy_g2s(&sm.rows[slot][lane][0], wt + (long long)j * ld + tile0, row_bytes, &sm.full[slot]);
+        }
+    }
+    return n_stages;
+}
+
+// Producer warp body of a CTA with one work item. Never returns with copies in flight into shared memory.
+template <int TILE, int SEV, int STAGES>
+__device__ __forceinline__ void stream_produce(StreamSmem<TILE, SEV, STAGES>& sm, const Event* __restrict__ evs, int E,
+                                               const float* __restrict__ wt, int ld, int tile0, int n_stages,
+                                               int lane, int* status) {
+    const int issued = stream_produce_at(sm, evs, E, wt, ld, tile0, n_stages, 0, lane, status);
+    if (sm.abort) stream_drain(sm, issued);
 }
 
 // Consumer side: wait for stage k (all lanes of the warp agree on the outcome).

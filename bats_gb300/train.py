@@ -106,10 +106,14 @@ class FCTrainStep:
 
     # -- the step as a fixed list of launches --------------------------------------------------------
     def _build_launches(self):
-        """(name, fn(stream)) for every entry-point call of one step, in order. All pointers are fixed."""
+        """(name, fn(stream)) for every entry-point call of one step, in order. All pointers are fixed.
+        Adam's bias-correction powers are advanced first; each layer's backward is prep, pre-spike errors (which
+        read the layer's weights before their update), then the batch-mean gradient fused with the layer's
+        Adam update."""
         B = self.B
         ws, wsb = ptr(self.ws), self.ws.numel()
-        L = []
+        L = [("adam.powers", lambda s: call("bats_adam_powers_advance", ptr(self.powers), float(self.b1),
+                                              float(self.b2), s))]
         pre_times, pre_counts = self.in_times, None
         for li, spec in enumerate(self.specs):
             ev = self.ev[li]
@@ -153,10 +157,6 @@ class FCTrainStep:
                           tb=tb: call("bats_backward_prep_layer", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]),
                                       ptr(e), B, spec.n_neurons, spec.max_n_spike, float(c), float(tau32),
                                       float(dtt), ptr(tb.f1), ptr(tb.f2), ptr(tb.tables), ptr(tb.nvalid), s)))
-            L.append((f"{tag}.grad", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
-                "bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
-                ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,
-                self.groups[li], 1, ptr(self.grad[li]), ws, wsb, s)))
             if li > 0:
                 pe = self.pre_err[li]
                 L.append((f"{tag}.pre_err", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, pe=pe, tau32=tau32: call(
@@ -165,19 +165,25 @@ class FCTrainStep:
                     spec.max_n_spike, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32), ptr(pe), ws,
                     wsb, s)))
                 errors = pe
-        L.append(("adam.powers", lambda s: call("bats_adam_powers_advance", ptr(self.powers), float(self.b1),
-                                                float(self.b2), s)))
-        for li in range(len(self.specs)):
-            w = self.W[li]
-            L.append((f"L{li + 1}.adam", lambda s, li=li, w=w: call(
-                "bats_adam_step_device", ptr(self.grad[li]), ptr(self.m[li]), ptr(self.v[li]), w.numel(),
-                float(self.b1), float(self.b2), float(self.eps), float(self.lr), ptr(self.powers), ptr(w),
-                ptr(self.Wt[li]), w.shape[0], w.shape[1], self.Wt[li].shape[1], s)))
+            L.append((f"{tag}.grad_adam", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
+                "bats_weights_gradient_adam", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed),
+                ptr(ev.bucket_offsets), ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons,
+                spec.max_n_spike, ev.n_neurons, self.groups[li], ptr(self.grad[li]), ptr(self.m[li]),
+                ptr(self.v[li]), float(self.b1), float(self.b2), float(self.eps), float(self.lr), ptr(self.powers),
+                ptr(self.W[li]), ptr(self.Wt[li]), self.Wt[li].shape[1], ws, wsb, s)))
         return L
 
+    def _grad_only(self, li: int, group: int, s) -> None:
+        """The batch-mean weight gradient of layer li into self.grad[li] (no weight update), from the tables of
+        the last backward pass: what the autotuner times for the gradient group size."""
+        spec, ev = self.specs[li], self.ev[li]
+        t, tb = self.out[li][3], self.tabs[li]
+        call("bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
+             ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), self.B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,
+             group, 1, ptr(self.grad[li]), ptr(self.ws), self.ws.numel(), s)
+
     # Kernels launched by each entry point (memsets counted as launches too).
-    KERNELS_PER_CALL = {"sort": 1, "forward": 1, "loss": 1, "prep": 1, "grad": 2, "pre_err": 3, "powers": 1,
-                        "adam": 1}
+    KERNELS_PER_CALL = {"sort": 1, "forward": 1, "loss": 1, "prep": 1, "grad_adam": 2, "pre_err": 3, "powers": 1}
 
     @property
     def launches_per_step(self) -> int:
@@ -202,7 +208,7 @@ class FCTrainStep:
         tuner = tuner or get_tuner()
         s = stream_ptr()
         for name, fn in self.launches:
-            if not name.endswith("adam") and name != "adam.powers":
+            if not name.endswith("grad_adam") and name != "adam.powers":  # leave the weights and Adam state alone
                 fn(s)
         torch.cuda.synchronize()
         B = self.B
@@ -210,7 +216,6 @@ class FCTrainStep:
         n_prev = self.in_times.shape[1]
         k_prev = self.in_times.shape[2]
         fwd = {nm: fn for nm, fn in self.launches if nm.endswith(".forward")}
-        grad = {nm: fn for nm, fn in self.launches if nm.endswith(".grad")}
         wsb = self.ws.numel()
         for li, spec in enumerate(self.specs):
             tag = f"L{li + 1}"
@@ -239,10 +244,7 @@ class FCTrainStep:
                     cands[str(g)] = g
             if len(cands) > 1:
                 def run_grad(g, li=li):
-                    saved = self.groups[li]
-                    self.groups[li] = g
-                    grad[f"{tag}.grad"](s)
-                    self.groups[li] = saved
+                    self._grad_only(li, g, s)
 
                 bg = tuner.pick("fc_grad_group", shape, {k: (lambda g=g: run_grad(g)) for k, g in cands.items()},
                                 force=force)

@@ -228,9 +228,12 @@ def algorithmic_bytes(ts, name):
     N = spec.n_neurons
     if kind == "forward":
         return 8 * S + 4 * S * N + ts.B * N * (4 + 16 * spec.max_n_spike)
-    if kind in ("grad", "pre_err"):
+    if kind in ("grad", "grad_adam", "pre_err"):
         n_spk = int(ts.out[li][0].sum().item())
-        return 4 * S * N + 16 * n_spk + (4 * N * ev.n_neurons if kind == "grad" else 0)
+        # + the batch-mean gradient write (grad), or the Adam update that consumes it in place: read W, m, v,
+        # write W, its transposed copy, m, v and the gradient (grad_adam)
+        extra = {"grad": 4, "grad_adam": 32, "pre_err": 0}[kind] * N * ev.n_neurons
+        return 4 * S * N + 16 * n_spk + extra
     if kind == "sort":
         return ts.B * ev.cap * 4 + 20 * S
     return None
@@ -297,10 +300,11 @@ def run_ours(args, dist, rank, world):
         }
         del ts
         torch.cuda.empty_cache()
-    # Plain (layer-by-layer) drop-in API and the reference kernels, active regime (few steps).
+    # Plain (layer-by-layer) drop-in API and the reference kernels, both configurations (few steps).
     if args.workload == "all":
-        result["active"]["plain_api"] = plain_api_rate("active", max(2, args.steps // 4), flush)
-        result["active"]["refkern"] = refkern_rate("active", 2, flush)
+        for variant in ("literal", "active"):
+            result[variant]["plain_api"] = plain_api_rate(variant, max(2, args.steps // 4), flush)
+            result[variant]["refkern"] = refkern_rate(variant, 2, flush)
     return result
 
 
@@ -819,7 +823,7 @@ def main():
                    "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (512 MB write)",
                    "cuda_graph": lit["graph"]},
         "roofline": lit["roofline"], "e2e": lit["e2e"], "gpu_launches": lit["gpu_launches"], "clocks": lit["clocks"],
-        "autotuned": lit["autotuned"],
+        "autotuned": lit["autotuned"], "plain_api": lit.get("plain_api"), "refkern": lit.get("refkern"),
         "cpu_baseline": cb, "spikes_per_layer": lit["spikes_per_layer_last_step"], "kernels_ms": lit["kernels_ms"],
         "active": act, "serving": serving, "conv": conv, "batching": batching,
     }

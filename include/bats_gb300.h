@@ -219,6 +219,23 @@ int bats_weights_gradient(const void* events, const int* ev_count, const void* e
                           const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, int mean,
                           float* grad, void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+/* The batch-mean weight gradient (bats_weights_gradient with group >= 2, mean) and the Adam update of the
+ * weights (bats_adam_step_device) in one call: the group partials are summed, divided by the batch and fed to
+ * Adam by one tiled kernel, so the gradient needs no round trip through memory; grad (n_post, n_pre) receives
+ * it too when not NULL (required when group >= batch, as the one partial lives there). m, v, weights and
+ * weights_t (n_pre, ld) are updated in place; powers as for bats_adam_step_device (advanced before the call).
+ * Results are bit-identical to the two calls. Replaces compute_weights_gradient + the batch mean
+ * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24, train_spike_count.py:167) and
+ * AdamOptimizer.step + Network.apply_deltas (bats/Optimizers/AdamOptimizer.py:35-55,
+ * bats/Layers/LIFLayer.py:112-113). The weights change, so a caller that propagates errors through this
+ * layer (bats_pre_errors) does so before this call. Workspace: bats_weights_gradient_workspace_bytes. */
+int bats_weights_gradient_adam(const void* events, const int* ev_count, const void* events_bucketed,
+                               const int* bucket_offsets, long long ev_cap, const float* post_times, const void* tables,
+                               const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, float* grad,
+                               float* m, float* v, float beta_1, float beta_2, float epsilon, float learning_rate,
+                               const double* powers, float* weights, float* weights_t, int ld, void* workspace,
+                               size_t workspace_bytes, cudaStream_t stream);
+
 /* Allocation-free batch mean of bats_weights_gradient (group >= 2), for callers that cannot allocate device
  * memory (a runtime with a fixed arena, a plugin host that passes only input and output buffers). No
  * counterpart in the reference. The per-group partial sums live in a 32 MiB static device array of the

@@ -12,6 +12,7 @@ from bats_gb300.Layers import InputLayer, LIFLayer
 from bats_gb300.Optimizers import AdamOptimizer, GradientDescentOptimizer
 from bats_gb300 import kernels as K
 from oracle import bats_ref64 as R
+from tests._helpers import mnist_like_input
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -224,3 +225,47 @@ def test_checkpoint_resumes_training_exactly(cuda, tmp_path):
     for _ in range(2):
         step(net2, opt2)
     assert torch.equal(hid.weights, hid2.weights) and torch.equal(out.weights, out2.weights)
+
+
+@pytest.mark.parametrize("group,bucketed", [(8, True), (8, False), (64, True)])
+def test_fused_gradient_adam_equals_gradient_then_adam(cuda, group, bucketed):
+    """bats_weights_gradient_adam (group partials summed, divided by the batch and fed to Adam by one tiled
+    kernel) gives the gradient, m, v, weights and transposed weights of bats_weights_gradient followed by
+    bats_adam_step_device bit for bit, over two steps: several partials (group 8 of a batch of 32) with the
+    bucketed or the plain event list, and one partial (group >= batch)."""
+    from bats_gb300._lib import call, ptr, stream_ptr
+    B, n_in, n_post = 32, 784, 120
+    t, _ = mnist_like_input(B, seed=12)
+    rng = np.random.default_rng(13)
+    W = torch.tensor(rng.uniform(-1, 1, (n_post, n_in)).astype(np.float32), device="cuda")
+    ev = K.sort_events(torch.tensor(t, device="cuda"), np.float32(0.13), np.float32(0.26), bucketed=bucketed)
+    wt = K.transpose_weights(W)
+    n, a, x, ts, z = K.lif_forward_fc(ev, wt, n_post, 20, 0.13, 0.2, 0.2, 0.2)
+    assert int(n.sum()) > 0
+    err = torch.tensor(rng.uniform(-1, 1, ts.shape).astype(np.float32), device="cuda")
+    tau32, c, dtt = K.lif_constants(0.13, 0.2, 0.2)
+    tabs = K.backward_prep(ts, a, x, z, err, c, tau32, dtt)
+    ws_bytes = max(256, K.call_size("bats_weights_gradient_workspace_bytes", B, n_post, n_in, group))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    state = []
+    for fused in (False, True):
+        w, wtt = W.clone(), wt.clone()
+        m, v = torch.zeros_like(W), torch.zeros_like(W)
+        g = torch.zeros_like(W)
+        powers = torch.tensor([1.0, 1.0, 0.0, 0.0], dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            call("bats_adam_powers_advance", ptr(powers), 0.9, 0.999, stream_ptr())
+            common = (ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets), ev.cap, ptr(ts),
+                      ptr(tabs.tables), ptr(tabs.nvalid), B, n_post, 20, n_in, group)
+            if fused:
+                call("bats_weights_gradient_adam", *common, ptr(g), ptr(m), ptr(v), 0.9, 0.999, 1e-8, 3e-3,
+                     ptr(powers), ptr(w), ptr(wtt), wtt.shape[1], ptr(ws), ws_bytes, stream_ptr())
+            else:
+                call("bats_weights_gradient", *common, 1, ptr(g), ptr(ws), ws_bytes, stream_ptr())
+                call("bats_adam_step_device", ptr(g), ptr(m), ptr(v), w.numel(), 0.9, 0.999, 1e-8, 3e-3,
+                     ptr(powers), ptr(w), ptr(wtt), n_post, n_in, wtt.shape[1], stream_ptr())
+        torch.cuda.synchronize()
+        state.append([v_.cpu().numpy() for v_ in (g, m, v, w, wtt)])
+    assert np.abs(state[0][0]).max() > 0
+    for name, p, q in zip(("grad", "m", "v", "weights", "transposed weights"), *state):
+        assert np.array_equal(p.view(np.uint32), q.view(np.uint32)), name
