@@ -981,6 +981,15 @@ extern "C" int bats_weights_gradient_adam(const void* events, const int* ev_coun
         BATS_CUDA(launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
                                    tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
     dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
+    if (grad && groups > 1 && (long long)grid.x * grid.y < 2 * 152) {
+        // Few weight tiles (a narrow layer) for many partials: the tile grid would leave most SMs idle while
+        // each thread sums the groups; the row-parallel reduction into grad, then the tiled Adam, is faster
+        // and computes the same values.
+        BATS_CUDA(launch_reduce(part, n_post, n_pre, groups, (float)batch, grad, flags, tile,
+                                (n_post + tile - 1) / tile, n_buckets, stream));
+        return bats_adam_step_device(grad, m, v, (long long)n_post * n_pre, beta_1, beta_2, epsilon, learning_rate,
+                                     powers, weights, weights_t, n_post, n_pre, ld, stream);
+    }
     BATS_CUDA(bats::launch(bats::reduce_adam_tiled_kernel, grid, block, 0, stream, part, flags, groups,
         log2_pow2(tile), log2_pow2(GRAD_JC), (n_post + tile - 1) / tile, n_buckets, (float)batch, grad, m, v, beta_1,
         (float)(1.0 - (double)beta_1), beta_2, (float)(1.0 - (double)beta_2), powers, learning_rate, epsilon, weights,

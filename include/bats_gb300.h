@@ -224,6 +224,8 @@ int bats_weights_gradient(const void* events, const int* ev_count, const void* e
  * Adam by one tiled kernel, so the gradient needs no round trip through memory; grad (n_post, n_pre) receives
  * it too when not NULL (required when group >= batch, as the one partial lives there). m, v, weights and
  * weights_t (n_pre, ld) are updated in place; powers as for bats_adam_step_device (advanced before the call).
+ * For a layer of fewer than 304 32 x 32 weight tiles (a narrow layer) with several partials and grad given, the
+ * row-parallel reduction into grad and the tiled Adam run as two kernels instead (more CTAs per partial sum).
  * Results are bit-identical to the two calls. Replaces compute_weights_gradient + the batch mean
  * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24, train_spike_count.py:167) and
  * AdamOptimizer.step + Network.apply_deltas (bats/Optimizers/AdamOptimizer.py:35-55,

@@ -227,14 +227,15 @@ def test_checkpoint_resumes_training_exactly(cuda, tmp_path):
     assert torch.equal(hid.weights, hid2.weights) and torch.equal(out.weights, out2.weights)
 
 
-@pytest.mark.parametrize("group,bucketed", [(8, True), (8, False), (64, True)])
-def test_fused_gradient_adam_equals_gradient_then_adam(cuda, group, bucketed):
+@pytest.mark.parametrize("group,bucketed,n_post", [(8, True, 120), (8, False, 120), (64, True, 120), (4, True, 400)])
+def test_fused_gradient_adam_equals_gradient_then_adam(cuda, group, bucketed, n_post):
     """bats_weights_gradient_adam (group partials summed, divided by the batch and fed to Adam by one tiled
-    kernel) gives the gradient, m, v, weights and transposed weights of bats_weights_gradient followed by
-    bats_adam_step_device bit for bit, over two steps: several partials (group 8 of a batch of 32) with the
-    bucketed or the plain event list, and one partial (group >= batch)."""
+    kernel; for layers of few weight tiles the row-parallel reduction, then the tiled Adam) gives the gradient,
+    m, v, weights and transposed weights of bats_weights_gradient followed by bats_adam_step_device bit for
+    bit, over two steps: several partials (group 8 of a batch of 32) with the bucketed or the plain event
+    list, one partial (group >= batch), and a layer of 400 x 784 weights (325 tiles: the fused kernel)."""
     from bats_gb300._lib import call, ptr, stream_ptr
-    B, n_in, n_post = 32, 784, 120
+    B, n_in = 32, 784
     t, _ = mnist_like_input(B, seed=12)
     rng = np.random.default_rng(13)
     W = torch.tensor(rng.uniform(-1, 1, (n_post, n_in)).astype(np.float32), device="cuda")
