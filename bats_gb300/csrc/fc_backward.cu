@@ -560,6 +560,8 @@ __global__ void reduce_groups_kernel(const float* __restrict__ partial, int n_ro
 // device-side powers); the new weights are also written transposed (through shared memory) into wt, and the
 // gradient into grad_out when given. Results are bit-identical to bats_weights_gradient followed by
 // bats_adam_step_device, without the gradient's round trip through memory and one launch fewer.
+constexpr int REDUCE_SMEM_FLAGS = 2048;
+
 __global__ void __launch_bounds__(256)
 reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restrict__ flags, int groups,
                          int tile_shift, int jc_shift, int tiles, int buckets, float divisor,
@@ -569,6 +571,7 @@ reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restric
                          float* __restrict__ wt, int n_post, int n_pre, int ld) {
     pdl_prologue();
     __shared__ float tile[32][33];
+    __shared__ unsigned char s_fl[REDUCE_SMEM_FLAGS];
     const double bias1 = 1.0 - powers[0];
     const double bias2 = 1.0 - powers[1];
     const float4 rp = *reinterpret_cast<const float4*>(powers + 2);
@@ -577,17 +580,26 @@ reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restric
     const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int j = j0 + tx;
+    // The gradient kernel's tiles (post neurons) and buckets (pre neurons) are multiples of 32 and aligned,
+    // so this 32 x 32 tile lies in one (tile, bucket) cell and its flags are the same for every element:
+    // they are read once into shared memory (up to REDUCE_SMEM_FLAGS groups; beyond, per element).
+    const int* fl_cta = flags ? flags + (j0 >> jc_shift) * tiles + (i0 >> tile_shift) : nullptr;
+    const bool fl_shared = fl_cta && groups <= REDUCE_SMEM_FLAGS;
+    if (fl_shared)
+        for (int gg = ty * 32 + tx; gg < groups; gg += 256) s_fl[gg] = fl_cta[gg * fstride] != 0;
+    __syncthreads();
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int i = i0 + ty + 8 * r;
         if (i < n_post && j < n_pre) {
             const long long q = (long long)i * n_pre + j;
             const int* fl = flags ? flags + (j >> jc_shift) * tiles + (i >> tile_shift) : nullptr;
+            auto has = [&](int gg) -> bool { return !fl || (fl_shared ? s_fl[gg] != 0 : fl[gg * fstride] != 0); };
             float acc = 0.0f;
             int gg = 0;
             for (; gg + 4 <= groups; gg += 4) {
-                const bool f0 = !fl || fl[gg * fstride], f1 = !fl || fl[(gg + 1) * fstride];
-                const bool f2 = !fl || fl[(gg + 2) * fstride], f3 = !fl || fl[(gg + 3) * fstride];
+                const bool f0 = has(gg), f1 = has(gg + 1);
+                const bool f2 = has(gg + 2), f3 = has(gg + 3);
                 const float p0 = f0 ? partial[(long long)gg * per_group + q] : 0.0f;
                 const float p1 = f1 ? partial[(long long)(gg + 1) * per_group + q] : 0.0f;
                 const float p2 = f2 ? partial[(long long)(gg + 2) * per_group + q] : 0.0f;
@@ -598,7 +610,7 @@ reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restric
                 if (f3) acc += p3;
             }
             for (; gg < groups; ++gg)
-                if (!fl || fl[gg * fstride]) acc += partial[(long long)gg * per_group + q];
+                if (has(gg)) acc += partial[(long long)gg * per_group + q];
             const float g = acc / divisor;
             if (grad_out) grad_out[q] = g;
             const float nm = beta_1 * m[q] + one_minus_beta_1 * g;
