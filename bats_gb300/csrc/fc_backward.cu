@@ -588,6 +588,19 @@ reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restric
     if (fl_shared)
         for (int gg = ty * 32 + tx; gg < groups; gg += 256) s_fl[gg] = fl_cta[gg * fstride] != 0;
     __syncthreads();
+    // The four rows' m, v and W are loaded before any arithmetic, so that their DRAM latencies overlap (the
+    // whole grid is resident at once; each thread otherwise waited for one row after another).
+    float m_in[4], v_in[4], w_in[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int i = i0 + ty + 8 * r;
+        if (i < n_post && j < n_pre) {
+            const long long q = (long long)i * n_pre + j;
+            m_in[r] = m[q];
+            v_in[r] = v[q];
+            w_in[r] = w[q];
+        }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int i = i0 + ty + 8 * r;
@@ -613,14 +626,14 @@ reduce_adam_tiled_kernel(const float* __restrict__ partial, const int* __restric
                 if (has(gg)) acc += partial[(long long)gg * per_group + q];
             const float g = acc / divisor;
             if (grad_out) grad_out[q] = g;
-            const float nm = beta_1 * m[q] + one_minus_beta_1 * g;
-            const float nv = beta_2 * v[q] + one_minus_beta_2 * g * g;
+            const float nm = beta_1 * m_in[r] + one_minus_beta_1 * g;
+            const float nv = beta_2 * v_in[r] + one_minus_beta_2 * g * g;
             m[q] = nm;
             v[q] = nv;
             const float m_hat = quotient_f64_to_f32(nm, rp.x, rp.y, bias1);
             const float v_hat = quotient_f64_to_f32(nv, rp.z, rp.w, bias2);
             const float d = -(lr * m_hat / (sqrtf(v_hat) + eps));
-            const float nw = w[q] + d;
+            const float nw = w_in[r] + d;
             w[q] = nw;
             tile[ty + 8 * r][tx] = nw;
         }

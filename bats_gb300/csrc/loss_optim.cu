@@ -191,21 +191,34 @@ adam_tiled_kernel(const float* __restrict__ grad, float* __restrict__ m, float* 
     const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int j = j0 + tx;
+    // All four rows' operands are loaded before the arithmetic, so that their latencies overlap.
+    float g_in[4], m_in[4], v_in[4], w_in[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int i = i0 + ty + 8 * r;
         if (i < n_post && j < n_pre) {
             const long long q = (long long)i * n_pre + j;
-            const float g = grad[q];
-            const float nm = beta_1 * m[q] + one_minus_beta_1 * g;
-            const float nv = beta_2 * v[q] + one_minus_beta_2 * g * g;
+            g_in[r] = grad[q];
+            m_in[r] = m[q];
+            v_in[r] = v[q];
+            w_in[r] = w[q];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int i = i0 + ty + 8 * r;
+        if (i < n_post && j < n_pre) {
+            const long long q = (long long)i * n_pre + j;
+            const float g = g_in[r];
+            const float nm = beta_1 * m_in[r] + one_minus_beta_1 * g;
+            const float nv = beta_2 * v_in[r] + one_minus_beta_2 * g * g;
             m[q] = nm;
             v[q] = nv;
             const float m_hat = quotient_f64_to_f32(nm, r1_hi, r1_lo, bias1);
             const float v_hat = quotient_f64_to_f32(nv, r2_hi, r2_lo, bias2);
             const float d = -(lr * m_hat / (sqrtf(v_hat) + eps));
             if (delta) delta[q] = d;
-            const float nw = w[q] + d;
+            const float nw = w_in[r] + d;
             w[q] = nw;
             tile[ty + 8 * r][tx] = nw;
         }
