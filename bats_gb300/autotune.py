@@ -87,14 +87,19 @@ class Autotuner:
             end.record(stream)
             end.synchronize()
             times[name] = start.elapsed_time(end) / self.reps
-        # Candidates within 3 % (or 2 us) of the fastest count as tied; the first of them in the caller's order
-        # (simplest variant first) wins, so that timing noise on near-empty work does not pick a heavier variant.
-        fastest = min(times.values())
-        best = next(n for n in candidates if times[n] <= max(fastest * 1.03, fastest + 0.002))
+        best = _choose(times, list(candidates))
         self.cache[k] = best
         self.timings[k] = times
         self._save()
         return best
+
+
+def _choose(times: Dict[str, float], order) -> str:
+    """The candidate to keep from measured times (ms): candidates within 3 % (or 2 us) of the fastest count as
+    tied, and the first of them in the caller's order (simplest variant first) wins, so that timing noise on
+    near-empty work does not pick a heavier variant."""
+    fastest = min(times.values())
+    return next(n for n in order if times[n] <= max(fastest * 1.03, fastest + 0.002))
 
 
 _GLOBAL: Optional[Autotuner] = None

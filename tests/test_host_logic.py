@@ -1,0 +1,71 @@
+"""Host-side logic that needs no GPU: the autotuner's choice rule, the kernel-variant flags of the Python
+binding, and the argument checks of the entry points added for the work-queue forward and the fused
+gradient-Adam (they return their status before any CUDA call)."""
+import ctypes
+
+import pytest
+
+from bats_gb300 import kernels as K
+from bats_gb300.autotune import _choose
+
+BAD_SHAPE, NULLPTR, WORKSPACE = 1, 2, 4
+
+
+def test_autotuner_ties_go_to_the_first_candidate():
+    order = ["tile", "lanes", "queue"]
+    assert _choose({"tile": 1.00, "lanes": 2.0, "queue": 0.99}, order) == "tile"      # within 3 %
+    assert _choose({"tile": 1.00, "lanes": 2.0, "queue": 0.90}, order) == "queue"     # clearly faster
+    assert _choose({"tile": 0.005, "lanes": 0.05, "queue": 0.004}, order) == "tile"   # within 2 us
+    assert _choose({"tile": 0.010, "lanes": 0.05, "queue": 0.004}, order) == "queue"
+
+
+def test_forward_variant_flags():
+    assert K.is_queue_algo(K.FWD_QUEUE) and K.is_queue_algo(K.FWD_QUEUE64)
+    assert K.is_queue_algo(K.FWD_QUEUE | K.FWD_NO_PAD | K.FWD_STAGE)
+    assert not K.is_queue_algo(K.FWD_TILE | K.FWD_STAGE) and not K.is_queue_algo(K.FWD_LANES)
+    assert K.FWD_STAGE & K.FWD_NO_PAD == 0 and K.FWD_STAGE & 0xff == 0
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from bats_gb300 import _lib
+    try:
+        return _lib.load()
+    except RuntimeError as exc:  # pragma: no cover - the library is built by build()
+        pytest.skip(str(exc))
+
+
+def _fwd_queue(L, batch=4, n_post=8, ld=8, algo=0, ws=16, ws_bytes=1 << 20):
+    fake = ctypes.c_void_p(256)  # never dereferenced: the checks below return first
+    return L.bats_lif_forward_fc_queue(fake, fake, 64, fake, ld, batch, n_post, 4, 1.0, 1.0, 0.26, 0.2, fake, fake,
+                                       fake, fake, fake, algo, ctypes.c_void_p(ws) if ws else None, ws_bytes, None)
+
+
+def test_work_queue_forward_argument_checks(lib):
+    L = lib
+    assert L.bats_lif_forward_fc_queue_workspace_bytes(0) == 256
+    assert L.bats_lif_forward_fc_queue_workspace_bytes(4096) == 256 + 4096 * 4
+    assert L.bats_lif_forward_fc_queue_workspace_bytes(33) == 256 + 256
+    assert _fwd_queue(L, batch=0) == 0                      # nothing to do
+    assert _fwd_queue(L, ld=6) == BAD_SHAPE                 # ld not a multiple of 4
+    assert _fwd_queue(L, algo=K.FWD_LANES) == BAD_SHAPE     # the queue runs the tile kernels only
+    assert _fwd_queue(L, ws=0) == NULLPTR
+    assert _fwd_queue(L, ws=8) == WORKSPACE                 # not 16-byte aligned
+    assert _fwd_queue(L, ws_bytes=64) == WORKSPACE          # below bats_lif_forward_fc_queue_workspace_bytes
+    assert b"workspace" in L.bats_last_error()
+
+
+def _grad_adam(L, group=8, ld=128, n_post=100, batch=32, ws_bytes=0, grad=True):
+    fake = ctypes.c_void_p(256)
+    return L.bats_weights_gradient_adam(fake, fake, None, None, 1000, fake, fake, fake, batch, n_post, 4, 50, group,
+                                        fake if grad else None, fake, fake, 0.9, 0.999, 1e-8, 1e-3, fake, fake, fake,
+                                        ld, fake if ws_bytes else None, ws_bytes, None)
+
+
+def test_fused_gradient_adam_argument_checks(lib):
+    L = lib
+    assert _grad_adam(L, group=1) == BAD_SHAPE              # the batch mean needs groups of >= 2 samples
+    assert _grad_adam(L, ld=64) == BAD_SHAPE                # the transposed copy's rows hold n_post
+    assert _grad_adam(L, batch=0) == 0
+    assert _grad_adam(L) == WORKSPACE                       # 4 partials need the workspace
+    assert _grad_adam(L, group=64, grad=False) == NULLPTR   # one partial lives in grad
