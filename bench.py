@@ -304,6 +304,7 @@ def run_ours(args, dist, rank, world):
     if args.workload == "all":
         for variant in ("literal", "active"):
             result[variant]["plain_api"] = plain_api_rate(variant, max(2, args.steps // 4), flush)
+            result[variant]["autograd"] = autograd_rate(variant, max(2, args.steps // 4), flush)
             result[variant]["refkern"] = refkern_rate(variant, 2, flush)
     return result
 
@@ -497,6 +498,30 @@ def plain_api_rate(variant, steps, flush):
     ms, _ = time_steps(step, steps, 1, flush)
     return {"value": B * steps / (ms / 1e3), "unit": "samples/s", "steps": steps,
             "what": "Network/LIFLayer/SpikeCountClassLoss/AdamOptimizer drop-in API, per-sample gradients"}
+
+
+def autograd_rate(variant, steps, flush):
+    """The differentiation pattern: 784-800-800-10 as three bats_gb300.autograd.lif_fc layers (batch 256), a
+    loss written with torch ops on the output spike times (their sum over the slots that hold a spike), and
+    torch.autograd.grad of it with respect to every layer's weights (the exact backward kernels behind the
+    autograd Function, the weight gradient summed over the batch)."""
+    import torch
+    from bats_gb300.autograd import lif_fc
+    ws = [torch.tensor(w, device="cuda", requires_grad=True) for w in make_weights(variant)]
+    ths = thresholds(variant)
+    t, _, _ = make_inputs(B, 0)
+    x0 = torch.tensor(t, device="cuda")
+
+    def step():
+        x = x0
+        for w, th in zip(ws, ths):
+            x, _ = lif_fc(x, w, TAU_S, th, th, K_SPIKE, MAX_SIM)
+        loss = torch.where(torch.isfinite(x), x, torch.zeros_like(x)).sum()
+        torch.autograd.grad(loss, ws, allow_unused=True)
+
+    ms, _ = time_steps(step, steps, 2, flush)
+    return {"value": B * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps, "steps": steps,
+            "what": "forward + torch.autograd.grad through bats_gb300.autograd.lif_fc (weights' gradients)"}
 
 
 def refkern_rate(variant, steps, flush):
@@ -823,7 +848,8 @@ def main():
                    "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (512 MB write)",
                    "cuda_graph": lit["graph"]},
         "roofline": lit["roofline"], "e2e": lit["e2e"], "gpu_launches": lit["gpu_launches"], "clocks": lit["clocks"],
-        "autotuned": lit["autotuned"], "plain_api": lit.get("plain_api"), "refkern": lit.get("refkern"),
+        "autotuned": lit["autotuned"], "plain_api": lit.get("plain_api"), "autograd": lit.get("autograd"),
+        "refkern": lit.get("refkern"),
         "cpu_baseline": cb, "spikes_per_layer": lit["spikes_per_layer_last_step"], "kernels_ms": lit["kernels_ms"],
         "active": act, "serving": serving, "conv": conv, "batching": batching,
     }
