@@ -16,6 +16,12 @@
 // test on each intermediate state; only if some event may cross does it replay the stage from its
 // saved state with the exact solver. The accumulation is the same FMA sequence either way, so the
 // results are those of the reference's one-event-at-a-time loop.
+//
+// Variants, all bit-identical: the stage screen (SCREEN, BATS_FWD_STAGE_SCREEN) first tests a whole
+// stage with one membrane bound per neuron (quiet layers); the persistent work-queue kernel
+// (bats_lif_forward_fc_queue) runs the same per-item code over (sample, tile) items taken longest
+// samples first by resident CTAs (uneven batches); the lanes kernel gives a warp to one (sample, neuron)
+// and 32 events at a time (narrow layers, small batches).
 #include <algorithm>
 #include <cmath>
 #include <limits>
