@@ -126,7 +126,9 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_start, flo
 // c' = c (1 - 2^-19), whose roundings (a few units of 2^-24) stay inside the 2^-20 margin; the same margin
 // covers the reference's fl(b^2) in place of b^2 (a 2^-24 change of b moves V by at most 2^-24 c right of
 // X0, where b/x < c). As for no_crossing, the run must start before 8 tau (X0 < 2981) and every |a_u| must
-// be at least 2^-60 (amag = min_u |a_u|), so that the discriminant's rounding is relative. fminf/fmaxf
+// be at least 2^-60 (amag = min_u |a_u|), so that the discriminant's rounding is relative; with
+// 2^-40 <= c <= 2^20, a state whose roots exist then has 2^-49 < b < c X0 and a < c X0^2 / 4 < 2^42, inside
+// the range where no_crossing's bound on the computed root holds. fminf/fmaxf
 // skip NaN, so the run's last state (a_last, b_last) must be finite: a non-finite state stays non-finite
 // through the later events of the run, and the reference turns it into a NaN spike. No division or square
 // root.
@@ -135,7 +137,7 @@ __device__ __forceinline__ bool stage_no_crossing(float amin, float bmax, float 
     const float x0 = e_first * (1.0f - 0x1p-17f);
     const float lhs = fmaf(fmaxf(bmax, 0.0f), x0, fmaxf(-amin, 0.0f));
     const float rhs = (k.c * (1.0f - 0x1p-19f)) * x0 * x0;
-    return k.fast && k.c >= 0x1p-40f && k.c <= 0x1p40f && x0 > 0.0f && x0 < 2981.0f && amag >= 0x1p-60f &&
+    return k.fast && k.c >= 0x1p-40f && k.c <= 0x1p20f && x0 > 0.0f && x0 < 2981.0f && amag >= 0x1p-60f &&
            fabsf(a_last) <= 0x1p120f &&
            fabsf(b_last) <= 0x1p120f && lhs < rhs;
 }
