@@ -194,6 +194,17 @@ def time_steps(fn, steps, warmup, flush_buf, kernel_timer=None, dist=None):
     return ms, wall
 
 
+def reduce_max(value, dist):
+    """The largest of the ranks' values (the slowest replica's time); the value itself with one process. The
+    reduction runs on a CUDA tensor under NCCL and on a CPU tensor under gloo."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_train_step(variant, graph=True):
     import torch
     from bats_gb300.train import FCLayerSpec, FCTrainStep
@@ -259,10 +270,7 @@ def run_ours(args, dist, rank, world):
         with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
             ms, wall = time_steps(fn, args.steps, args.warmup, flush, dist=dist)
         clocks = clk.summary()
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = reduce_max(ms, dist)
         sps = world * B * args.steps / (ms / 1e3)
         kb = kernel_breakdown(ts)
         top = max(kb, key=kb.get)
