@@ -349,52 +349,55 @@ class FCTrainStep:
         losses are read back when its slot is reused. Results are those of step_host called per batch."""
         dev = self.in_times.device
         if not hasattr(self, "_pipe"):
+            h_in = [torch.empty(self.in_times.shape, dtype=torch.float32, pin_memory=True) for _ in range(2)]
+            h_lab = [torch.empty((self.B,), dtype=torch.int32, pin_memory=True) for _ in range(2)]
+            h_loss = [torch.empty((self.B,), dtype=torch.float32, pin_memory=True) for _ in range(2)]
             self._pipe = {
-                "h_in": [torch.empty(self.in_times.shape, dtype=torch.float32, pin_memory=True) for _ in range(2)],
-                "h_lab": [torch.empty((self.B,), dtype=torch.int32, pin_memory=True) for _ in range(2)],
+                "h_in": h_in, "h_lab": h_lab, "h_loss": h_loss,
+                # numpy views of the pinned slots and the slots' events, made once: each event is re-recorded
+                # once per use of its slot, and every wait or synchronize refers to its latest record
+                "np_in": [t.numpy() for t in h_in], "np_lab": [t.numpy() for t in h_lab],
+                "np_loss": [t.numpy() for t in h_loss],
                 "d_in": [torch.empty_like(self.in_times) for _ in range(2)],
                 "d_lab": [torch.empty_like(self.labels) for _ in range(2)],
-                "h_loss": [torch.empty((self.B,), dtype=torch.float32, pin_memory=True) for _ in range(2)],
+                "staged": [torch.cuda.Event() for _ in range(2)],
+                "consumed": [torch.cuda.Event() for _ in range(2)],
+                "done": [torch.cuda.Event() for _ in range(2)],
                 "copy": torch.cuda.Stream(device=dev),
             }
         P = self._pipe
         comp = torch.cuda.current_stream(dev)
-        staged = [None, None]    # H2D of the slot finished (the pinned buffer may be refilled)
-        consumed = [None, None]  # the step has copied the device slot into its input buffers
-        done = [None, None]      # the step's losses are in the pinned loss slot
+        cs = P["copy"]
+        staged, consumed, done = P["staged"], P["consumed"], P["done"]
+        used = [False, False]  # the slot has been used (its events recorded) in this call
         losses: List[np.ndarray] = []
         order: List[int] = []
         for i, (times, labels) in enumerate(batches):
             k = i & 1
-            if done[k] is not None:  # step i-2: read its losses before the slot is reused
-                done[k].synchronize()
-                losses.append(P["h_loss"][k].numpy().copy())
-            if staged[k] is not None:
-                staged[k].synchronize()
-            P["h_in"][k].numpy()[...] = times
-            P["h_lab"][k].numpy()[...] = labels
-            cs = P["copy"]
-            if consumed[k] is not None:
-                cs.wait_event(consumed[k])
+            if used[k]:
+                done[k].synchronize()       # step i-2 finished: its losses are in the pinned slot
+                losses.append(P["np_loss"][k].copy())
+                staged[k].synchronize()     # its host -> device copies finished: the pinned slot may be refilled
+                cs.wait_event(consumed[k])  # and the device slot was copied into the step's inputs
+            np.copyto(P["np_in"][k], times)
+            np.copyto(P["np_lab"][k], labels, casting="unsafe")
             with torch.cuda.stream(cs):
                 P["d_in"][k].copy_(P["h_in"][k], non_blocking=True)
                 P["d_lab"][k].copy_(P["h_lab"][k], non_blocking=True)
-                staged[k] = torch.cuda.Event()
                 staged[k].record(cs)
             comp.wait_event(staged[k])
             self.in_times.copy_(P["d_in"][k], non_blocking=True)
             self.labels.copy_(P["d_lab"][k], non_blocking=True)
-            consumed[k] = torch.cuda.Event()
             consumed[k].record(comp)
             self.run()
             P["h_loss"][k].copy_(self.loss, non_blocking=True)
-            done[k] = torch.cuda.Event()
             done[k].record(comp)
+            used[k] = True
             order.append(k)
         n = len(order)
         for k in order[max(0, n - 2):]:  # the last one or two steps, in step order
             done[k].synchronize()
-            losses.append(P["h_loss"][k].numpy().copy())
+            losses.append(P["np_loss"][k].copy())
         return losses
 
     @property
