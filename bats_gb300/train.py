@@ -182,17 +182,29 @@ class FCTrainStep:
              ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), self.B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,
              group, 1, ptr(self.grad[li]), ptr(self.ws), self.ws.numel(), s)
 
-    # Kernels launched by each entry point (memsets counted as launches too).
-    KERNELS_PER_CALL = {"sort": 1, "forward": 1, "loss": 1, "prep": 1, "grad_adam": 2, "pre_err": 3, "powers": 1}
-
     @property
     def launches_per_step(self) -> int:
-        """Kernels launched by one step with the current variant choices."""
+        """Kernels of this library launched by one step with the current variant choices (memsets not
+        counted), following the branches of the entry points."""
         return self._count_launches()
 
+    def _kernels_of(self, name: str) -> int:
+        tag, _, kind = name.rpartition(".")  # "L2.grad_adam", "adam.powers", "loss"
+        if tag[:1] == "L" and tag[1:].isdigit():
+            li = int(tag[1:]) - 1
+            spec, n_pre = self.specs[li], self.ev[li].n_neurons
+        if kind == "forward":  # the work queue adds its order kernel
+            return 2 if K.is_queue_algo(self.fwd_algo[li]) else 1
+        if kind == "pre_err":  # narrow layers: one event-parallel kernel; else the tile kernel and the scatter
+            return 1 if spec.n_neurons <= 32 else 2
+        if kind == "grad_adam":  # the gradient, then the fused reduce-Adam, or for few weight tiles and
+            groups = -(-self.B // self.groups[li])  # several partials the reduction and the tiled Adam
+            tiles = -(-n_pre // 32) * -(-spec.n_neurons // 32)
+            return 3 if groups > 1 and tiles < 2 * 152 else 2
+        return 1  # sort, loss, prep, powers
+
     def _count_launches(self):
-        n = sum(self.KERNELS_PER_CALL[name.split(".")[-1]] for name, _ in self.launches)
-        return n + sum(1 for a in self.fwd_algo if K.is_queue_algo(a))  # the queue's order kernel
+        return sum(self._kernels_of(name) for name, _ in self.launches)
 
     def step(self) -> None:
         """One training step on the device-resident inputs (in_times, labels), launched eagerly."""

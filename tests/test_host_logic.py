@@ -69,3 +69,31 @@ def test_fused_gradient_adam_argument_checks(lib):
     assert _grad_adam(L, batch=0) == 0
     assert _grad_adam(L) == WORKSPACE                       # 4 partials need the workspace
     assert _grad_adam(L, group=64, grad=False) == NULLPTR   # one partial lives in grad
+
+
+def _step_stand_in(batch, sizes, groups, algos):
+    """An FCTrainStep's launch list and variant choices without its device buffers."""
+    import types
+    from bats_gb300.train import FCLayerSpec, FCTrainStep
+    ts = FCTrainStep.__new__(FCTrainStep)
+    ts.B = batch
+    ts.specs = [FCLayerSpec(n, 0.13, 1.0, 1.0, 30) for n in sizes[1:]]
+    ts.ev = [types.SimpleNamespace(n_neurons=n) for n in sizes[:-1]]
+    ts.groups = list(groups)
+    ts.fwd_algo = list(algos)
+    L = len(sizes) - 1
+    names = ["adam.powers"] + [f"L{i}.{k}" for i in range(1, L + 1) for k in ("sort", "forward")] + ["loss"]
+    for i in range(L, 0, -1):
+        names += [f"L{i}.prep"] + ([f"L{i}.pre_err"] if i > 1 else []) + [f"L{i}.grad_adam"]
+    ts.launches = [(n, None) for n in names]
+    return ts
+
+
+def test_launch_count_matches_the_launch_lists():
+    """gpu_launches of the bench: the kernels of one train step, as ncu lists them (profiles/
+    train_step_launches_*.md): 21 for the literal 784-800-800-10 step, 15 for the 1024-1024-20 uneven batch
+    with the output layer on the work queue."""
+    lit = _step_stand_in(256, (784, 800, 800, 10), (32, 32, 16), (K.FWD_TILE | K.FWD_STAGE, K.FWD_TILE, K.FWD_TILE))
+    assert lit.launches_per_step == 21
+    bat = _step_stand_in(4096, (1024, 1024, 20), (64, 16), (K.FWD_TILE, K.FWD_QUEUE))
+    assert bat.launches_per_step == 15
