@@ -16,7 +16,7 @@ SolveConst make_solve_const(float c, float dtt, float tau, float max_sim);
 // environment, launches carry programmatic stream serialization, so the next kernel's CTAs become resident
 // while the current kernel's last CTAs finish, and wait there (they read nothing before the wait returns,
 // when the prerequisite grids have completed and their memory is visible). Off by default: measured on a
-// GB300 it gained 1.3 % on the 23-launch literal train step but cost the serving loop 30 % of its median
+// GB300 it gained 1.3 % on the literal train step (26 kernels then) but cost the serving loop 30 % of its median
 // latency (the waiting CTAs hold SM slots that concurrent lanes' kernels need) and the conv step 5 %.
 // Without the attribute the prologue's two instructions are no-ops.
 bool pdl_enabled();
