@@ -157,7 +157,8 @@ __device__ __forceinline__ bool stage_no_crossing(float amin, float bmax, float 
 // instead of double): the FC discriminant through fc_discriminant, which reproduces the reference's
 // double expression without FP64 on its common path, everything else operation for operation.
 template <bool CONV>
-__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_start, float e_next,
+__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_start,
+                                                float e_next,
                                                 const SolveConst& k, int& n, int k_post,
                                                 float* __restrict__ a_out, float* __restrict__ x_out,
                                                 float* __restrict__ t_out, float* __restrict__ z_out) {

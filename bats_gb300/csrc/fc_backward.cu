@@ -853,7 +853,8 @@ extern "C" int bats_backward_prep_layer(const float* post_times, const float* a,
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0, BATS_ERR_BAD_SHAPE, "backward_prep_layer: bad shape");
     const long long total = (long long)batch * n_post;
     if (total == 0) return BATS_OK;
-    BATS_REQUIRE(post_times && a && x && post_exp_tau && errors && tables && nvalid && ((f1 == nullptr) == (f2 == nullptr)),
+    BATS_REQUIRE(post_times && a && x && post_exp_tau && errors && tables && nvalid &&
+                     ((f1 == nullptr) == (f2 == nullptr)),
                  BATS_ERR_NULL, "backward_prep_layer: null pointer");
     if (k_post > 32) {
         BATS_REQUIRE(f1 && f2, BATS_ERR_NULL, "backward_prep_layer: f1/f2 buffers are required when k_post > 32");
@@ -940,7 +941,8 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 1, BATS_ERR_BAD_SHAPE,
                  "weights_gradient: bad shape");
     if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
-    BATS_REQUIRE(post_times && tables && nvalid && grad && ((events && ev_count) || (events_bucketed && bucket_offsets)),
+    BATS_REQUIRE(post_times && tables && nvalid && grad &&
+                     ((events && ev_count) || (events_bucketed && bucket_offsets)),
                  BATS_ERR_NULL, "weights_gradient: null pointer");
     const int n_buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
     const int groups = group == 1 ? batch : (batch + group - 1) / group;

@@ -509,7 +509,8 @@ static int launch_forward_queue(const void* events, const int* ev_count, long lo
 // The stage-screen choice (a run-time flag) mapped onto the kernel template.
 template <int TILE, int SEV, int STAGES, typename... Args>
 static int launch_tile(bool screen, Args... args) {
-    return screen ? launch_forward<TILE, SEV, STAGES, true>(args...) : launch_forward<TILE, SEV, STAGES, false>(args...);
+    return screen ? launch_forward<TILE, SEV, STAGES, true>(args...)
+                  : launch_forward<TILE, SEV, STAGES, false>(args...);
 }
 template <int TILE, int SEV, int STAGES, typename... Args>
 static int launch_queue(bool screen, Args... args) {
@@ -548,7 +549,8 @@ static int forward_fc_impl(const void* events, const int* ev_count, long long ev
     BATS_REQUIRE(((uintptr_t)weights_t & 15) == 0 && ((uintptr_t)events & 15) == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc: weights_t and events must be 16-byte aligned");
     const bats::SolveConst sk = bats::make_solve_const(c, delta_theta_tau, tau, max_simulation);
-    if (algo == BATS_FWD_AUTO) algo = bats_lif_forward_fc_default_algo(batch, n_post, (int)(ev_cap < (1LL << 30) ? ev_cap : (1LL << 30)));
+    if (algo == BATS_FWD_AUTO)
+        algo = bats_lif_forward_fc_default_algo(batch, n_post, (int)(ev_cap < (1LL << 30) ? ev_cap : (1LL << 30)));
     if (algo == BATS_FWD_LANES)
         return bats::launch_forward_lanes<4>(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, sk,
                                              n_spikes, a, x, times, post_exp_tau, pad, stream);
@@ -616,7 +618,8 @@ extern "C" int bats_lif_forward_fc_queue(const void* events, const int* ev_count
                  BATS_ERR_NULL, "lif_forward_fc_queue: null pointer");
     BATS_REQUIRE(((uintptr_t)weights_t & 15) == 0 && ((uintptr_t)events & 15) == 0, BATS_ERR_BAD_SHAPE,
                  "lif_forward_fc_queue: weights_t and events must be 16-byte aligned");
-    BATS_REQUIRE(((uintptr_t)workspace & 15) == 0 && workspace_bytes >= bats_lif_forward_fc_queue_workspace_bytes(batch),
+    BATS_REQUIRE(((uintptr_t)workspace & 15) == 0 &&
+                     workspace_bytes >= bats_lif_forward_fc_queue_workspace_bytes(batch),
                  BATS_ERR_WORKSPACE, "lif_forward_fc_queue: workspace too small or not 16-byte aligned");
     const bats::SolveConst sk = bats::make_solve_const(c, delta_theta_tau, tau, max_simulation);
     int* status = nullptr;

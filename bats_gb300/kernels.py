@@ -376,7 +376,8 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
     # The bucketed copy serves this kernel only when it is grouped by BUCKET_WIDTH pre neurons.
     by_bucket = events.bucketed is not None and events.bucket_width == BUCKET_WIDTH
     call("bats_weights_gradient", ptr(events.events), ptr(events.counts), ptr(events.bucketed if by_bucket else None),
-         ptr(events.bucket_offsets if by_bucket else None), events.cap, ptr(post_times), ptr(tabs.tables), ptr(tabs.nvalid), B, n_post,
+         ptr(events.bucket_offsets if by_bucket else None), events.cap, ptr(post_times), ptr(tabs.tables),
+         ptr(tabs.nvalid), B, n_post,
          k_post, n_pre, g, int(reduce == "mean"), ptr(out), ptr(ws), ws_bytes, stream_ptr())
     return out
 

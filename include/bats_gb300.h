@@ -126,7 +126,8 @@ int bats_lif_forward_fc_algo(const void* events, const int* ev_count, long long 
  * items from the queue, longest samples first, each producer warp streaming its next item while the consumers
  * finish the current one. Outputs, arguments and results are those of bats_lif_forward_fc_algo (bit-identical);
  * algo is BATS_FWD_AUTO or BATS_FWD_TILE (tile width by n_post) or BATS_FWD_TILE64, optionally OR-ed with
- * BATS_FWD_NO_PAD and BATS_FWD_STAGE_SCREEN. The workspace (16-byte aligned, bats_lif_forward_fc_queue_workspace_bytes(batch) bytes) must
+ * BATS_FWD_NO_PAD and BATS_FWD_STAGE_SCREEN. The workspace (16-byte aligned,
+ * bats_lif_forward_fc_queue_workspace_bytes(batch) bytes) must
  * not be used by another launch until this one ends. Replaces the same reference wrappers as
  * bats_lif_forward_fc (get_spike_weights.py:9-18, compute_spike_times.py:11-32); the reference runs one thread
  * per (sample, neuron) with no scheduling of its own. */
