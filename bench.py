@@ -121,12 +121,15 @@ def cpu_baseline(variant, budget_s=12.0, cores=None):
 # GPU helpers
 
 class ClockSampler:
-    """nvidia-smi SM clock / throttle sampling during the timed region."""
+    """nvidia-smi SM clock / throttle sampling during the timed region. The samples go to
+    clocks_<pid>.csv in BATS_GB300_CLOCKS_DIR (default: the system's temporary directory)."""
 
     def __init__(self, index=0):
+        import tempfile
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(os.environ.get("BATS_GB300_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 f"clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
