@@ -321,8 +321,26 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
     }
     __syncthreads();
 
+    if (n <= SORT_THREADS) {
+        // One item per thread: its rank is the number of smaller keys plus the equal keys before it in
+        // compaction order, which is the stable order of the radix passes below, with one barrier.
+        const uint32_t key = tid < n ? ka[tid] : 0u;
+        const V val = tid < n ? va[tid] : V(0);
+        int rank = 0;
+        for (int q = 0; q < n; ++q) {
+            const uint32_t kq = ka[q];
+            rank += (kq < key || (kq == key && q < tid)) ? 1 : 0;
+        }
+        if (tid < n) {
+            kb[rank] = key;
+            vb[rank] = val;
+        }
+        __syncthreads();
+        uint32_t* t0 = ka; ka = kb; kb = t0;
+        V* t1 = va; va = vb; vb = t1;
+    }
     // LSD radix sort on the time key, 4 passes of 8 bits; passes whose digit is uniform are skipped.
-    for (int shift = 0; shift < 32; shift += 8) {
+    for (int shift = 0; n > SORT_THREADS && shift < 32; shift += 8) {
         sh.hist[tid] = 0;
         __syncthreads();
         for (int i = tid; i < n; i += SORT_THREADS) atomicAdd(&sh.hist[(ka[i] >> shift) & 255u], 1);
