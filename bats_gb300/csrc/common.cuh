@@ -74,17 +74,22 @@ struct SolveConst {
 //     bounds z by the root of Q with a lowered by 2^-24 B2 / c). The sign of Q at a point Z is known
 //     when the evaluated Q(Z) exceeds its rounding error (2^-21 of the sum of its terms' magnitudes;
 //     plus 2^-23 B2 / c for conv) in magnitude.
-//     - Right of the window: Z_hi = min(exp(t_next/tau), exp(max_sim/tau)), widened by 2^-19 + 2^-20
-//       for the errors of __expf, of __logf and of the root. If Z_hi lies left of the vertex of Q
-//       (2c Z_hi < sqrt(B2)) and Q(Z_hi) > 0, then Z_hi < z1: the spike time tau ln z exceeds t_next or
-//       max_sim, and the reference rejects it.
+//     - Right of the window: Z_hi = min(exp(t_next/tau), exp(max_sim/tau)), widened by 2^-19 + 2^-20.
+//       If Z_hi lies left of the vertex of Q (2c Z_hi < sqrt(B2)) and Q(Z_hi) > 0 beyond its error bound
+//       (whose 2^-21 relative slack adds at least 2^-20 more), then Z_hi < z1: the spike time tau ln z
+//       exceeds t_next or max_sim, and the reference rejects it. The margin covers the documented error
+//       bounds of __expf (2 + floor(1.173 |x|) ulp, in the event table's exp(t_next/tau)) and of __logf
+//       (3 ulp), the root's and the roundings of t/tau and of tau * ln z, for Z_hi < 2980: a root that
+//       close to Z_hi then lies below e^8, where 3 ulp of the logarithm are 1.5 x 2^-20 (from e^8 = 2980.96
+//       on they double, and a window ending in [2980, 2981) could be claimed wrongly).
 //     - Left of the window (FC only; e_start = exp(t_event/tau) of the window's first event, 0 to skip):
 //       Z_lo = e_start (1 - 2^-17). If Q(Z_lo) < 0 (Z_lo between the roots), or Q(Z_lo) > 0 with Z_lo
 //       right of the vertex (both roots below it), then z1 < Z_lo: the spike time tau ln z lies before
 //       the event (the margin 2^-17 covers __expf, __logf and the root), and the reference rejects it
 //       as not after the last spike or event. Strongly driven neurons that were reset meet this after
 //       most events.
-//     Both tests are used for windows ending before 8 tau (Z < 2981), where those error bounds hold.
+//     The left test is used for Z_lo < 2981 (about 8 tau), where the root's bound holds; its 2^-17 margin
+//     also covers the doubled __logf error of a root in [e^8, 2981).
 //     LEFT = false leaves the left test out (a cheaper first screen; the solver applies it).
 //     No square root or division is needed.
 template <bool CONV, bool LEFT = !CONV>
@@ -98,7 +103,7 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_start, flo
     const float q = fmaf(fmaf(k.c, Z, -b), Z, a);                 // (cZ - b) Z + a
     float err = 0x1p-21f * fmaf(fmaf(k.c, Z, b), Z, a);           // |rounding| + |sqrt(B2) - b| Z
     if (CONV) err = fmaf(0x1p-23f * B2, k.inv_c, err);
-    const bool right_of_window = Z < 2981.0f && (2.0f * k.c) * Z < b * (1.0f - 0x1p-21f) && q > err;
+    const bool right_of_window = Z < 2980.0f && (2.0f * k.c) * Z < b * (1.0f - 0x1p-21f) && q > err;
     bool left_of_window = false;
     if (LEFT && !CONV) {
         const float Zl = e_start * (1.0f - 0x1p-17f);

@@ -1,18 +1,14 @@
 """The per-stage no-crossing screen of the FC forward (stage_no_crossing, bats_gb300/csrc/common.cuh) is
 conservative: whenever it passes a stage, the reference solver accepts no crossing after any event of the
 stage (bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83: discriminant formed in double, root
-z = 2a / (sqrt(tmp) + b), time tau * log z, accepted in (last event or spike, next event]). Host emulation in
-NumPy float32/float64 of both, on random stages chosen so that the screen's bound lies within 10 % of the
+z = 2a / (sqrt(tmp) + b), time tau * __logf(z), accepted in (last event or spike, next event]), for every value
+of __logf and of the stage's first exp(t/tau) within their documented error bounds (tests/_float_model.py).
+Host emulation in NumPy float32/float64 of both, on random stages chosen so that the screen's bound lies within 10 % of the
 threshold (the cases where a loose proof would fail), with states of both signs, times from 0 to past 8 tau,
 and windows that end at the next event or never."""
 import numpy as np
 
-F = np.float32
-
-
-def fmaf(x, y, z):
-    """float32 fused multiply-add (the product of two floats is exact in double; one rounding to float)."""
-    return (x.astype(np.float64) * y.astype(np.float64) + z.astype(np.float64)).astype(F)
+from tests._float_model import F, expf_range, fmaf, reference_may_accept
 
 
 def screen(amin, bmax, amag, a_last, b_last, e_first, c):
@@ -21,22 +17,6 @@ def screen(amin, bmax, amag, a_last, b_last, e_first, c):
     rhs = ((F(c) * F(1.0 - 2.0 ** -19)) * x0 * x0).astype(F)
     fin = (np.abs(a_last) <= F(2.0 ** 120)) & (np.abs(b_last) <= F(2.0 ** 120))
     return (c >= 2.0 ** -40) & (c <= 2.0 ** 20) & (x0 > 0) & (x0 < 2981.0) & (amag >= F(2.0 ** -60)) & fin & (lhs < rhs)
-
-
-def reference_spikes(a, b, last_t, next_t, c, tau, max_sim):
-    """True where the reference solver accepts a crossing after the event (one solve; a spike's reset would
-    only follow an accepted crossing)."""
-    with np.errstate(all="ignore"):
-        b2 = (b * b).astype(F)
-        tmp = (b2.astype(np.float64) - 4.0 * a.astype(np.float64) * np.float64(F(c))).astype(F)
-        ok = ~(tmp < 0)
-        x = np.sqrt(np.where(ok, tmp, F(0))).astype(F)
-        den = (x + b).astype(F)
-        ok &= den != 0
-        z = ((F(2) * a).astype(F) / np.where(den == 0, F(1), den)).astype(F)
-        ok &= ~(z < 0)
-        t = (F(tau) * np.log(z.astype(np.float64)).astype(F)).astype(F)
-        return ok & ~(t <= last_t) & ~(t > max_sim) & ~(t > next_t)
 
 
 def test_screen_never_passes_a_stage_with_a_crossing():
@@ -68,7 +48,7 @@ def test_screen_never_passes_a_stage_with_a_crossing():
             states_b.append(bb)
         A, Bm = np.stack(states_a, 1), np.stack(states_b, 1)
         amin, bmax, amag = A.min(1), Bm.max(1), np.abs(A).min(1)
-        ok = screen(amin, bmax, amag, aa, bb, e[:, 0], c)
+        ok = screen(amin, bmax, amag, aa, bb, expf_range(t[:, 0], tau)[1], c)
         # keep the hard cases: bound within 10 % of the threshold
         x0 = (e[:, 0] * F(1.0 - 2.0 ** -17)).astype(np.float64)
         bound = np.maximum(bmax, 0) / x0 + np.maximum(-amin, 0) / x0 ** 2
@@ -78,7 +58,7 @@ def test_screen_never_passes_a_stage_with_a_crossing():
         never_ends = rng.random(n) < 0.3
         for u in range(sev):
             next_t = np.where(never_ends & (u == sev - 1), np.inf, t[:, u + 1]).astype(F)
-            spk = reference_spikes(A[:, u], Bm[:, u], t[:, u], next_t, c, tau, F(np.inf))
+            spk = reference_may_accept(A[:, u], Bm[:, u], t[:, u], next_t, c, tau, F(np.inf))
             bad = ok & spk
             assert not bad.any(), (f"screen passed a stage whose state {u} crosses: a={A[bad, u][:3]}, "
                                    f"b={Bm[bad, u][:3]}, t={t[bad, u][:3]}, c={c}")
@@ -119,9 +99,9 @@ def test_screen_rejects_stages_that_cross_just_after_their_first_event():
     planted_caught = 0
     for _ in range(5):
         c, tau, t, e, A, Bm = _crossing_stages(rng, 200_000, 0.13)
-        spk = reference_spikes(A[:, 0], Bm[:, 0], t[:, 0], t[:, 1], c, tau, F(np.inf))
+        spk = reference_may_accept(A[:, 0], Bm[:, 0], t[:, 0], t[:, 1], c, tau, F(np.inf))
         assert spk.mean() > 0.9  # the rest cross within a float ulp of the event and are rounded to it
-        ok = screen(A.min(1), Bm.max(1), np.abs(A).min(1), A[:, -1], Bm[:, -1], e[:, 0], c)
+        ok = screen(A.min(1), Bm.max(1), np.abs(A).min(1), A[:, -1], Bm[:, -1], expf_range(t[:, 0], tau)[1], c)
         assert not (ok & spk).any(), "the screen passed a stage that crosses"
         wrong = screen(A.min(1), Bm.max(1), np.abs(A).min(1), A[:, -1], Bm[:, -1], e[:, -1], c)
         planted_caught += int((wrong & spk).sum())
