@@ -73,23 +73,51 @@ def reference_root(a, b, c):
         return ok, z
 
 
-def reference_may_accept(a, b, last_t, next_t, c, tau, max_sim):
-    """True where the reference solver accepts the crossing after the event for some __logf value within its
-    bound: spike time tau * L (one IEEE product) in (last_t, min(next_t, max_sim)]."""
-    ok, z = reference_root(a, b, c)
+def reference_roots_conv(a, b, c):
+    """[(ok, z)] of the conv solver (compute_spike_times_conv.cu:59-71), whose discriminant
+    b * b - 4 * a * c is formed in float: once per evaluation order a compiler may choose (two roundings, or
+    either product fused into the subtraction)."""
     with np.errstate(all="ignore"):
-        l_lo, l_hi = logf_range(np.where(ok & (z > 0), z, F(1)))
-        t_lo = (F(tau) * l_lo).astype(F)
-        t_hi = (F(tau) * l_hi).astype(F)
-        zero = ok & (z == 0)                                      # log(0) = -inf: never after the event
-        return ok & ~zero & (t_hi > np.asarray(last_t, F)) & (t_lo <= F(max_sim)) & (t_lo <= np.asarray(next_t, F))
+        a, b = np.asarray(a, F), np.asarray(b, F)
+        c = F(c)
+        p = ((F(4) * a).astype(F) * c).astype(F)
+        b2 = (b * b).astype(F)
+        tmps = [(b2 - p).astype(F),
+                fmaf(b, b, -p),
+                fmaf(-(F(4) * a).astype(F), np.full_like(a, c), b2)]
+        out = []
+        for tmp in tmps:
+            ok = ~(tmp < 0)
+            x = np.sqrt(np.where(ok, tmp, F(0))).astype(F)
+            den = (x + b).astype(F)
+            ok = ok & (den != 0)
+            z = ((F(2) * a).astype(F) / np.where(den == 0, F(1), den)).astype(F)
+            out.append((ok & ~(z < 0), z))
+        return out
+
+
+def reference_may_accept(a, b, last_t, next_t, c, tau, max_sim, conv=False):
+    """True where the reference solver accepts the crossing after the event for some __logf value within its
+    bound: spike time tau * L (one IEEE product) in (last_t, min(next_t, max_sim)]. conv: the conv solver,
+    for any of its discriminant's evaluation orders."""
+    roots = reference_roots_conv(a, b, c) if conv else [reference_root(a, b, c)]
+    may = np.zeros(np.shape(a), dtype=bool)
+    with np.errstate(all="ignore"):
+        for ok, z in roots:
+            l_lo, l_hi = logf_range(np.where(ok & (z > 0), z, F(1)))
+            t_lo = (F(tau) * l_lo).astype(F)
+            t_hi = (F(tau) * l_hi).astype(F)
+            zero = ok & (z == 0)                                  # log(0) = -inf: never after the event
+            may |= ok & ~zero & (t_hi > np.asarray(last_t, F)) & (t_lo <= F(max_sim)) & (
+                t_lo <= np.asarray(next_t, F))
+    return may
 
 
 def no_crossing(a, b, e_start, e_next, c, e_max=np.inf, widen=1.5 * 2.0 ** -19, cap=2980.0, margin=2.0 ** -17,
-                left=True):
-    """The per-event screen of the FC layer, operation for operation; widen, cap and margin are the right
-    window's widening and upper limit and the left window's margin (parameters so that a test can plant a
-    mistake in the model)."""
+                left=True, conv=False, conv_slack=2.0 ** -23):
+    """The per-event screen, operation for operation (conv: the conv layer's form, which adds conv_slack * B2 / c
+    to the error bound and has no left test); widen, cap, margin and conv_slack are parameters so that a test
+    can plant a mistake in the model."""
     with np.errstate(all="ignore"):
         a, b = np.asarray(a, F), np.asarray(b, F)
         c = F(c)
@@ -102,9 +130,11 @@ def no_crossing(a, b, e_start, e_next, c, e_max=np.inf, widen=1.5 * 2.0 ** -19, 
         z = (np.minimum(np.asarray(e_next, F), F(e_max)) * F(1.0 + widen)).astype(F)
         q = fmaf(fmaf(cc, z, -b), z, a)
         err = (F(2.0 ** -21) * fmaf(fmaf(cc, z, b), z, a)).astype(F)
+        if conv:
+            err = fmaf((F(conv_slack) * b2).astype(F), np.full_like(a, (F(1) / c).astype(F)), err)
         right = (z < F(cap)) & (((F(2) * c) * z).astype(F) < (b * F(1.0 - 2.0 ** -21)).astype(F)) & (q > err)
         left_w = np.zeros_like(right)
-        if left:
+        if left and not conv:
             zl = (np.asarray(e_start, F) * F(1.0 - margin)).astype(F)
             ql = fmaf(fmaf(cc, zl, -b), zl, a)
             errl = (F(2.0 ** -21) * fmaf(fmaf(cc, zl, b), zl, a)).astype(F)

@@ -122,3 +122,29 @@ def test_model_reproduces_the_root_and_brackets_the_log():
     l = np.log(z.astype(np.float64))
     assert np.all(lo <= l) and np.all(hi >= l)
     assert np.all((hi.astype(np.float64) - lo) <= 8 * ulp32(l.astype(F)) + 2 * 2.0 ** -21.41)
+
+
+def test_conv_right_of_window_claims_are_never_accepted():
+    """The conv layer's screen (right-of-window test with the float discriminant's extra slack; no left test)
+    against the conv solver (compute_spike_times_conv.cu:59-77) under every evaluation order of its float
+    discriminant, with roots from near-tangent (delta 1e-9) to far apart (1e6). The slack and the widening
+    together carry the margin: a screen with a widening of 2^-20 and no slack (a planted mistake) claims some
+    windows the reference may accept."""
+    rng = np.random.default_rng(16)
+    claims = planted = 0
+    for tau in TAUS:
+        for theta in THETAS:
+            n = 200_000
+            c = F(F(theta) / tau)
+            t_next = (rng.uniform(0.2, 8.2, n) * np.float64(tau)).astype(F)
+            e_lo, _ = expf_range(t_next, tau)
+            u = rng.uniform(-2.0, 12.0, n) * 2.0 ** -20
+            delta = np.exp(rng.uniform(np.log(1e-9), np.log(1e6), n))
+            a, b = states_with_root_near(e_lo.astype(np.float64), u, delta, c)
+            may = reference_may_accept(a, b, NO_T, t_next, c, tau, F(np.inf), conv=True)
+            claim = no_crossing(a, b, 0.0, e_lo, c, conv=True)
+            assert not (claim & may).any(), "the conv screen claimed a window in which the reference may spike"
+            claims += int(claim.sum())
+            planted += int((no_crossing(a, b, 0.0, e_lo, c, conv=True, widen=2.0 ** -20, conv_slack=0.0) & may).sum())
+    assert claims > 100_000, claims
+    assert planted > 0, "a widening of 2^-20 without the slack should be too small"
