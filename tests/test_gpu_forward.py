@@ -1,7 +1,7 @@
 """GPU parity of the forward path (event sort + FC LIF forward) against the reference's CUDA kernels
 (oracle/refkern.py) and the float64 oracle.
 
-Tolerances (the spec contract): spike times within 1e-5 relative; spike counts exact except
+Tolerances: spike times within 1e-5 relative; spike counts exact except
 for neurons whose membrane maximum lies within 1e-5 (relative) of the threshold, identified by the
 float64 oracle at theta*(1 -+ 1e-5), which are counted and must stay rare.
 """
