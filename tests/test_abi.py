@@ -42,6 +42,80 @@ def test_python_binding_covers_every_declared_symbol():
     assert not missing, missing
 
 
+_SCALARS = {"int": ctypes.c_int, "long long": ctypes.c_longlong, "float": ctypes.c_float,
+            "double": ctypes.c_double, "size_t": ctypes.c_size_t, "unsigned": ctypes.c_uint}
+
+
+def _strip_comments(src):
+    return re.sub(r"//[^\n]*", "", re.sub(r"/\*.*?\*/", "", src, flags=re.S))
+
+
+def _ctype_of(decl, is_return=False):
+    """ctypes class for one C declaration ("const float* times", "int batch", "cudaStream_t stream"), or
+    "pointer" for any data pointer (the binding passes those as void* or as a typed pointer)."""
+    decl = " ".join(decl.replace("const ", " ").split())
+    if is_return:
+        base = decl
+    else:
+        base = decl.rsplit(" ", 1)[0] if " " in decl and not decl.endswith("*") else decl
+    if "*" in decl or base.startswith("cudaStream_t"):
+        return ctypes.c_char_p if is_return and base.startswith("char") else "pointer"
+    base = base.strip()
+    assert base in _SCALARS, f"unmapped C type {base!r} in {decl!r}"
+    return _SCALARS[base]
+
+
+def header_declarations():
+    """{name: (return ctype, [parameter ctypes])} of every function the header declares."""
+    src = _strip_comments(open(HEADER).read())
+    out = {}
+    for m in re.finditer(r"([A-Za-z_][A-Za-z0-9_ ]*\**)\s*\b(bats_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+        ret, name, params = m.group(1).strip(), m.group(2), " ".join(m.group(3).split())
+        args = [] if params in ("", "void") else [_ctype_of(p.strip()) for p in params.split(",")]
+        out[name] = (_ctype_of(ret, is_return=True), args)
+    return out
+
+
+def _same(binding_type, header_type):
+    if header_type == "pointer":
+        return binding_type is ctypes.c_void_p or (isinstance(binding_type, type)
+                                                   and issubclass(binding_type, ctypes._Pointer))
+    return binding_type is header_type
+
+
+def test_binding_signatures_match_the_header():
+    """Every ctypes signature of the binding has the header's parameter count, order and types (a drift
+    would pass wrong values without any error)."""
+    from bats_gb300 import _lib
+    decls = header_declarations()
+    assert set(decls) == set(declared_symbols())
+    wrong = []
+    for name, (ret, args) in decls.items():
+        b_ret, b_args = _lib.SIGNATURES[name]
+        if not _same(b_ret, ret) or len(b_args) != len(args) or not all(map(_same, b_args, args)):
+            wrong.append(name)
+    assert not wrong, wrong
+
+
+def test_layer_struct_matches_the_header():
+    from bats_gb300 import _lib
+    src = _strip_comments(open(HEADER).read())
+    body = re.search(r"typedef struct BatsFcLayer \{(.*?)\} BatsFcLayer;", src, re.S).group(1)
+    fields = []
+    for line in body.split(";"):
+        line = " ".join(line.replace("const ", " ").split())
+        if not line:
+            continue
+        first, *rest = [d.strip() for d in line.split(",")]
+        head, name0 = first.replace("*", "* ").rsplit(" ", 1)
+        for nm in [name0] + rest:
+            ptr = "*" in head or nm.startswith("*")
+            fields.append((nm.lstrip("*"), "pointer" if ptr else _SCALARS[head.strip()]))
+    mirror = _lib.BatsFcLayer._fields_
+    assert [f[0] for f in mirror] == [f[0] for f in fields]
+    assert all(_same(bt, ht) for (_, bt), (_, ht) in zip(mirror, fields))
+
+
 def test_status_strings_and_version(lib):
     lib.bats_status_string.restype = ctypes.c_char_p
     lib.bats_abi_version.restype = ctypes.c_int
