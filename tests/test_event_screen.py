@@ -148,3 +148,18 @@ def test_conv_right_of_window_claims_are_never_accepted():
             planted += int((no_crossing(a, b, 0.0, e_lo, c, conv=True, widen=2.0 ** -20, conv_slack=0.0) & may).sum())
     assert claims > 100_000, claims
     assert planted > 0, "a widening of 2^-20 without the slack should be too small"
+
+
+def test_sweep_script_runs_clean_at_small_size():
+    """tests/screen_sweep.py (the same checks with c and tau drawn over wide ranges, for large host runs)
+    finds no violation on a small run."""
+    import json
+    import os
+    import subprocess
+    import sys
+    script = os.path.join(os.path.dirname(os.path.abspath(__file__)), "screen_sweep.py")
+    r = subprocess.run([sys.executable, script, "--cases-per-kind", "250000", "--workers", "2", "--seed", "7"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    kinds = json.loads(r.stdout.strip().splitlines()[-1])["kinds"]
+    assert all(k["violations"] == 0 and k["claims"] > 0 for k in kinds.values()), kinds
