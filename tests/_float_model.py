@@ -120,18 +120,18 @@ def no_crossing(a, b, e_start, e_next, c, e_max=np.inf, widen=1.5 * 2.0 ** -19, 
     can plant a mistake in the model."""
     with np.errstate(all="ignore"):
         a, b = np.asarray(a, F), np.asarray(b, F)
-        c = F(c)
+        c = np.asarray(c, F)
         ab = np.abs(b)
-        usable = (ab >= F(2.0 ** -60)) & (ab <= F(2.0 ** 60)) & (a <= F(2.0 ** 60))
+        usable = (c > 0) & (ab >= F(2.0 ** -60)) & (ab <= F(2.0 ** 60)) & (a <= F(2.0 ** 60))
         p_hi = ((F(4) * a).astype(F) * c).astype(F)
         b2 = (b * b).astype(F)
         level1 = (a <= 0) | (b < 0) | (b2 < p_hi)
         cc = np.full_like(a, c)
-        z = (np.minimum(np.asarray(e_next, F), F(e_max)) * F(1.0 + widen)).astype(F)
+        z = (np.fmin(np.asarray(e_next, F), np.asarray(e_max, F)) * F(1.0 + widen)).astype(F)  # fminf: NaN-skipping
         q = fmaf(fmaf(cc, z, -b), z, a)
         err = (F(2.0 ** -21) * fmaf(fmaf(cc, z, b), z, a)).astype(F)
         if conv:
-            err = fmaf((F(conv_slack) * b2).astype(F), np.full_like(a, (F(1) / c).astype(F)), err)
+            err = fmaf((F(conv_slack) * b2).astype(F), np.full_like(a, (F(1) / c).astype(F)), err)  # k.inv_c
         right = (z < F(cap)) & (((F(2) * c) * z).astype(F) < (b * F(1.0 - 2.0 ** -21)).astype(F)) & (q > err)
         left_w = np.zeros_like(right)
         if left and not conv:
@@ -141,6 +141,18 @@ def no_crossing(a, b, e_start, e_next, c, e_max=np.inf, widen=1.5 * 2.0 ** -19, 
             left_w = (zl > 0) & (zl < F(2981)) & (
                 (ql < -errl) | ((ql > errl) & (((F(2) * c) * zl).astype(F) > (b * F(1.0 + 2.0 ** -21)).astype(F))))
         return usable & (level1 | right | left_w)
+
+
+def stage_no_crossing(amin, bmax, amag, a_last, b_last, e_first, c):
+    """The per-stage screen, operation for operation."""
+    with np.errstate(all="ignore"):
+        c = np.asarray(c, F)
+        x0 = (np.asarray(e_first, F) * F(1.0 - 2.0 ** -17)).astype(F)
+        lhs = fmaf(np.fmax(bmax, F(0)), x0, np.fmax(-np.asarray(amin, F), F(0)))  # fmaxf: NaN-skipping
+        rhs = (((c * F(1.0 - 2.0 ** -19)).astype(F) * x0).astype(F) * x0).astype(F)
+        fin = (np.abs(a_last) <= F(2.0 ** 120)) & (np.abs(b_last) <= F(2.0 ** 120))
+        return ((c >= F(2.0 ** -40)) & (c <= F(2.0 ** 20)) & (x0 > 0) & (x0 < F(2981)) & (amag >= F(2.0 ** -60))
+                & fin & (lhs < rhs))
 
 
 def states_with_root_near(x, rel, delta, c, larger=False):

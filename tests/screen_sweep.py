@@ -21,7 +21,7 @@ import numpy as np
 sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 from tests._float_model import (F, expf_range, fmaf, no_crossing, reference_may_accept,  # noqa: E402
-                                states_with_root_near)
+                                stage_no_crossing, states_with_root_near)
 
 KINDS = ("right", "right_8tau", "max_sim", "left", "conv", "stage")
 CHUNK = 250_000
@@ -35,16 +35,6 @@ def _draw_c_tau(rng):
 
 def _delta(rng, n, lo=1e-9, hi=1e6):
     return np.exp(rng.uniform(np.log(lo), np.log(hi), n))
-
-
-def stage_screen(amin, bmax, amag, a_last, b_last, e_first, c):
-    """stage_no_crossing, operation for operation."""
-    x0 = (e_first * F(1.0 - 2.0 ** -17)).astype(F)
-    lhs = fmaf(np.maximum(bmax, F(0)), x0, np.maximum(-amin, F(0)))
-    rhs = ((F(c) * F(1.0 - 2.0 ** -19)) * x0 * x0).astype(F)
-    fin = (np.abs(a_last) <= F(2.0 ** 120)) & (np.abs(b_last) <= F(2.0 ** 120))
-    return ((c >= 2.0 ** -40) & (c <= 2.0 ** 20) & (x0 > 0) & (x0 < 2981.0) & (amag >= F(2.0 ** -60)) & fin
-            & (lhs < rhs))
 
 
 def _chunk(kind, rng, n):
@@ -98,7 +88,7 @@ def _chunk(kind, rng, n):
                 Bm.append(bb)
             A, Bm = np.stack(A, 1), np.stack(Bm, 1)
             _, e_hi = expf_range(t[:, 0], tau)
-            claim = stage_screen(A.min(1), Bm.max(1), np.abs(A).min(1), aa, bb, e_hi, c)
+            claim = stage_no_crossing(A.min(1), Bm.max(1), np.abs(A).min(1), aa, bb, e_hi, c)
             never_ends = rng.random(n) < 0.3
             may = np.zeros(n, dtype=bool)
             for k in range(sev):

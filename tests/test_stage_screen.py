@@ -9,14 +9,7 @@ and windows that end at the next event or never."""
 import numpy as np
 
 from tests._float_model import F, expf_range, fmaf, reference_may_accept
-
-
-def screen(amin, bmax, amag, a_last, b_last, e_first, c):
-    x0 = (e_first * F(1.0 - 2.0 ** -17)).astype(F)
-    lhs = fmaf(np.maximum(bmax, F(0)), x0, np.maximum(-amin, F(0)))
-    rhs = ((F(c) * F(1.0 - 2.0 ** -19)) * x0 * x0).astype(F)
-    fin = (np.abs(a_last) <= F(2.0 ** 120)) & (np.abs(b_last) <= F(2.0 ** 120))
-    return (c >= 2.0 ** -40) & (c <= 2.0 ** 20) & (x0 > 0) & (x0 < 2981.0) & (amag >= F(2.0 ** -60)) & fin & (lhs < rhs)
+from tests._float_model import stage_no_crossing as screen
 
 
 def test_screen_never_passes_a_stage_with_a_crossing():
