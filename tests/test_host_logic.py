@@ -1,13 +1,16 @@
 """Host-side logic that needs no GPU: the autotuner's choice rule, the kernel-variant flags of the Python
 binding, and the argument checks of the entry points added for the work-queue forward and the fused
-gradient-Adam (they return their status before any CUDA call)."""
+gradient-Adam (they return their status before any CUDA call), and that the package never reaches into the
+oracle."""
 import ctypes
+import os
 
 import pytest
 
 from bats_gb300 import kernels as K
 from bats_gb300.autotune import _choose
 
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 BAD_SHAPE, NULLPTR, WORKSPACE = 1, 2, 4
 
 
@@ -97,3 +100,25 @@ def test_launch_count_matches_the_launch_lists():
     assert lit.launches_per_step == 21
     bat = _step_stand_in(4096, (1024, 1024, 20), (64, 16), (K.FWD_TILE, K.FWD_QUEUE))
     assert bat.launches_per_step == 15
+
+
+def test_product_does_not_import_the_oracle():
+    """The oracle is test infrastructure: no module of the package imports it, and no native source includes
+    anything from it."""
+    import ast
+    pkg = os.path.join(ROOT, "bats_gb300")
+    offenders = []
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            path = os.path.join(dirpath, f)
+            if f.endswith(".py"):
+                tree = ast.parse(open(path).read(), filename=path)
+                for node in ast.walk(tree):
+                    names = ([a.name for a in node.names] if isinstance(node, ast.Import)
+                             else [node.module or ""] if isinstance(node, ast.ImportFrom) else [])
+                    if any(n == "oracle" or n.startswith("oracle.") for n in names):
+                        offenders.append(path)
+            elif f.endswith((".cu", ".cuh", ".h", ".cpp")):
+                if any(line.lstrip().startswith("#include") and "oracle" in line for line in open(path)):
+                    offenders.append(path)
+    assert not offenders, offenders
