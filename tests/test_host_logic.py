@@ -122,3 +122,14 @@ def test_product_does_not_import_the_oracle():
                 if any(line.lstrip().startswith("#include") and "oracle" in line for line in open(path)):
                     offenders.append(path)
     assert not offenders, offenders
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """Without the built library every entry point raises: there is no fallback to compute elsewhere."""
+    from bats_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libbats_gb300.so"))
+    with pytest.raises(RuntimeError, match="missing"):
+        _lib.load()
+    with pytest.raises(RuntimeError, match="missing"):
+        _lib.call("bats_abi_version")
