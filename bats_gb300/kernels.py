@@ -30,6 +30,15 @@ def _c(t, dtype=F32):
     return t.contiguous()
 
 
+def _out(out, shape, dtype=F32):
+    """A caller-supplied output: the kernels write through its raw pointer in row-major order, so it must be a
+    contiguous CUDA tensor of exactly `shape` and `dtype` (any other layout would be filled wrongly)."""
+    if (not torch.is_tensor(out) or not out.is_cuda or out.dtype != dtype or not out.is_contiguous()
+            or tuple(out.shape) != tuple(shape)):
+        raise ValueError(f"out must be a contiguous CUDA {dtype} tensor of shape {tuple(shape)}")
+    return out
+
+
 def lif_constants(tau_s, theta, delta_theta):
     """(tau, theta/tau, delta_theta/tau) as float32, the way LIFLayer.__init__ forms them
     (bats/Layers/LIFLayer.py:16-19): tau = float32(2 tau_s), the quotients taken in double and rounded."""
@@ -49,6 +58,8 @@ def transpose_weights(weights, out=None):
     ld = padded_ld(n_post)
     if out is None:
         out = torch.zeros((n_pre, ld), dtype=F32, device=w.device)
+    else:
+        out = _out(out, (n_pre, ld))
     call("bats_transpose", ptr(w), n_post, n_pre, ptr(out), ld, stream_ptr())
     return out
 
@@ -371,6 +382,8 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
         shape = (n_post, n_pre)
     if out is None:
         out = torch.empty(shape, dtype=F32, device=dev)
+    else:
+        out = _out(out, shape)
     ws_bytes = call_size("bats_weights_gradient_workspace_bytes", B, n_post, n_pre, g)
     ws = workspace(ws_bytes, dev) if ws_bytes else None
     # The bucketed copy serves this kernel only when it is grouped by BUCKET_WIDTH pre neurons.
@@ -407,6 +420,8 @@ def pre_errors(events: Events, weights_t, post_times, tabs: BackwardTables, tau_
     dev = post_times.device
     if out is None:
         out = torch.empty((B, events.n_neurons, events.k), dtype=F32, device=dev)
+    else:
+        out = _out(out, (B, events.n_neurons, events.k))
     ws_bytes = call_size("bats_pre_errors_workspace_bytes", B, events.cap, n_post)
     ws = workspace(ws_bytes, dev) if ws_bytes else None
     call("bats_pre_errors", ptr(events.events), ptr(events.slots), ptr(events.counts), events.cap, ptr(weights_t),

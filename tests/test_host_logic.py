@@ -133,3 +133,19 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         _lib.load()
     with pytest.raises(RuntimeError, match="missing"):
         _lib.call("bats_abi_version")
+
+
+def test_caller_outputs_are_checked_before_any_call():
+    """An `out` tensor that the kernels could not fill in row-major order is refused with ValueError before
+    the library is called (here: host tensors, a wrong shape, a transposed view)."""
+    from types import SimpleNamespace
+    import torch
+    post = torch.zeros((2, 3, 4))
+    ev = SimpleNamespace(n_neurons=5, k=1, cap=5)
+    with pytest.raises(ValueError, match="contiguous CUDA"):
+        K.weights_gradient(ev, post, None, 5, per_sample=True, out=torch.zeros((2, 3, 5)))
+    with pytest.raises(ValueError, match="contiguous CUDA"):
+        K.weights_gradient(ev, post, None, 5, per_sample=False, group=2, out=torch.zeros((5, 3)).t())
+    with pytest.raises(ValueError, match="contiguous CUDA"):
+        K.pre_errors(ev, None, post, None, 0.13, 0.26, out=torch.zeros((2, 5, 2)))
+    assert K._out.__doc__
