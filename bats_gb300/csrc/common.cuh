@@ -62,7 +62,8 @@ struct SolveConst {
 
 // True when the reference solver provably accepts no crossing in the window (t_last, t_next] for the
 // state (a, b), so that its exact evaluation can be skipped without changing any result. With
-// B2 = fl(b*b), D = B2 - 4ac and (|b| a normal float, a <= 2^60, c > 0):
+// B2 = fl(b*b), D = B2 - 4ac and (|b| a normal float, |a| <= 2^60, c > 0; a state below -2^60 can
+// overflow 2a and the discriminant, where the reference's z = 2a/(x + b) is NaN and accepted as a spike):
 //   * a <= 0 or b < 0: the reference's x = sqrt(tmp) satisfies x >= |b| (a <= 0) or x <= |b|
 //     (a > 0, b < 0), because sqrt(fl(b^2)) == |b| in binary floating point; then x + b == 0, or
 //     z = 2a/(x + b) <= 0, and the log of a non-positive z is rejected.
@@ -95,7 +96,7 @@ struct SolveConst {
 template <bool CONV, bool LEFT = !CONV>
 __device__ __forceinline__ bool no_crossing(float a, float b, float e_start, float e_next, const SolveConst& k) {
     const float ab = fabsf(b);
-    const bool usable = k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && a <= 0x1p60f;
+    const bool usable = k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && fabsf(a) <= 0x1p60f;
     const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), k.c);
     const float B2 = __fmul_rn(b, b);
     const bool level1 = a <= 0.0f || b < 0.0f || B2 < p_hi;

@@ -122,7 +122,7 @@ def no_crossing(a, b, e_start, e_next, c, e_max=np.inf, widen=1.5 * 2.0 ** -19, 
         a, b = np.asarray(a, F), np.asarray(b, F)
         c = np.asarray(c, F)
         ab = np.abs(b)
-        usable = (c > 0) & (ab >= F(2.0 ** -60)) & (ab <= F(2.0 ** 60)) & (a <= F(2.0 ** 60))
+        usable = (c > 0) & (ab >= F(2.0 ** -60)) & (ab <= F(2.0 ** 60)) & (np.abs(a) <= F(2.0 ** 60))
         p_hi = ((F(4) * a).astype(F) * c).astype(F)
         b2 = (b * b).astype(F)
         level1 = (a <= 0) | (b < 0) | (b2 < p_hi)

@@ -1,0 +1,154 @@
+"""The FC crossing solver of the forward kernels (solve_crossings<false>, bats_gb300/csrc/common.cuh), compiled for
+the host, gives bit for bit the results of the reference's solver loop
+(bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83, restated below in plain C from its
+behaviour: discriminant (float)(fl(b*b) - 4.0*a*c) in double, x = sqrtf, z = 2a / (x + b), t = tau * log z,
+accepted in (last, min(next, max_sim)], reset b -= (delta_theta/tau) z, at most K spikes). Both sides use the
+host's logf and expf, which lie within the documented error bounds of __logf and __expf, so the check covers
+what the screens may skip (no_crossing must never drop a spike the loop accepts), the FP64-free
+discriminant, the window tests, the reset and the K cap. Both are compiled without floating-point
+contraction, the same policy on both sides (on the GPU, nvcc and the reference's runtime compiler both
+contract the reset). Cases: roots within a few 2^-20 of the window's start or end, windows near 8 tau,
+strongly driven neurons that spike several times in one window, and operands of every magnitude, sign and
+class."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+from tests.test_screen_source import _cuda_include
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+PROGRAM = r'''
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <cuda_runtime.h>
+// Host stand-ins for the device-only names that common.cuh uses.
+#define __fmul_rn(x, y) ((x) * (y))
+#define __logf(x) logf(x)
+static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
+static inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+template <class T> static inline T __shfl_xor_sync(unsigned, T v, int, int = 32) { return v; }
+static const uint3 threadIdx = {0, 0, 0};
+#include "common.cuh"
+
+// The reference's per-event solver loop, restated from its behaviour.
+static bool reference_solve(float c, float dtt, float tau, float max_sim, float a, float& b, float last, float next,
+                            int& n, int K, float* ao, float* xo, float* to, float* zo) {
+    while (true) {
+        const float bb = b * b;
+        float tmp = (float)((double)bb - 4.0 * (double)a * (double)c);
+        if (tmp < 0) return false;
+        const float x = sqrtf(tmp);
+        tmp = x + b;
+        if (tmp == 0.0f) return false;
+        const float z = 2 * a / tmp;
+        if (z < 0) return false;
+        tmp = tau * logf(z);
+        if (tmp <= last || tmp > max_sim || tmp > next) return false;
+        ao[n] = a; xo[n] = x; to[n] = tmp; zo[n] = z;
+        last = tmp;
+        b -= dtt * z;
+        n++;
+        if (n >= K) return true;
+    }
+}
+
+static bool same(float x, float y) { uint32_t a, b; std::memcpy(&a, &x, 4); std::memcpy(&b, &y, 4); return a == b; }
+
+int main(int argc, char** argv) {
+    const long long N = std::atoll(argv[1]);
+    std::mt19937_64 rng(2024);
+    std::uniform_real_distribution<double> U(0, 1);
+    auto logu = [&](double lo, double hi) { return std::exp(std::log(lo) + U(rng) * (std::log(hi) - std::log(lo))); };
+    const float specials[] = {0.0f, -0.0f, 1e-45f, 1e-38f, INFINITY, -INFINITY, NAN, 1.0f, -1.0f, 3e38f};
+    long long bad = 0, spikes = 0, screened = 0, multi = 0;
+    for (long long q = 0; q < N; ++q) {
+        const float tau = (float)logu(1e-3, 10.0);
+        const float c = (float)logu(std::ldexp(1.0, -20), std::ldexp(1.0, 12));
+        const float dtt = (float)(c * U(rng) * 2.0);
+        const float max_sim = U(rng) < 0.5 ? INFINITY : (float)(tau * U(rng) * 9.0);
+        const double xt = (q % 8 == 0) ? 8.0 + (U(rng) - 0.8) * 5e-4 : U(rng) * 8.2;
+        const float t_ev = (float)(tau * xt);
+        const float next = U(rng) < 0.3 ? INFINITY : (float)(t_ev + tau * logu(1e-7, 1.0));
+        const float e_ev = expf(t_ev / tau), e_nx = expf(next / tau);
+        double x = e_ev;
+        float a, b;
+        switch (q % 4) {
+            case 0: {  // a root within a few 2^-20 of the window's start or end
+                const double edge = (U(rng) < 0.5 || !std::isfinite(e_nx)) ? (double)e_ev : (double)e_nx;
+                const double delta = logu(1e-9, 1e6), s = std::sqrt(delta / (1 + delta));
+                const double root = edge * (1 + (U(rng) - 0.5) * std::ldexp(48.0, -20));
+                const double bd = (U(rng) < 0.5) ? 2 * c * root / (1 - s) : 2 * c * root / (1 + s);
+                b = (float)bd;
+                a = (float)(bd * bd / (4.0 * c * (1 + delta)));
+                break;
+            }
+            case 1: {  // strongly driven: crosses soon after the event, several times after resets
+                const double bd = 2 * c * x * (1 + logu(1e-6, 30.0));
+                b = (float)bd;
+                a = (float)(bd * bd / (4.0 * c) * (1 - U(rng)));
+                break;
+            }
+            case 2:
+                a = (float)((U(rng) < 0.5 ? -1 : 1) * logu(1e-30, 1e30));
+                b = (float)((U(rng) < 0.7 ? 1 : -1) * logu(1e-30, 1e30));
+                break;
+            default:
+                a = U(rng) < 0.5 ? specials[rng() % 10] : (float)((U(rng) - 0.3) * 100);
+                b = U(rng) < 0.5 ? specials[rng() % 10] : (float)((U(rng) - 0.3) * 100);
+                break;
+        }
+        bats::SolveConst k{};
+        k.c = c; k.dtt = dtt; k.tau = tau; k.max_sim = max_sim;
+        const double em = std::exp((double)max_sim / (double)tau);
+        k.e_max = std::isfinite(em) && em < 3.0e38 ? (float)em : INFINITY;
+        k.inv_c = 1.0f / c;
+        k.fast = true;
+        const int K = 1 + (int)(rng() % 30), n0 = (int)(rng() % K);
+        float ao1[32], xo1[32], to1[32], zo1[32], ao2[32], xo2[32], to2[32], zo2[32];
+        std::memset(ao1, 0, sizeof ao1); std::memcpy(ao2, ao1, sizeof ao1);
+        std::memcpy(xo1, ao1, sizeof ao1); std::memcpy(xo2, ao1, sizeof ao1);
+        std::memcpy(to1, ao1, sizeof ao1); std::memcpy(to2, ao1, sizeof ao1);
+        std::memcpy(zo1, ao1, sizeof ao1); std::memcpy(zo2, ao1, sizeof ao1);
+        float b1 = b, b2 = b;
+        int n1 = n0, n2 = n0;
+        const bool r1 = reference_solve(c, dtt, tau, max_sim, a, b1, t_ev, next, n1, K, ao1, xo1, to1, zo1);
+        if (bats::no_crossing<false>(a, b, e_ev, e_nx, k)) ++screened;
+        const bool r2 = bats::solve_crossings<false>(a, b2, t_ev, next, e_ev, e_nx, k, n2, K, ao2, xo2, to2, zo2);
+        bool ok = r1 == r2 && n1 == n2 && same(b1, b2);
+        for (int i = n0; ok && i < n1; ++i)
+            ok = same(ao1[i], ao2[i]) && same(xo1[i], xo2[i]) && same(to1[i], to2[i]) && same(zo1[i], zo2[i]);
+        spikes += n1 - n0;
+        multi += n1 - n0 >= 2;
+        if (!ok) {
+            if (bad < 5) std::printf("mismatch a=%a b=%a c=%a tau=%a t=%a next=%a: n %d/%d\n", a, b, c, tau, t_ev, next, n1, n2);
+            ++bad;
+        }
+    }
+    std::printf("%lld mismatches of %lld; spikes %lld; multi %lld; screened %lld\n", bad, N, spikes, multi, screened);
+    return bad != 0;
+}
+'''
+
+
+def test_solver_matches_the_reference_loop(tmp_path):
+    inc = _cuda_include()
+    if shutil.which("g++") is None or inc is None:
+        pytest.skip("no host C++ compiler or CUDA headers")
+    src, exe = tmp_path / "solver.cpp", tmp_path / "solver"
+    src.write_text(PROGRAM)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "bats_gb300", "csrc"),
+                    "-I", inc, "-o", str(exe), str(src)], check=True)
+    r = subprocess.run([str(exe), "4000000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    words = r.stdout.split()
+    assert words[0] == "0", r.stdout
+    spikes, multi, screened = int(words[5].rstrip(";")), int(words[7].rstrip(";")), int(words[9])
+    assert spikes > 500_000 and multi > 50_000 and screened > 1_000_000, r.stdout
