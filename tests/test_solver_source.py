@@ -1,6 +1,7 @@
-"""The FC crossing solver of the forward kernels (solve_crossings<false>, bats_gb300/csrc/common.cuh), compiled for
-the host, gives bit for bit the results of the reference's solver loop
-(bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83, restated below in plain C from its
+"""The crossing solver of the forward kernels (solve_crossings, bats_gb300/csrc/common.cuh; FC and conv forms),
+compiled for the host, gives bit for bit the results of the reference's solver loops
+(bats/CudaKernels/CuFiles/Inference/compute_spike_times.cu:53-83 and compute_spike_times_conv.cu:59-90, whose
+discriminant is formed in float; restated below in plain C from its
 behaviour: discriminant (float)(fl(b*b) - 4.0*a*c) in double, x = sqrtf, z = 2a / (x + b), t = tau * log z,
 accepted in (last, min(next, max_sim)], reset b -= (delta_theta/tau) z, at most K spikes). Both sides use the
 host's logf and expf, which lie within the documented error bounds of __logf and __expf, so the check covers
@@ -38,12 +39,14 @@ template <class T> static inline T __shfl_xor_sync(unsigned, T v, int, int = 32)
 static const uint3 threadIdx = {0, 0, 0};
 #include "common.cuh"
 
-// The reference's per-event solver loop, restated from its behaviour.
+// The reference's per-event solver loop, restated from its behaviour (conv: the conv layer's loop, whose
+// discriminant is formed in float).
+template <bool CONV>
 static bool reference_solve(float c, float dtt, float tau, float max_sim, float a, float& b, float last, float next,
                             int& n, int K, float* ao, float* xo, float* to, float* zo) {
     while (true) {
         const float bb = b * b;
-        float tmp = (float)((double)bb - 4.0 * (double)a * (double)c);
+        float tmp = CONV ? bb - 4 * a * c : (float)((double)bb - 4.0 * (double)a * (double)c);
         if (tmp < 0) return false;
         const float x = sqrtf(tmp);
         tmp = x + b;
@@ -62,8 +65,8 @@ static bool reference_solve(float c, float dtt, float tau, float max_sim, float 
 
 static bool same(float x, float y) { uint32_t a, b; std::memcpy(&a, &x, 4); std::memcpy(&b, &y, 4); return a == b; }
 
-int main(int argc, char** argv) {
-    const long long N = std::atoll(argv[1]);
+template <bool CONV>
+static int run(long long N) {
     std::mt19937_64 rng(2024);
     std::uniform_real_distribution<double> U(0, 1);
     auto logu = [&](double lo, double hi) { return std::exp(std::log(lo) + U(rng) * (std::log(hi) - std::log(lo))); };
@@ -119,9 +122,9 @@ int main(int argc, char** argv) {
         std::memcpy(zo1, ao1, sizeof ao1); std::memcpy(zo2, ao1, sizeof ao1);
         float b1 = b, b2 = b;
         int n1 = n0, n2 = n0;
-        const bool r1 = reference_solve(c, dtt, tau, max_sim, a, b1, t_ev, next, n1, K, ao1, xo1, to1, zo1);
-        if (bats::no_crossing<false>(a, b, e_ev, e_nx, k)) ++screened;
-        const bool r2 = bats::solve_crossings<false>(a, b2, t_ev, next, e_ev, e_nx, k, n2, K, ao2, xo2, to2, zo2);
+        const bool r1 = reference_solve<CONV>(c, dtt, tau, max_sim, a, b1, t_ev, next, n1, K, ao1, xo1, to1, zo1);
+        if (bats::no_crossing<CONV>(a, b, e_ev, e_nx, k)) ++screened;
+        const bool r2 = bats::solve_crossings<CONV>(a, b2, t_ev, next, e_ev, e_nx, k, n2, K, ao2, xo2, to2, zo2);
         bool ok = r1 == r2 && n1 == n2 && same(b1, b2);
         for (int i = n0; ok && i < n1; ++i)
             ok = same(ao1[i], ao2[i]) && same(xo1[i], xo2[i]) && same(to1[i], to2[i]) && same(zo1[i], zo2[i]);
@@ -135,10 +138,16 @@ int main(int argc, char** argv) {
     std::printf("%lld mismatches of %lld; spikes %lld; multi %lld; screened %lld\n", bad, N, spikes, multi, screened);
     return bad != 0;
 }
+
+int main(int argc, char** argv) {
+    const long long N = std::atoll(argv[1]);
+    return std::atoi(argv[2]) ? run<true>(N) : run<false>(N);
+}
 '''
 
 
-def test_solver_matches_the_reference_loop(tmp_path):
+@pytest.mark.parametrize("conv", [0, 1], ids=["fc", "conv"])
+def test_solver_matches_the_reference_loop(tmp_path, conv):
     inc = _cuda_include()
     if shutil.which("g++") is None or inc is None:
         pytest.skip("no host C++ compiler or CUDA headers")
@@ -146,7 +155,7 @@ def test_solver_matches_the_reference_loop(tmp_path):
     src.write_text(PROGRAM)
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "bats_gb300", "csrc"),
                     "-I", inc, "-o", str(exe), str(src)], check=True)
-    r = subprocess.run([str(exe), "4000000"], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([str(exe), "4000000", str(conv)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     words = r.stdout.split()
     assert words[0] == "0", r.stdout
