@@ -161,3 +161,92 @@ def test_solver_matches_the_reference_loop(tmp_path, conv):
     assert words[0] == "0", r.stdout
     spikes, multi, screened = int(words[5].rstrip(";")), int(words[7].rstrip(";")), int(words[9])
     assert spikes > 500_000 and multi > 50_000 and screened > 1_000_000, r.stdout
+
+
+MERGED = PROGRAM.split("// The reference's per-event solver loop")[0] + r'''
+static bool same(float x, float y) { uint32_t a, b; std::memcpy(&a, &x, 4); std::memcpy(&b, &y, 4); return a == b; }
+
+// Conv layer, finite exponentials: the reference visits every event of the sample, with weight 0 outside the
+// neuron's receptive field, and solves each window (t_i, t_{i+1}] (compute_spike_times_conv.cu:155-172); the
+// conv kernel visits only the relevant events and solves the merged window between them, then (t_last, inf).
+int main(int argc, char** argv) {
+    const long long N = std::atoll(argv[1]);
+    std::mt19937_64 rng(77);
+    std::uniform_real_distribution<double> U(0, 1);
+    std::normal_distribution<double> G(0, 1);
+    long long bad = 0, spikes = 0;
+    for (long long q = 0; q < N; ++q) {
+        const int E = 1 + (int)(rng() % 60), K = 1 + (int)(rng() % 12);
+        const float tau_s = (float)(0.02 + U(rng) * 0.3), tau = 2 * tau_s;
+        const float theta = (float)(0.05 + U(rng) * 1.5), c = theta / tau, dtt = (float)(U(rng) * 2 * theta) / tau;
+        const float max_sim = U(rng) < 0.5 ? INFINITY : (float)(U(rng) * 0.4);
+        float t[64], es[64], e[64], w[64];
+        bool rel[64];
+        for (int i = 0; i < E; ++i) t[i] = (float)(U(rng) * 0.3);
+        std::sort(t, t + E);
+        if (q % 5 == 0) for (int i = 1; i < E; i += 3) t[i] = t[i - 1];   // ties
+        const double scale = std::exp(G(rng));
+        for (int i = 0; i < E; ++i) {
+            es[i] = expf(t[i] / tau_s); e[i] = expf(t[i] / tau);
+            rel[i] = U(rng) < 0.35;
+            w[i] = (float)((G(rng) + 0.8) * scale);
+        }
+        bats::SolveConst k{};
+        k.c = c; k.dtt = dtt; k.tau = tau; k.max_sim = max_sim;
+        const double em = std::exp((double)max_sim / (double)tau);
+        k.e_max = std::isfinite(em) && em < 3.0e38 ? (float)em : INFINITY;
+        k.inv_c = 1.0f / c; k.fast = true;
+        float ao1[16], xo1[16], to1[16], zo1[16], ao2[16], xo2[16], to2[16], zo2[16];
+        // the reference's loop over every event
+        float a = 0, b = 0;
+        int n1 = 0;
+        for (int i = 0; i < E; ++i) {
+            const float wi = rel[i] ? w[i] : 0.0f;
+            a += wi * es[i];
+            b += wi * e[i];
+            const float next = i + 1 < E ? t[i + 1] : INFINITY;
+            if (bats::solve_crossings<true>(a, b, t[i], next, 0.0f, i + 1 < E ? e[i + 1] : INFINITY, k, n1, K,
+                                            ao1, xo1, to1, zo1)) break;
+        }
+        // the conv kernel's loop over the relevant events only
+        float a2 = 0, b2 = 0, last = 0;
+        int n2 = 0;
+        bool has_prev = false, done = false;
+        for (int i = 0; i < E && !done; ++i) {
+            if (!rel[i]) continue;
+            if (has_prev) {
+                done = bats::solve_crossings<true>(a2, b2, last, t[i], 0.0f, e[i], k, n2, K, ao2, xo2, to2, zo2);
+                if (done) break;
+            }
+            a2 += w[i] * es[i];
+            b2 += w[i] * e[i];
+            last = t[i];
+            has_prev = true;
+        }
+        if (has_prev && !done) bats::solve_crossings<true>(a2, b2, last, INFINITY, 0.0f, INFINITY, k, n2, K, ao2, xo2, to2, zo2);
+        bool ok = n1 == n2;
+        for (int i = 0; ok && i < n1; ++i)
+            ok = same(ao1[i], ao2[i]) && same(xo1[i], xo2[i]) && same(to1[i], to2[i]) && same(zo1[i], zo2[i]);
+        spikes += n1;
+        if (!ok) { if (bad < 5) std::printf("mismatch q=%lld n %d/%d\n", q, n1, n2); ++bad; }
+    }
+    std::printf("%lld mismatches of %lld; spikes %lld\n", bad, N, spikes);
+    return bad != 0;
+}
+'''
+
+
+def test_conv_merged_windows_match_the_reference_loop(tmp_path):
+    """With finite exponentials, solving the merged windows between a neuron's relevant events gives the same
+    spikes, bit for bit, as the reference's per-event windows over every event of the sample (ties included)."""
+    inc = _cuda_include()
+    if shutil.which("g++") is None or inc is None:
+        pytest.skip("no host C++ compiler or CUDA headers")
+    src, exe = tmp_path / "merged.cpp", tmp_path / "merged"
+    src.write_text(MERGED.replace("#include <random>", "#include <random>\n#include <algorithm>"))
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "bats_gb300", "csrc"),
+                    "-I", inc, "-o", str(exe), str(src)], check=True)
+    r = subprocess.run([str(exe), "400000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    words = r.stdout.split()
+    assert words[0] == "0" and int(words[5]) > 200_000, r.stdout
