@@ -946,6 +946,8 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
                  BATS_ERR_NULL, "weights_gradient: null pointer");
     const int n_buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
     const int groups = group == 1 ? batch : (batch + group - 1) / group;
+    BATS_REQUIRE(groups <= 65535, BATS_ERR_BAD_SHAPE,
+                 "weights_gradient: more than 65535 sample groups (the grid's z limit); raise group");
     float* part = grad;
     int* flags = nullptr;  // all-zero partial tiles are skipped (bucketed kernel, partials in the workspace)
     if (group > 1 && groups > 1) {
@@ -986,6 +988,8 @@ extern "C" int bats_weights_gradient_adam(const void* events, const int* ev_coun
                  BATS_ERR_NULL, "weights_gradient_adam: null pointer");
     const int n_buckets = (n_pre + GRAD_JC - 1) / GRAD_JC;
     const int groups = (batch + group - 1) / group;
+    BATS_REQUIRE(groups <= 65535, BATS_ERR_BAD_SHAPE,
+                 "weights_gradient_adam: more than 65535 sample groups (the grid's z limit); raise group");
     float* part = grad;
     int* flags = nullptr;
     if (groups > 1) {
@@ -1123,7 +1127,10 @@ static __device__ __align__(256) float g_noalloc_grad_scratch[NOALLOC_GRAD_SCRAT
 #include <mutex>
 
 // Device address of the scratch array, looked up once per device (host code only sees a stand-in
-// for the symbol, so the address must come from cudaGetSymbolAddress with that device current).
+// for the symbol, so the address must come from cudaGetSymbolAddress with that device current). The
+// cached address belongs to the device's current primary context: after cudaDeviceReset (or any other
+// teardown of that context) the library's module is loaded again and the old address is stale, so a
+// process that resets a device must not call the allocation-free entry point on it afterwards.
 static int noalloc_scratch_ptr(float** out) {
     static std::mutex mu;
     static float* cache[128] = {nullptr};
@@ -1154,6 +1161,8 @@ extern "C" int bats_weights_gradient_mean_noalloc(const void* events, const int*
     BATS_REQUIRE(events && ev_count && post_times && tables && nvalid && grad, BATS_ERR_NULL,
                  "weights_gradient_mean_noalloc: null pointer");
     const int groups = (batch + group - 1) / group;
+    BATS_REQUIRE(groups <= 65535, BATS_ERR_BAD_SHAPE,
+                 "weights_gradient_mean_noalloc: more than 65535 sample groups (the grid's z limit); raise group");
     const long long per = (long long)n_post * n_pre;
     float* part = grad;
     if (groups > 1) {

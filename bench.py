@@ -4,15 +4,16 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line. `value` is the device-resident batched train step (bats_gb300.train.FCTrainStep,
-replayed as a CUDA graph when capture works) at the literal configuration (weights N(0, 1/sqrt(fan_in)),
-thresholds 1.0 hidden / 1.3 output); `active` repeats it in the reference's MNIST training regime
-(weights U(-1, 1), hidden threshold 0.2) where every layer spikes. `e2e` is the same step through the
-public API with host inputs (pinned host -> device copy and the loss read back inside the timed
+replayed as a CUDA graph when capture works) in the reference's MNIST training regime (weights U(-1, 1),
+hidden threshold 0.2, output 1.3), where every layer spikes (`spikes_per_layer` beside it); `literal`
+repeats every measurement with the configuration's literal constants (weights N(0, 1/sqrt(fan_in)),
+thresholds 1.0 hidden / 1.3 output), where the hidden layers stay silent. `e2e` is the same step through
+the public API with host inputs (pinned host -> device copy and the loss read back inside the timed
 region). `plain_api` is the layer-by-layer drop-in API (Network / LIFLayer / AdamOptimizer with
 per-sample gradients and the caller's batch mean); `refkern` runs the reference's own CUDA kernels on
 the same GPU; `cpu_baseline` is the float64 oracle on the host cores. `--impl reference` times the
-reference path on the host cores (the reference has no CPU implementation of its own, so this is the
-oracle port of it).
+reference path on the host cores on the same workload and configuration (the reference has no CPU
+implementation of its own, so this is the oracle port of it).
 """
 from __future__ import annotations
 
@@ -63,6 +64,19 @@ def thresholds(variant):
     return [hidden] * (len(SIZES) - 2) + [1.3]
 
 
+HEADLINE = "active"
+VARIANT_DESC = {"active": "active: W~U(-1,1), theta 0.2 hidden / 1.3 out (the reference's MNIST training regime)",
+                "literal": "literal: W~N(0,1/sqrt(fan_in)), theta 1.0 hidden / 1.3 out"}
+
+
+def headline_config(world):
+    """The workload both arms of the comparison measure (the same dict in both JSON lines)."""
+    return {"workload": "784-800-800-10 BATS train step (forward, spike-count loss, exact backward, Adam), "
+                        "synthetic MNIST-shaped input (784 inputs, p 0.19 at U(0, 0.01) s), max_n_spike 30",
+            "global_batch": B * world, "variant": VARIANT_DESC[HEADLINE], "parallelism": f"replicas x{world}",
+            "l2": "GPU arm: flushed between timed steps (512 MB write)"}
+
+
 # ---------------------------------------------------------------------------------------------------------------------
 # CPU baseline (float64 oracle), run in spawned worker processes
 
@@ -80,7 +94,7 @@ def _oracle_train_samples(args):
         outs.append(o)
         layer_in.append(o[3])
     n_out = outs[-1][0]
-    targets = R.class_targets(labels, SIZES[-1], TARGET_TRUE, TARGET_FALSE)
+    targets = R.class_targets(labels, weights[-1].shape[0], TARGET_TRUE, TARGET_FALSE)
     _, err = R.spike_count_loss(n_out, targets, K_SPIKE)
     grads = []
     for li in range(len(weights) - 1, -1, -1):
@@ -115,6 +129,33 @@ def cpu_baseline(variant, budget_s=12.0, cores=None):
     return {"value": done / el, "unit": "samples/s", "cores": cores, "kind": "port",
             "sample": f"{done} samples of the {variant} 784-800-800-10 train step (forward, loss, exact backward; "
                       f"float64 NumPy oracle, one process per core), {el:.1f} s"}
+
+
+def batching_cpu_baseline(budget_s=12.0, cores=None, stride=32):
+    """The float64 oracle on the uneven-batch workload (batching_inputs, 1024-1024-20): one sample per
+    `stride` of the 4096 taken at evenly spaced ranks of the event count (the same spread of lengths), one
+    sample per task, as many processes as host cores, in whole passes over that set until the budget is
+    spent; samples/s."""
+    cores = cores or os.cpu_count() or 1
+    t, labels, counts = batching_inputs()
+    ws, ths = batching_weights()
+    idx = np.sort(np.argsort(counts, kind="stable")[stride // 2::stride])
+    chunks = [(t[i:i + 1], labels[i:i + 1], ws, ths) for i in idx]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_train_samples, chunks[:cores])
+        t0 = time.perf_counter()
+        done = 0
+        while True:
+            done += sum(pool.map(_oracle_train_samples, chunks))
+            el = time.perf_counter() - t0
+            if el >= budget_s or done >= 8 * len(chunks):
+                break
+    return {"value": done / el, "unit": "samples/s", "cores": cores, "kind": "port",
+            "sample": f"{done} samples ({len(chunks)} of the 4096-sample uneven batch at evenly spaced event-count "
+                      f"ranks, mean {float(counts[idx].mean()):.0f} input events vs {float(counts.mean()):.0f} "
+                      f"for all 4096) of the 1024-1024-20 train step (forward, loss, exact backward; float64 NumPy "
+                      f"oracle, one process per core), {el:.1f} s"}
 
 
 # ---------------------------------------------------------------------------------------------------------------------
@@ -233,7 +274,10 @@ def spike_counts(ts):
 
 
 def algorithmic_bytes(ts, name):
-    """SpMM-convention bytes of one launch (one FP32 weight read per event x post-neuron synapse)."""
+    """SpMM-convention bytes of one launch (one FP32 weight read per event x post-neuron synapse). The forward
+    writes the spike counts (4 bytes per neuron), a, x, t and post_exp_tau of every spike it emits (16 bytes
+    per spike) and, only when the layer's trains are padded, +inf into t and post_exp_tau of every slot past
+    the count (8 bytes per empty slot); it reads 8 bytes (time and index) per input event."""
     li = int(name[1]) - 1
     kind = name.split(".")[1]
     ev = ts.ev[li]
@@ -241,7 +285,10 @@ def algorithmic_bytes(ts, name):
     spec = ts.specs[li]
     N = spec.n_neurons
     if kind == "forward":
-        return 8 * S + 4 * S * N + ts.B * N * (4 + 16 * spec.max_n_spike)
+        n_spk = int(ts.out[li][0].sum().item())
+        pad = ts._pad_flag(li) == 0
+        pad_bytes = 8 * (ts.B * N * spec.max_n_spike - n_spk) if pad else 0
+        return 8 * S + 4 * S * N + 4 * ts.B * N + 16 * n_spk + pad_bytes
     if kind in ("grad", "grad_adam", "pre_err"):
         n_spk = int(ts.out[li][0].sum().item())
         # + the batch-mean gradient write (grad), or the Adam update that consumes it in place: read W, m, v,
@@ -263,7 +310,7 @@ def run_ours(args, dist, rank, world):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
     result = {}
-    variants = ("literal", "active") if args.workload == "all" else (
+    variants = (HEADLINE, "literal") if args.workload == "all" else (
         (args.workload,) if args.workload in ("literal", "active") else ())
     for variant in variants:
         ts = build_train_step(variant)
@@ -292,28 +339,37 @@ def run_ours(args, dist, rank, world):
         e2e_s = time.perf_counter() - t0
         e2e = {"value": world * B * args.steps / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": ts.h2d_bytes,
                "d2h_bytes_per_step": ts.d2h_bytes, "api": "FCTrainStep.train_host"}
-        traffic, traffic_src = None, None
+        traffic, traffic_src, tinfo = None, None, {}
         tpath = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(tpath):
             tinfo = json.load(open(tpath)).get(variant, {})
             if tinfo.get("kernel") == top:
                 traffic, traffic_src = tinfo.get("bytes"), tinfo.get("source")
+            else:
+                tinfo = {}
+        roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
+                "traffic_source": traffic_src,
+                "algorithmic_bytes_per_launch": abytes, "launch_ms": top_ms,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6800 GB/s"}
+        if traffic:
+            # What the DRAM actually moved per launch (ncu capture) over the live launch time: the weights stay
+            # in L2, so this is far below the SpMM-convention fraction.
+            roof["dram_frac"] = traffic / (top_ms / 1e3) / 1e9 / hbm_peak
+        if tinfo.get("warp_instructions") and tinfo.get("warp_events"):
+            roof["warp_instructions_per_warp_event"] = tinfo["warp_instructions"] / tinfo["warp_events"]
         result[variant] = {
             "value": sps, "ms_per_step": ms / args.steps, "graph": graphed, "autotuned": tuned, "clocks": clocks,
             "e2e": e2e,
-            "spikes_per_layer_last_step": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
-            "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic,
-                         "traffic_source": traffic_src,
-                         "algorithmic_bytes_per_launch": abytes, "launch_ms": top_ms,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
+            "spikes_per_layer": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
+            "roofline": roof,
             "gpu_launches": ts.launches_per_step * args.steps,
         }
         del ts
         torch.cuda.empty_cache()
     # Plain (layer-by-layer) drop-in API and the reference kernels, both configurations (few steps).
     if args.workload == "all":
-        for variant in ("literal", "active"):
+        for variant in (HEADLINE, "literal"):
             result[variant]["plain_api"] = plain_api_rate(variant, max(2, args.steps // 4), flush)
             result[variant]["autograd"] = autograd_rate(variant, max(2, args.steps // 4), flush)
             result[variant]["refkern"] = refkern_rate(variant, 2, flush)
@@ -328,10 +384,9 @@ def profile_one_step(workload):
     if workload == "batching":
         from bats_gb300.train import FCLayerSpec, FCTrainStep
         t, labels, _ = batching_inputs()
-        rng = np.random.default_rng(12)
-        sizes = [1024, 1024, 20]
-        ws = [torch.tensor(rng.uniform(-1, 1, (o, i)).astype(np.float32)) for i, o in zip(sizes[:-1], sizes[1:])]
-        specs = [FCLayerSpec(1024, TAU_S, 0.2, 0.2, K_SPIKE), FCLayerSpec(20, TAU_S, 1.3, 1.3, K_SPIKE)]
+        ws_np, ths = batching_weights()
+        ws = [torch.tensor(w) for w in ws_np]
+        specs = [FCLayerSpec(1024, TAU_S, ths[0], ths[0], K_SPIKE), FCLayerSpec(20, TAU_S, ths[1], ths[1], K_SPIKE)]
         ts = FCTrainStep(t.shape[0], 1024, t.shape[2], specs, ws, TARGET_TRUE, TARGET_FALSE, learning_rate=LR,
                          max_simulation=MAX_SIM)
         ts.set_inputs(torch.tensor(t), torch.tensor(labels))
@@ -594,6 +649,54 @@ def batching_inputs(batch=4096, n_in=1024, seed=11, median=200, lo=20, hi=4000, 
     return t, labels, counts
 
 
+def batching_weights():
+    """Weights U(-1, 1) of the 1024-1024-20 network (seeded) and its thresholds 0.2 hidden / 1.3 output."""
+    rng = np.random.default_rng(12)
+    sizes = [1024, 1024, 20]
+    ws = [rng.uniform(-1, 1, (o, i)).astype(np.float32) for i, o in zip(sizes[:-1], sizes[1:])]
+    return ws, [0.2, 1.3]
+
+
+def batching_plain_rate(t, labels, flush, steps=2):
+    """The uneven batch through the drop-in layer API (Network / LIFLayer / SpikeCountClassLoss /
+    AdamOptimizer, per-sample gradients and the caller's batch mean), one launch chain per layer and no
+    graph: the plain per-layer path the batched step is compared with."""
+    import torch
+    from bats_gb300 import Network, SpikeCountClassLoss
+    from bats_gb300.Layers import InputLayer, LIFLayer
+    from bats_gb300.Optimizers import AdamOptimizer
+    ws, ths = batching_weights()
+    net = Network()
+    prev = InputLayer(n_neurons=1024, name="in")
+    net.add_layer(prev, input=True)
+    for i, (w, th) in enumerate(zip(ws, ths)):
+        layer = LIFLayer(prev, n_neurons=w.shape[0], tau_s=TAU_S, theta=th, delta_theta=th,
+                         weight_initializer=lambda a, b, w=w: torch.tensor(w, device="cuda"), max_n_spike=K_SPIKE,
+                         name=f"l{i}")
+        net.add_layer(layer)
+        prev = layer
+    loss_fn = SpikeCountClassLoss(TARGET_TRUE, TARGET_FALSE)
+    opt = AdamOptimizer(learning_rate=LR)
+    td = torch.tensor(t, device="cuda")
+    nd = torch.isfinite(td).sum(2).to(torch.int32)
+    labels_d = torch.tensor(labels, device="cuda")
+
+    def step():
+        net.reset()
+        net.forward(td, nd, max_simulation=MAX_SIM, training=True)
+        sp, nsp = net.output_spike_trains
+        loss, err = loss_fn.compute_loss_and_errors(sp, nsp, labels_d)
+        g = net.backward(err)
+        net.apply_deltas(opt.step([None if x is None else x.mean(0) for x in g]))
+
+    ms, _ = time_steps(step, steps, 1, flush)
+    del net
+    torch.cuda.empty_cache()
+    return {"value": t.shape[0] * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps,
+            "steps": steps, "what": "Network/LIFLayer/SpikeCountClassLoss/AdamOptimizer drop-in API, per-sample "
+                                    "gradients (4096 x 1024 x 1024 for the first layer), no graph"}
+
+
 def batching_bench(steps: int = 5, warmup: int = 3):
     """Uneven batches: 4096 samples over 1024 input channels with lognormal spike counts (median 200,
     20-4000), times U(0, 0.1) s, network 1024-1024-20, max_n_spike 30, in the reference's MNIST regime
@@ -602,10 +705,9 @@ def batching_bench(steps: int = 5, warmup: int = 3):
     import torch
     from bats_gb300.train import FCLayerSpec, FCTrainStep
     t, labels, counts = batching_inputs()
-    rng = np.random.default_rng(12)
-    sizes = [1024, 1024, 20]
-    ws = [torch.tensor(rng.uniform(-1, 1, (o, i)).astype(np.float32)) for i, o in zip(sizes[:-1], sizes[1:])]
-    specs = [FCLayerSpec(1024, TAU_S, 0.2, 0.2, K_SPIKE), FCLayerSpec(20, TAU_S, 1.3, 1.3, K_SPIKE)]
+    ws_np, ths = batching_weights()
+    ws = [torch.tensor(w) for w in ws_np]
+    specs = [FCLayerSpec(1024, TAU_S, ths[0], ths[0], K_SPIKE), FCLayerSpec(20, TAU_S, ths[1], ths[1], K_SPIKE)]
     ts = FCTrainStep(t.shape[0], 1024, t.shape[2], specs, ws, TARGET_TRUE, TARGET_FALSE, learning_rate=LR,
                      max_simulation=MAX_SIM)
     ts.set_inputs(torch.tensor(t), torch.tensor(labels))
@@ -618,10 +720,12 @@ def batching_bench(steps: int = 5, warmup: int = 3):
     out = {"value": t.shape[0] * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps,
            "steps": steps, "batch": int(t.shape[0]), "k_in": int(t.shape[2]), "graph": graphed, "autotuned": tuned,
            "input_events": {"mean": float(counts.mean()), "max": int(counts.max()), "min": int(counts.min())},
-           "spikes_per_layer_last_step": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
+           "spikes_per_layer": spike_counts(ts), "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
            "network": "1024-1024-20, K 30, U(-1,1) weights, theta 0.2 hidden / 1.3 output"}
     del ts
     torch.cuda.empty_cache()
+    out["plain_api"] = batching_plain_rate(t, labels, flush)
+    out["batched_vs_plain"] = out["value"] / out["plain_api"]["value"]
     return out
 
 
@@ -776,7 +880,8 @@ def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float =
     peak = n_sat / sat_s
     rate = load * peak
     n_p = int(min(40_000, max(1000, rate * poisson_seconds)))
-    res = run_poisson(server, batch_of(n_p, 100_000), rate, seed=1)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        res = run_poisson(server, batch_of(n_p, 100_000), rate, seed=1)
     st = latency_stats(res)
     events = np.array([len(r.indices) for r in pool])
     return {"network": "700-512-512-20, max_n_spike 30, W~(N(1.5,1))/sqrt(fan_in), theta 1.0/1.3",
@@ -786,7 +891,7 @@ def serving_bench(n_sat: int = 3000, poisson_seconds: float = 2.0, load: float =
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
             "lanes": len(server.lanes), "max_batch": server.max_batch, "rejected": len(server.rejected),
             "forward_variant_per_batch_bucket": tuned,
-            "batches": server.batches_launched}
+            "batches": server.batches_launched, "clocks": clk.summary()}
 
 
 def main():
@@ -812,11 +917,13 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline("active", budget_s=max(5.0, min(60.0, args.cpu_budget * args.steps / 10)))
+        # The reference's path on the host cores, on the headline's workload and configuration (same config
+        # dict as our arm's line); a step is a bounded sample of it.
+        cb = cpu_baseline(HEADLINE, budget_s=max(5.0, min(60.0, args.cpu_budget * args.steps / 10)))
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "samples/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "784-800-800-10 BATS train step, batch 256, active regime (host cores)"},
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * B / cb["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": headline_config(args.gpus),
                 "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "samples/s", "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -829,8 +936,10 @@ def main():
         profile_kernels()
         return
 
-    # CPU baseline first (spawned workers, before any GPU context exists in this process).
-    cb = cpu_baseline("active", budget_s=args.cpu_budget) if rank == 0 and not args.no_cpu else None
+    # CPU baselines first (spawned workers, before any GPU context exists in this process).
+    cb = cpu_baseline(HEADLINE, budget_s=args.cpu_budget) if rank == 0 and not args.no_cpu else None
+    cb_batching = (batching_cpu_baseline(budget_s=args.cpu_budget)
+                   if rank == 0 and not args.no_cpu and args.workload in ("all", "batching") else None)
 
     dist = None
     if world > 1:
@@ -841,6 +950,8 @@ def main():
     serving = serving_bench() if args.workload in ("all", "serving") else None
     conv = conv_bench() if args.workload in ("all", "conv") else None
     batching = batching_bench() if args.workload in ("all", "batching") else None
+    if batching is not None:
+        batching["cpu_baseline"] = cb_batching
     if rank != 0:
         return
     if args.workload != "all":
@@ -849,20 +960,19 @@ def main():
                           "unit": "samples/s", "steps": args.steps, "warmup": args.warmup, "detail": head,
                           "serving": serving, "conv": conv, "batching": batching}))
         return
-    lit, act = res["literal"], res["active"]
+    head, lit = res[HEADLINE], res["literal"]
     line = {
-        "metric": METRIC, "value": lit["value"], "unit": "samples/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": lit["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "784-800-800-10 BATS train step (forward, spike-count loss, exact backward, Adam)",
-                   "global_batch": B * world, "variant": "literal: W~N(0,1/sqrt(fan_in)), theta 1.0 hidden/1.3 out",
-                   "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (512 MB write)",
-                   "cuda_graph": lit["graph"]},
-        "roofline": lit["roofline"], "e2e": lit["e2e"], "gpu_launches": lit["gpu_launches"], "clocks": lit["clocks"],
-        "autotuned": lit["autotuned"], "plain_api": lit.get("plain_api"), "autograd": lit.get("autograd"),
-        "refkern": lit.get("refkern"),
-        "cpu_baseline": cb, "spikes_per_layer": lit["spikes_per_layer_last_step"], "kernels_ms": lit["kernels_ms"],
-        "active": act, "serving": serving, "conv": conv, "batching": batching,
+        "metric": METRIC, "value": head["value"], "spikes_per_layer": head["spikes_per_layer"], "unit": "samples/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": headline_config(world), "cuda_graph": head["graph"],
+        "roofline": head["roofline"], "e2e": head["e2e"], "gpu_launches": head["gpu_launches"],
+        "clocks": head["clocks"], "cpu_baseline": cb,
+        "plain_api": head.get("plain_api"), "batched_vs_plain": (head["value"] / head["plain_api"]["value"]
+                                                                 if head.get("plain_api") else None),
+        "autograd": head.get("autograd"), "refkern": head.get("refkern"),
+        "autotuned": head["autotuned"], "kernels_ms": head["kernels_ms"],
+        "serving": serving, "conv": conv, "batching": batching, "literal": lit,
     }
     print(json.dumps(line))
 

@@ -245,8 +245,10 @@ int bats_weights_gradient_adam(const void* events, const int* ev_count, const vo
  * library (bats_weights_gradient_noalloc_capacity() floats, held on every GPU that loads the library until
  * exit): ceil(batch/group) * n_post * n_pre must not exceed it (BATS_ERR_CAPACITY otherwise). The first call
  * on a device looks the array's address up (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the array, so calls whose kernels overlap on the GPU race and must be serialised
- * by the caller. */
+ * capture. The address is cached per device for the life of the process: after cudaDeviceReset on a device
+ * (which tears down the context that holds the array) this entry point must not be called on that device
+ * again. All calls share the array, so calls whose kernels overlap on the GPU race and must be serialised
+ * by the caller. More than 65535 sample groups (ceil(batch/group)) give BATS_ERR_BAD_SHAPE. */
 long long bats_weights_gradient_noalloc_capacity(void);
 int bats_weights_gradient_mean_noalloc(const void* events, const int* ev_count, long long ev_cap,
                                        const float* post_times, const void* tables, const int* nvalid, int batch,

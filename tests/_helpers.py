@@ -65,3 +65,47 @@ def rel_err(a, b, floor=0.0):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+def assert_sum_close(got, ref, abs_scale, rtol=1e-5, what=""):
+    """|got - ref| <= rtol |ref| + rtol * abs_scale elementwise, where abs_scale is the sum of the magnitudes
+    of the terms that make up ref (a sum of signed terms may cancel far below its terms). Returns
+    (entries, entries that need the abs_scale term, worst error / tolerance)."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = np.asarray(abs_scale, dtype=np.float64)
+    tol = rtol * np.abs(ref) + rtol * scale + 1e-30
+    err = np.abs(got - ref)
+    worst = float(np.max(err / tol)) if err.size else 0.0
+    assert worst <= 1.0, f"{what}: worst error / tolerance = {worst:.3f}"
+    return int(err.size), int((err > rtol * np.abs(ref)).sum()), worst
+
+
+def ref_layer_backward(layer, errors, want_pre=True):
+    """The reference's LIFLayer.backward (bats/Layers/LIFLayer.py:93-110) on its compiled kernels, for a
+    refkern.RefLIF layer after its forward, with `errors` (B, N, K) (changed in place by the reset-error
+    step, as the reference does). Returns the batch-summed weight gradient and its term-magnitude sum
+    (the same kernel on |errors|, |f1|, -|f2|), and the pre-spike errors and their term-magnitude sum
+    (|W|, |errors|, |f1|, |f2|, -tau). The gradients are float64 numpy arrays, the pre errors CUDA tensors
+    (B, N_pre, K_pre), so that they can feed the layer below (None without want_pre)."""
+    import torch
+
+    from oracle import refkern
+    n, a, x, t, z = layer.out
+    refkern.propagate_recurrent_errors(x, z, errors, layer.dtt)
+    f1, f2 = refkern.compute_factors(t, a, layer.c, x, z, layer.tau)
+    g = refkern.compute_weights_gradient(f1, f2, t, layer.pre_t, layer.es, layer.ee, errors)
+    g_sum = g.double().sum(0).cpu().numpy()
+    del g
+    ga = refkern.compute_weights_gradient(f1.abs(), -f2.abs(), t, layer.pre_t, layer.es, layer.ee, errors.abs())
+    g_abs = ga.double().sum(0).cpu().numpy()
+    del ga
+    pre = pre_abs = None
+    if want_pre:
+        pre = refkern.propagate_errors_to_pre_spikes(f1, f2, t, layer.pre_t, layer.es, layer.ee, layer.w, errors,
+                                                     layer.tau_s, layer.tau)
+        torch.cuda.synchronize()
+        pre_abs = refkern.propagate_errors_to_pre_spikes(f1.abs(), f2.abs(), t, layer.pre_t, layer.es, layer.ee,
+                                                         layer.w.abs(), errors.abs(), layer.tau_s,
+                                                         -np.float32(layer.tau))
+    return g_sum, g_abs, pre, pre_abs

@@ -17,10 +17,16 @@
   Tolerance: |g_autograd - g_fd| <= 1e-2 |g_fd| + 1e-3 max|g_fd| + 30 s, s the entry's movement under
   that threshold change (oracle/fd.py gradient_sensitivity); the 1e-2 relative term covers the central
   difference's own truncation error at eps 1e-4.
-* The same gradients as the reference's CUDA kernels (oracle/refkern.py) on the same inputs, batch 64,
-  in the reference's MNIST regime (hidden threshold 0.2, weights U(-1, 1)): every entry within 1e-4 of
-  the layer's largest gradient (the per-sample sums run in a different order than the reference's
-  loops; the forward is bit-identical).
+* The same gradients as the reference's CUDA kernels (oracle/refkern.py), batch 256, in the reference's
+  MNIST regime (hidden threshold 0.2, weights U(-1, 1)), layer by layer: each lif_fc layer gets the
+  reference's own input spikes and incoming errors (the loss errors for the output layer, the reference's
+  pre-spike errors of the layer above otherwise), and torch.autograd.grad's weight gradient and input-time
+  gradient must match the reference's batch-summed gradient and pre-spike errors within
+  1e-5 |ref| + 1e-5 sum|terms| (sum|terms|: the reference kernels on |errors|, |f1|, -|f2|, |W|, -tau).
+* The whole network differentiated in one torch.autograd.grad call, batch 256: the forward is bit-identical
+  to the reference's, and every layer's gradient within 1e-4 of the layer's largest entry of the
+  reference's chained backward (the incoming errors of the lower layers differ from the reference's by the
+  upper layers' rounding, which the chained sums carry along).
 """
 import numpy as np
 import pytest
@@ -29,7 +35,7 @@ import torch
 from bats_gb300.autograd import lif_fc
 from oracle import fd as FD
 from oracle import refkern
-from tests._helpers import mnist_like_input
+from tests._helpers import assert_sum_close, mnist_like_input, ref_layer_backward
 
 pytestmark = pytest.mark.gpu
 
@@ -106,10 +112,43 @@ def test_finite_differences_on_64_weights_per_layer(cuda):
         assert not bad.any(), (li, np.c_[ad[m][bad], fd[m][bad]][:5])
 
 
-def test_autograd_gradients_match_reference_kernels(cuda):
+def test_autograd_layers_match_reference_kernels_batch_256(cuda):
     if not refkern.available():
         pytest.skip("reference kernels not built")
-    t, n, ws_np = make_case(batch=64, seed=5)
+    t, n, ws_np = make_case(batch=256, seed=5)
+    layers = [refkern.RefLIF(torch.tensor(w, device="cuda"), TAU_S, th, th, K) for w, th in zip(ws_np, THETAS)]
+    x, c = torch.tensor(t, device="cuda"), torch.tensor(n, device="cuda")
+    inputs = []
+    for L in layers:
+        inputs.append(x)
+        o = L.forward(x, c, np.float32(MAX_SIM))
+        x, c = o[3], o[0]
+    r = torch.tensor(smooth_loss_weights(x.shape, seed=7), device="cuda")
+    e_in = torch.where(torch.isfinite(x), r, torch.zeros_like(r)).contiguous()
+    report = []
+    for li in (2, 1, 0):
+        x_in = inputs[li].clone().requires_grad_(li > 0)
+        w = torch.tensor(ws_np[li], device="cuda", requires_grad=True)
+        out, cnt = lif_fc(x_in, w, TAU_S, THETAS[li], THETAS[li], K, MAX_SIM)
+        assert torch.equal(cnt, layers[li].out[0]), f"layer {li + 1}: spike counts differ from the reference"
+        wanted = [w, x_in] if li > 0 else [w]
+        grads = torch.autograd.grad(out, wanted, grad_outputs=e_in)
+        g_ref, g_abs, pe_ref, pe_abs = ref_layer_backward(layers[li], e_in.clone(), want_pre=li > 0)
+        st = assert_sum_close(grads[0].double().cpu().numpy(), g_ref, g_abs, what=f"layer {li + 1} weight gradient")
+        report.append(f"L{li + 1} W: {st[1]}/{st[0]} need sum|terms|, worst {st[2]:.3f}")
+        if li > 0:
+            st = assert_sum_close(grads[1].double().cpu().numpy(), pe_ref.double().cpu().numpy(),
+                                  pe_abs.double().cpu().numpy(), what=f"layer {li + 1} input-time gradient")
+            report.append(f"L{li + 1} input times: {st[1]}/{st[0]} need sum|terms|, worst {st[2]:.3f}")
+            e_in = pe_ref.contiguous()
+        torch.cuda.empty_cache()
+    print("\n[autograd vs reference kernels, batch 256] " + "; ".join(report))
+
+
+def test_autograd_network_matches_reference_chain_batch_256(cuda):
+    if not refkern.available():
+        pytest.skip("reference kernels not built")
+    t, n, ws_np = make_case(batch=256, seed=5)
     t_in = torch.tensor(t, device="cuda")
     ws = [torch.tensor(w, device="cuda", requires_grad=True) for w in ws_np]
     out, counts = forward(t_in, ws)

@@ -72,3 +72,19 @@ def test_noalloc_gradient_refuses_oversized_scratch(cuda):
         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert status == 3  # BATS_ERR_CAPACITY
     assert b"static scratch" in _lib.load().bats_last_error()
+
+
+def test_noalloc_gradient_refuses_too_many_groups(cuda):
+    """More sample groups than a grid's z dimension holds (65535) are refused on the host, before any launch,
+    with a message that says to raise the group size."""
+    ev, ts, tabs = _case(8, 32, 16, seed=14)
+    out = torch.zeros((16, 32), device="cuda")
+    B, n_post, k_post = ts.shape
+    # Claim 140000 samples in groups of 2 (70000 groups) of a 1 x 1 layer: the scratch would hold them, the
+    # grid would not.
+    status = _lib.load().bats_weights_gradient_mean_noalloc(
+        ev.events.data_ptr(), ev.counts.data_ptr(), ev.cap, ts.data_ptr(), tabs.tables.data_ptr(),
+        tabs.nvalid.data_ptr(), 140000, 1, k_post, 1, 2, out.data_ptr(),
+        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert status == 1  # BATS_ERR_BAD_SHAPE
+    assert b"raise group" in _lib.load().bats_last_error()
