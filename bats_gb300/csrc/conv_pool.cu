@@ -10,7 +10,11 @@
 // and each thread integrates only the events of its own receptive field, searching for crossings
 // in (t_prev_relevant, t_this_relevant] before adding the next one. Because the neuron state does
 // not change at an irrelevant event and the reference's windows between consecutive events tile
-// that interval, this finds the same spikes with the same arithmetic.
+// that interval, this finds the same spikes with the same arithmetic. An event outside the field
+// changes the reference's state only when one of its exponentials is not finite (an input later than
+// about 88 tau_s overflows exp(t/tau_s)): its weight 0 times +inf is NaN, which the reference's solver
+// turns into NaN spikes. Such events are therefore relevant to every neuron, with weight 0 outside the
+// field, exactly as the reference adds them.
 //
 // Backward (replaces compute_weights_gradient_conv and propagate_errors_to_pre_spikes_conv,
 // .../Backpropagation/compute_weights_gradient_conv.cu:11-61, propagate_errors_to_pre_spikes_conv.cu:11-89):
@@ -86,7 +90,8 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
                 const Event e = evs[m0 + q];
                 const int j = e.j;
                 const int cc = j % C, xy = j / C, yy = xy % Y, xx = xy / Y;
-                keep = xx >= rx0 && xx < rx1 && yy >= ry0 && yy < ry1;
+                // In the tile's receptive field, or relevant to every neuron (a non-finite exponential).
+                keep = (xx >= rx0 && xx < rx1 && yy >= ry0 && yy < ry1) || !(isfinite(e.es) && isfinite(e.e));
                 ce.t = e.t;
                 ce.es = e.es;
                 ce.e = e.e;
@@ -110,12 +115,13 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
         for (int m = 0; m < kept && !done; ++m) {
             const ConvEvent e = sev[m];
             const int dx = (e.xyc & 1023) - xo, dy = ((e.xyc >> 10) & 1023) - yo;
-            if (dx < 0 || dx >= fx || dy < 0 || dy >= fy) continue;
+            const bool in_field = dx >= 0 && dx < fx && dy >= 0 && dy < fy;
+            if (!in_field && isfinite(e.es) && isfinite(e.e)) continue;  // weight 0 times a finite value
             if (has_prev) {
                 done = solve_crossings<true>(a, b, last_t, e.t, 0.0f, e.e, sk, n, k_post, ao, xo_, to, zo);
                 if (done) break;
             }
-            const float w = Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)];
+            const float w = in_field ? Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)] : 0.0f;
             a += w * e.es;
             b += w * e.e;
             last_t = e.t;

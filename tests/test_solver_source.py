@@ -163,14 +163,21 @@ def test_solver_matches_the_reference_loop(tmp_path, conv):
     assert spikes > 500_000 and multi > 50_000 and screened > 1_000_000, r.stdout
 
 
-MERGED = PROGRAM.split("// The reference's per-event solver loop")[0] + r'''
+MERGED = PROGRAM.split("\nstatic bool same(")[0] + r'''
 static bool same(float x, float y) { uint32_t a, b; std::memcpy(&a, &x, 4); std::memcpy(&b, &y, 4); return a == b; }
 
-// Conv layer, finite exponentials: the reference visits every event of the sample, with weight 0 outside the
-// neuron's receptive field, and solves each window (t_i, t_{i+1}] (compute_spike_times_conv.cu:155-172); the
-// conv kernel visits only the relevant events and solves the merged window between them, then (t_last, inf).
+// Conv layer: the reference visits every event of the sample, with weight 0 outside the neuron's receptive
+// field, and solves each window (t_i, t_{i+1}] (compute_spike_times_conv.cu:155-172); the conv kernel visits
+// only the relevant events and solves the merged window between them, then (t_last, inf). An event outside
+// the field is relevant when one of its exponentials is not finite (0 * inf is NaN in the reference's sums).
+// argv[2] = 1 plants the old mistake: outside events are never relevant.
+// argv[3] = 1 uses the plain restatement of the reference's solver on the reference side (else the device
+// solver there too, which isolates the window merging).
 int main(int argc, char** argv) {
     const long long N = std::atoll(argv[1]);
+    const bool old_rule = argc > 2 && std::atoi(argv[2]) != 0;
+    const bool plain_ref = argc > 3 && std::atoi(argv[3]) != 0;
+    long long overflow_cases = 0;
     std::mt19937_64 rng(77);
     std::uniform_real_distribution<double> U(0, 1);
     std::normal_distribution<double> G(0, 1);
@@ -182,7 +189,10 @@ int main(int argc, char** argv) {
         const float max_sim = U(rng) < 0.5 ? INFINITY : (float)(U(rng) * 0.4);
         float t[64], es[64], e[64], w[64];
         bool rel[64];
-        for (int i = 0; i < E; ++i) t[i] = (float)(U(rng) * 0.3);
+        // One case in four reaches past 88 tau_s, where expf(t / tau_s) overflows to +inf (and past 177 tau_s,
+        // where expf(t / tau) does too), with max_sim = inf half the time as above.
+        const bool late = q % 4 == 3;
+        for (int i = 0; i < E; ++i) t[i] = late ? (float)(tau_s * (80.0 + U(rng) * 110.0)) : (float)(U(rng) * 0.3);
         std::sort(t, t + E);
         if (q % 5 == 0) for (int i = 1; i < E; i += 3) t[i] = t[i - 1];   // ties
         const double scale = std::exp(G(rng));
@@ -197,6 +207,9 @@ int main(int argc, char** argv) {
         k.e_max = std::isfinite(em) && em < 3.0e38 ? (float)em : INFINITY;
         k.inv_c = 1.0f / c; k.fast = true;
         float ao1[16], xo1[16], to1[16], zo1[16], ao2[16], xo2[16], to2[16], zo2[16];
+        bool any_inf = false;
+        for (int i = 0; i < E; ++i) any_inf |= !std::isfinite(es[i]);
+        overflow_cases += any_inf;
         // the reference's loop over every event
         float a = 0, b = 0;
         int n1 = 0;
@@ -205,21 +218,26 @@ int main(int argc, char** argv) {
             a += wi * es[i];
             b += wi * e[i];
             const float next = i + 1 < E ? t[i + 1] : INFINITY;
-            if (bats::solve_crossings<true>(a, b, t[i], next, 0.0f, i + 1 < E ? e[i + 1] : INFINITY, k, n1, K,
-                                            ao1, xo1, to1, zo1)) break;
+            const bool full = plain_ref
+                ? reference_solve<true>(c, dtt, tau, max_sim, a, b, t[i], next, n1, K, ao1, xo1, to1, zo1)
+                : bats::solve_crossings<true>(a, b, t[i], next, 0.0f, i + 1 < E ? e[i + 1] : INFINITY, k, n1, K,
+                                              ao1, xo1, to1, zo1);
+            if (full) break;
         }
         // the conv kernel's loop over the relevant events only
         float a2 = 0, b2 = 0, last = 0;
         int n2 = 0;
         bool has_prev = false, done = false;
         for (int i = 0; i < E && !done; ++i) {
-            if (!rel[i]) continue;
+            const bool finite = std::isfinite(es[i]) && std::isfinite(e[i]);
+            if (!rel[i] && (finite || old_rule)) continue;
             if (has_prev) {
                 done = bats::solve_crossings<true>(a2, b2, last, t[i], 0.0f, e[i], k, n2, K, ao2, xo2, to2, zo2);
                 if (done) break;
             }
-            a2 += w[i] * es[i];
-            b2 += w[i] * e[i];
+            const float wi = rel[i] ? w[i] : 0.0f;
+            a2 += wi * es[i];
+            b2 += wi * e[i];
             last = t[i];
             has_prev = true;
         }
@@ -230,15 +248,17 @@ int main(int argc, char** argv) {
         spikes += n1;
         if (!ok) { if (bad < 5) std::printf("mismatch q=%lld n %d/%d\n", q, n1, n2); ++bad; }
     }
-    std::printf("%lld mismatches of %lld; spikes %lld\n", bad, N, spikes);
+    std::printf("%lld mismatches of %lld; spikes %lld; overflow %lld\n", bad, N, spikes, overflow_cases);
     return bad != 0;
 }
 '''
 
 
 def test_conv_merged_windows_match_the_reference_loop(tmp_path):
-    """With finite exponentials, solving the merged windows between a neuron's relevant events gives the same
-    spikes, bit for bit, as the reference's per-event windows over every event of the sample (ties included)."""
+    """Solving the merged windows between a neuron's relevant events gives the same spikes, bit for bit, as the
+    reference's per-event windows over every event of the sample (ties included), also when inputs later than
+    88 tau_s overflow exp(t/tau_s): events outside the field with a non-finite exponential count as relevant
+    (weight 0, as the reference adds them). Without that rule the overflowing cases differ."""
     inc = _cuda_include()
     if shutil.which("g++") is None or inc is None:
         pytest.skip("no host C++ compiler or CUDA headers")
@@ -246,7 +266,13 @@ def test_conv_merged_windows_match_the_reference_loop(tmp_path):
     src.write_text(MERGED.replace("#include <random>", "#include <random>\n#include <algorithm>"))
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "bats_gb300", "csrc"),
                     "-I", inc, "-o", str(exe), str(src)], check=True)
-    r = subprocess.run([str(exe), "400000"], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([str(exe), "400000", "0", "1"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     words = r.stdout.split()
-    assert words[0] == "0" and int(words[5]) > 200_000, r.stdout
+    assert words[0] == "0" and int(words[5].rstrip(";")) > 200_000 and int(words[7]) > 50_000, r.stdout
+    # The same check with the device solver on both sides (window merging alone).
+    r = subprocess.run([str(exe), "400000", "0", "0"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.split()[0] == "0", r.stdout + r.stderr
+    # A planted mistake: outside events never relevant, as before overflowing exponentials were handled.
+    r = subprocess.run([str(exe), "400000", "1", "1"], capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0 and int(r.stdout.split("mismatches")[0].split()[-1]) > 1000, r.stdout
