@@ -185,15 +185,31 @@ def compute_weights_gradient(f1, f2, post_times, pre_times, pre_exp_tau_s, pre_e
     return g
 
 
+def sample_chunks(batch, per_sample, limit=2 ** 31 - 1):
+    """(start, stop) sample ranges for the error-propagation kernels, whose element index into their
+    (B, N_pre, K_pre, N_post) temporary, (sample * N_pre * K_pre + ...) * N_post, is formed in 32-bit integers
+    (propagate_errors_to_pre_spikes.cu:23-31 signed, propagate_errors_to_pre_spikes_conv.cu:55-63 unsigned):
+    batches whose temporary has 2^31 elements or more are launched in chunks of samples below that size
+    (samples are independent, so each sample's result is that of one launch). The reference's own wrappers
+    launch the whole batch at once; for such batches that index would wrap."""
+    step = max(1, limit // max(1, per_sample))
+    return [(c0, min(batch, c0 + step)) for c0 in range(0, batch, step)]
+
+
 def propagate_errors_to_pre_spikes(f1, f2, post_times, pre_times, pre_exp_tau_s, pre_exp_tau, weights, errors, tau_s,
                                    tau):
     B, n_post, k_post = f1.shape
     _, n_pre, k_pre = pre_exp_tau_s.shape
-    tmp = torch.zeros((B, n_pre, k_pre, n_post), dtype=torch.float32, device=f1.device)
-    launch("propagate_errors_to_pre_spikes", "propagate_errors_to_pre_spikes_kernel", (n_pre, k_pre, n_post), (B,),
-           (f1, f2, post_times, pre_times, pre_exp_tau_s, pre_exp_tau, weights, errors, tmp, k_post, f32(tau_s),
-            f32(tau)))
-    return tmp.sum(dim=3)
+    out = torch.empty((B, n_pre, k_pre), dtype=torch.float32, device=f1.device)
+    for c0, c1 in sample_chunks(B, n_pre * k_pre * n_post):
+        sl = slice(c0, c1)
+        tmp = torch.zeros((c1 - c0, n_pre, k_pre, n_post), dtype=torch.float32, device=f1.device)
+        launch("propagate_errors_to_pre_spikes", "propagate_errors_to_pre_spikes_kernel", (n_pre, k_pre, n_post),
+               (c1 - c0,), (f1[sl], f2[sl], post_times[sl], pre_times[sl], pre_exp_tau_s[sl], pre_exp_tau[sl],
+                            weights, errors[sl], tmp, k_post, f32(tau_s), f32(tau)))
+        out[sl] = tmp.sum(dim=3)
+        del tmp
+    return out
 
 
 def compute_weights_gradient_conv(f1, f2, post_times, pre_times, pre_exp_tau_s, pre_exp_tau, pre_shape, post_shape,
@@ -217,12 +233,19 @@ def propagate_errors_to_pre_spikes_conv(f1, f2, post_times, pre_times, pre_exp_t
     C_out, fx, fy, C = (int(v) for v in filter_shape)
     nf = C_out * fx * fy
     dev = f1.device
-    tmp = torch.zeros((B, n_pre, k_pre, nf), dtype=torch.float32, device=dev)
     shp = lambda v: torch.tensor(np.asarray(v, dtype=np.int32), device=dev)
-    launch("propagate_errors_to_pre_spikes_conv", "propagate_errors_to_pre_spikes_conv_kernel", (n_pre, k_pre, nf),
-           (B,), (f1, f2, post_times, pre_times, pre_exp_tau_s, pre_exp_tau, weights, errors, shp(post_shape),
-                  shp(pre_shape), shp(filter_shape), tmp, n_post, k_post, f32(tau_s), f32(tau)))
-    return tmp.sum(dim=3)
+    out = torch.empty((B, n_pre, k_pre), dtype=torch.float32, device=dev)
+    for c0, c1 in sample_chunks(B, n_pre * k_pre * nf):
+        sl = slice(c0, c1)
+        tmp = torch.zeros((c1 - c0, n_pre, k_pre, nf), dtype=torch.float32, device=dev)
+        launch("propagate_errors_to_pre_spikes_conv", "propagate_errors_to_pre_spikes_conv_kernel",
+               (n_pre, k_pre, nf), (c1 - c0,),
+               (f1[sl], f2[sl], post_times[sl], pre_times[sl], pre_exp_tau_s[sl], pre_exp_tau[sl], weights,
+                errors[sl], shp(post_shape), shp(pre_shape), shp(filter_shape), tmp, n_post, k_post, f32(tau_s),
+                f32(tau)))
+        out[sl] = tmp.sum(dim=3)
+        del tmp
+    return out
 
 
 # ---- layers (bats/Layers/LIFLayer.py:63-110, ConvLIFLayer.py:77-134, PoolingLayer.py:49-66) --------------------

@@ -88,8 +88,6 @@ def ref_layer_backward(layer, errors, want_pre=True):
     (the same kernel on |errors|, |f1|, -|f2|), and the pre-spike errors and their term-magnitude sum
     (|W|, |errors|, |f1|, |f2|, -tau). The gradients are float64 numpy arrays, the pre errors CUDA tensors
     (B, N_pre, K_pre), so that they can feed the layer below (None without want_pre)."""
-    import torch
-
     from oracle import refkern
     n, a, x, t, z = layer.out
     refkern.propagate_recurrent_errors(x, z, errors, layer.dtt)
@@ -104,8 +102,34 @@ def ref_layer_backward(layer, errors, want_pre=True):
     if want_pre:
         pre = refkern.propagate_errors_to_pre_spikes(f1, f2, t, layer.pre_t, layer.es, layer.ee, layer.w, errors,
                                                      layer.tau_s, layer.tau)
-        torch.cuda.synchronize()
         pre_abs = refkern.propagate_errors_to_pre_spikes(f1.abs(), f2.abs(), t, layer.pre_t, layer.es, layer.ee,
                                                          layer.w.abs(), errors.abs(), layer.tau_s,
                                                          -np.float32(layer.tau))
+    return g_sum, g_abs, pre, pre_abs
+
+
+def ref_conv_layer_backward(layer, errors, want_pre=True):
+    """ConvLIFLayer.backward (bats/Layers/ConvLIFLayer.py:109-134) on the reference's compiled kernels for a
+    refkern.RefConvLIF layer after its forward, as ref_layer_backward: the batch-summed filter gradient
+    (C_out, fx, fy, C_in) and its term-magnitude sum as float64 numpy arrays, the pre-spike errors and their
+    term-magnitude sum as CUDA tensors (None without want_pre)."""
+    from oracle import refkern
+    n, a, x, t, z = layer.out
+    refkern.propagate_recurrent_errors(x, z, errors, layer.dtt)
+    f1, f2 = refkern.compute_factors(t, a, layer.c, x, z, layer.tau)
+    geo = (layer.pre_shape, layer.post_shape, layer.filter_shape)
+    g = refkern.compute_weights_gradient_conv(f1, f2, t, layer.pre_t, layer.es, layer.ee, *geo, errors)
+    g_sum = g.double().sum(0).cpu().numpy()
+    del g
+    ga = refkern.compute_weights_gradient_conv(f1.abs(), -f2.abs(), t, layer.pre_t, layer.es, layer.ee, *geo,
+                                               errors.abs())
+    g_abs = ga.double().sum(0).cpu().numpy()
+    del ga
+    pre = pre_abs = None
+    if want_pre:
+        pre = refkern.propagate_errors_to_pre_spikes_conv(f1, f2, t, layer.pre_t, layer.es, layer.ee, layer.w, errors,
+                                                          layer.tau_s, layer.tau, *geo)
+        pre_abs = refkern.propagate_errors_to_pre_spikes_conv(f1.abs(), f2.abs(), t, layer.pre_t, layer.es, layer.ee,
+                                                              layer.w.abs(), errors.abs(), layer.tau_s,
+                                                              -np.float32(layer.tau), *geo)
     return g_sum, g_abs, pre, pre_abs
