@@ -147,6 +147,7 @@ def test_train_step_equals_kernel_chain_784_800_800_10_batch_256(cuda, variant):
         wts.append(wt)
         x = o[3]
     err = _count_errors(chain[-1][0], labels)
+    pre = {}
     for li in (2, 1, 0):
         n, a, xx, tt, z = chain[li]
         _, c, dtt = K.lif_constants(TAU_S, thetas[li], thetas[li])
@@ -159,7 +160,10 @@ def test_train_step_equals_kernel_chain_784_800_800_10_batch_256(cuda, variant):
             f"layer {li + 1}: train-step gradient differs from the kernel chain"
         if li > 0:
             err = K.pre_errors(evs[li], wts[li], tt, tabs, TAU_S, tau32)
-            pe_ts = ts.pre_err[li]
-            cnt = chain[li - 1][0]
-            valid = torch.arange(KP, device="cuda")[None, None, :] < cnt[:, :, None]
-            assert torch.equal(pe_ts[valid], err[valid]), f"layer {li + 1}: train-step pre errors differ"
+            pre[li] = err
+    # The pre-spike errors of layer l are the next layer down's incoming errors, which its reset-error step
+    # changes in place (in the train step as in the chain): compared after the whole backward.
+    for li, err in pre.items():
+        cnt = chain[li - 1][0]
+        valid = torch.arange(KP, device="cuda")[None, None, :] < cnt[:, :, None]
+        assert torch.equal(ts.pre_err[li][valid], err[valid]), f"layer {li + 1}: train-step pre errors differ"
