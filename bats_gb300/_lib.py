@@ -89,6 +89,9 @@ SIGNATURES = {
                                       c_int, c_int, c_int, c_vp]),
     "bats_add_deltas": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_vp]),
     "bats_transpose": (c_int, [c_vp, c_int, c_int, c_vp, c_int, c_vp]),
+    "bats_fc_train_step_workspace_bytes": (c_size, [c_int, c_vp, c_int]),
+    "bats_fc_train_step": (c_int, [c_vp, c_vp, c_int, c_vp, c_int, c_float, c_float, c_float, c_float, c_float,
+                                   c_float, c_vp, c_vp, c_vp, c_vp, c_size, c_vp]),
 }
 
 
@@ -127,6 +130,13 @@ class BatsFcLayer(ctypes.Structure):
                 ("max_simulation", c_float), ("algo", c_int), ("events", c_vp), ("slots", c_vp),
                 ("ev_count", c_vp), ("n_spikes", c_vp), ("a", c_vp), ("x", c_vp), ("times", c_vp),
                 ("post_exp_tau", c_vp)]
+
+
+class BatsFcTrainLayer(ctypes.Structure):
+    """struct BatsFcTrainLayer of include/bats_gb300.h (one layer of bats_fc_train_step)."""
+    _fields_ = [("fwd", BatsFcLayer), ("weights", c_vp), ("adam_m", c_vp), ("adam_v", c_vp), ("grad", c_vp),
+                ("events_bucketed", c_vp), ("bucket_offsets", c_vp), ("tables", c_vp), ("nvalid", c_vp),
+                ("f1", c_vp), ("f2", c_vp), ("pre_errors", c_vp), ("grad_group", c_int)]
 
 
 def call(name: str, *args):

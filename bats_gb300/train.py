@@ -173,6 +173,43 @@ class FCTrainStep:
                 ptr(self.W[li]), ptr(self.Wt[li]), self.Wt[li].shape[1], ws, wsb, s)))
         return L
 
+    # -- the same step as one foreign call (bats_fc_train_step) -------------------------------------
+    def native_layers(self):
+        """The layers as an array of struct BatsFcTrainLayer for bats_fc_train_step, built from this step's
+        buffers, forward variants and gradient groups as they are now (call again after autotune)."""
+        from ._lib import BatsFcLayer, BatsFcTrainLayer
+        arr = (BatsFcTrainLayer * len(self.specs))()
+        n_prev, k_prev = self.in_times.shape[1], self.in_times.shape[2]
+        for li, spec in enumerate(self.specs):
+            ev, tb = self.ev[li], self.tabs[li]
+            n, a, x, t, z = self.out[li]
+            tau32, c, dtt = K.lif_constants(spec.tau_s, spec.theta, spec.delta_theta)
+            algo = self.fwd_algo[li]
+            fwd = BatsFcLayer(n_prev, k_prev, spec.n_neurons, spec.max_n_spike, ptr(self.Wt[li]), self.Wt[li].shape[1],
+                              float(np.float32(spec.tau_s)), float(tau32), float(c), float(dtt),
+                              float(np.float32(self.max_sim)), int(algo), ptr(ev.events), ptr(ev.slots),
+                              ptr(ev.counts), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z))
+            arr[li] = BatsFcTrainLayer(fwd, ptr(self.W[li]), ptr(self.m[li]), ptr(self.v[li]), ptr(self.grad[li]),
+                                       ptr(ev.bucketed), ptr(ev.bucket_offsets), ptr(tb.tables), ptr(tb.nvalid),
+                                       ptr(tb.f1), ptr(tb.f2), ptr(self.pre_err[li]) if li > 0 else None,
+                                       int(self.groups[li]))
+            n_prev, k_prev = spec.n_neurons, spec.max_n_spike
+        return arr
+
+    def native_step(self) -> None:
+        """One training step as a single call of the C ABI's bats_fc_train_step: the same launches, arguments
+        and results as step()."""
+        import ctypes
+        layers = self.native_layers()
+        need = K.call_size("bats_fc_train_step_workspace_bytes", self.B, ctypes.cast(layers, ctypes.c_void_p),
+                           len(self.specs))
+        assert need <= self.ws.numel(), "workspace smaller than bats_fc_train_step needs"
+        call("bats_fc_train_step", ptr(self.in_times), ptr(self.labels), self.B, ctypes.cast(layers, ctypes.c_void_p),
+             len(self.specs), float(self.tt), float(self.tf), float(self.b1), float(self.b2), float(self.eps),
+             float(self.lr), ptr(self.powers), ptr(self.loss), ptr(self.errors), ptr(self.ws), self.ws.numel(),
+             stream_ptr())
+        self.t += 1
+
     def _grad_only(self, li: int, group: int, s) -> None:
         """The batch-mean weight gradient of layer li into self.grad[li] (no weight update), from the tables of
         the last backward pass: what the autotuner times for the gradient group size."""

@@ -381,6 +381,62 @@ int bats_serve_fc_batch(const int* h_indices, const float* h_times, const int* h
                         void* sort_workspace, size_t sort_workspace_bytes, int* h_out_counts, float* h_out_times,
                         int* h_overflow, cudaStream_t stream);
 
+/* ---- Training step ---------------------------------------------------------------------------- */
+
+/* Forward kernel choices of bats_fc_train_step beyond BATS_FWD_TILE/LANES/TILE64: the persistent work-queue
+ * forward (bats_lif_forward_fc_queue) with 128- or 64-neuron tiles. */
+#define BATS_FWD_QUEUE 4
+#define BATS_FWD_QUEUE64 5
+
+/* One trainable fully-connected layer of bats_fc_train_step: the forward part as for serving (`fwd`: shapes,
+ * transposed weights, which Adam keeps in sync, constants, forward variant, events, slots, counts and outputs
+ * for `batch` samples), and the backward and optimizer state, all device buffers owned by the caller:
+ *   weights (n_post, n_pre), adam_m, adam_v (same shape), grad (same shape: the last step's batch-mean gradient);
+ *   events_bucketed (batch, n_pre*k_pre records) and bucket_offsets (batch, ceil(n_pre/64) + 1): the events
+ *     grouped by 64-neuron pre buckets for the gradient (both NULL: the gradient reads the time-sorted events);
+ *   tables (batch, n_post, k_post + 1, 2 floats), nvalid (batch, n_post): the backward's suffix tables;
+ *   f1, f2 (batch, n_post, k_post): factors, needed only when k_post > 32 (else may be NULL);
+ *   pre_errors (batch, n_pre, k_pre): errors of the layer's input spikes, filled for every layer but the first
+ *     (NULL there); they are the incoming errors of the layer below, whose reset-error step changes them;
+ *   grad_group: samples per partial gradient (>= 2). */
+typedef struct BatsFcTrainLayer {
+    BatsFcLayer fwd;
+    float* weights;
+    float* adam_m;
+    float* adam_v;
+    float* grad;
+    void* events_bucketed;
+    int* bucket_offsets;
+    void* tables;
+    int* nvalid;
+    float* f1;
+    float* f2;
+    float* pre_errors;
+    int grad_group;
+} BatsFcTrainLayer;
+
+/* Workspace of bats_fc_train_step: the largest of the sort, work-queue, gradient and pre-error workspaces of
+ * its layers. */
+size_t bats_fc_train_step_workspace_bytes(int batch, const BatsFcTrainLayer* layers, int n_layers);
+
+/* One training step of a fully-connected network on device-resident inputs, enqueued on `stream` with no host
+ * synchronisation and no allocation, so that it can be called from any language through this ABI (and
+ * captured in a CUDA graph): Adam's bias-correction powers advanced on the device (`powers`: 4 doubles,
+ * {1, 1, 0, 0} before the first step); per layer the event sort (bucketed copy included) and the LIF forward
+ * (hidden layers unpadded); the spike-count class loss (targets target_true / target_false, per-sample loss
+ * (batch) and output-layer errors (batch, n_out, k_out)); then per layer from the last one the reset errors,
+ * factors and suffix tables, the pre-spike errors (every layer but the first, with the weights before this
+ * step's update) and the batch-mean gradient fused with Adam (weights, their transposed copy, m, v, grad).
+ * in_times (batch, layers[0].fwd.n_pre, layers[0].fwd.k_pre), labels (batch) int32.
+ * Replaces the reference's training iteration (experiments/mnist/train_spike_count.py:143-177: Network.forward,
+ * SpikeCountClassLoss.compute_loss_and_errors, Network.backward, the batch mean, AdamOptimizer.step,
+ * Network.apply_deltas; bats/Network.py:32-54). Results are those of the same sequence of the entry points it
+ * calls. */
+int bats_fc_train_step(const float* in_times, const int* labels, int batch, BatsFcTrainLayer* layers, int n_layers,
+                       float target_true, float target_false, float beta_1, float beta_2, float epsilon,
+                       float learning_rate, double* powers, float* loss, float* errors, void* workspace,
+                       size_t workspace_bytes, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

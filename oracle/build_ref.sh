@@ -6,10 +6,11 @@
 # export the same kernel symbol. nvcc's defaults (-fmad=true, IEEE division and square root, no
 # fast-math) match NVRTC's defaults, which the reference uses through cp.RawKernel with no options.
 set -e
-REF="${BATS_REFERENCE:-/root/reference}"
+REF="${BATS_REFERENCE:-}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 NVCC="${NVCC:-nvcc}"
+[ -n "$REF" ] || { echo "set BATS_REFERENCE to a checkout of the reference" >&2; exit 1; }
 [ -d "$REF/bats/CudaKernels/CuFiles" ] || { echo "reference not found at $REF" >&2; exit 1; }
 mkdir -p "$OUT"
 pids=""

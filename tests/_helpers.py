@@ -133,3 +133,21 @@ def ref_conv_layer_backward(layer, errors, want_pre=True):
                                                               layer.w.abs(), errors.abs(), layer.tau_s,
                                                               -np.float32(layer.tau), *geo)
     return g_sum, g_abs, pre, pre_abs
+
+
+def uneven_input(batch, n_in=1024, seed=11, median=200, lo=20, hi=4000, t_max=0.1):
+    """Samples of very uneven length: per-sample input spike count clip(round(lognormal(ln median, 1)), lo, hi),
+    channels uniform over n_in, times U(0, t_max). Returns spike trains (B, n_in, K_in) (K_in the largest
+    per-channel count, +inf padding), counts (B, n_in) and the per-sample event counts."""
+    rng = np.random.default_rng(seed)
+    counts = np.clip(np.round(rng.lognormal(np.log(median), 1.0, batch)), lo, hi).astype(np.int64)
+    chans = [rng.integers(0, n_in, c) for c in counts]
+    times = [np.sort(rng.uniform(0, t_max, c)).astype(np.float32) for c in counts]
+    k_in = max(int(np.bincount(ch, minlength=n_in).max()) for ch in chans)
+    t = np.full((batch, n_in, k_in), np.inf, dtype=np.float32)
+    for q, (ch, tm) in enumerate(zip(chans, times)):
+        order = np.argsort(ch, kind="stable")
+        ch_s, tm_s = ch[order], tm[order]
+        first = np.searchsorted(ch_s, ch_s, side="left")
+        t[q, ch_s, np.arange(len(ch_s)) - first] = tm_s
+    return t, np.isfinite(t).sum(2).astype(np.int32), counts

@@ -1,7 +1,7 @@
 """Generates the golden fixtures of tests/golden/ from the reference's own unit tests.
 
-Run in a container where the reference checkout exists (default /root/reference, or
-BATS_REFERENCE=<path>):   python tests/golden/make_golden.py
+Run where a checkout of the reference exists, naming it in BATS_REFERENCE:
+    BATS_REFERENCE=<path to the reference checkout> python tests/golden/make_golden.py
 
 The reference's tests (tests/**/*.py of Florian-BACHO/bats) import cupy and the bats package,
 neither of which can run without its GPU stack. This script loads the test files themselves with
@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from oracle import bats_ref64 as R  # noqa: E402
 
-REF = os.environ.get("BATS_REFERENCE", "/root/reference")
+REF = os.environ.get("BATS_REFERENCE", "")
 
 
 # ---- NumPy stand-in for cupy ----------------------------------------------------------------
@@ -579,8 +579,9 @@ def capture_known_answers():
 
 
 def main():
-    if not os.path.isdir(os.path.join(REF, "tests")):
-        raise SystemExit(f"reference tests not found under {REF}")
+    if not REF or not os.path.isdir(os.path.join(REF, "tests")):
+        raise SystemExit("set BATS_REFERENCE to a checkout of the reference (its tests/ folder was not found"
+                         + (f" under {REF})" if REF else ")"))
     install_fakes()
     results = run_reference_tests()
     capture_known_answers()

@@ -97,10 +97,11 @@ def test_binding_signatures_match_the_header():
     assert not wrong, wrong
 
 
-def test_layer_struct_matches_the_header():
+@pytest.mark.parametrize("struct", ["BatsFcLayer", "BatsFcTrainLayer"])
+def test_layer_structs_match_the_header(struct):
     from bats_gb300 import _lib
     src = _strip_comments(open(HEADER).read())
-    body = re.search(r"typedef struct BatsFcLayer \{(.*?)\} BatsFcLayer;", src, re.S).group(1)
+    body = re.search(r"typedef struct " + struct + r" \{(.*?)\} " + struct + ";", src, re.S).group(1)
     fields = []
     for line in body.split(";"):
         line = " ".join(line.replace("const ", " ").split())
@@ -110,10 +111,15 @@ def test_layer_struct_matches_the_header():
         head, name0 = first.replace("*", "* ").rsplit(" ", 1)
         for nm in [name0] + rest:
             ptr = "*" in head or nm.startswith("*")
-            fields.append((nm.lstrip("*"), "pointer" if ptr else _SCALARS[head.strip()]))
-    mirror = _lib.BatsFcLayer._fields_
+            kind = "pointer" if ptr else (head.strip() if head.strip().startswith("Bats") else _SCALARS[head.strip()])
+            fields.append((nm.lstrip("*"), kind))
+    mirror = getattr(_lib, struct)._fields_
     assert [f[0] for f in mirror] == [f[0] for f in fields]
-    assert all(_same(bt, ht) for (_, bt), (_, ht) in zip(mirror, fields))
+    for (_, bt), (_, ht) in zip(mirror, fields):
+        if isinstance(ht, str) and ht.startswith("Bats"):
+            assert bt is getattr(_lib, ht)  # a nested struct of the header, mirrored by the same name
+        else:
+            assert _same(bt, ht)
 
 
 def test_status_strings_and_version(lib):

@@ -167,3 +167,65 @@ def test_train_step_equals_kernel_chain_784_800_800_10_batch_256(cuda, variant):
         cnt = chain[li - 1][0]
         valid = torch.arange(KP, device="cuda")[None, None, :] < cnt[:, :, None]
         assert torch.equal(ts.pre_err[li][valid], err[valid]), f"layer {li + 1}: train-step pre errors differ"
+
+
+def test_uneven_batch_slice_vs_reference_kernels(cuda):
+    """The uneven-batch configuration (1024-1024-20, max_n_spike 30, weights U(-1, 1), thresholds 0.2 / 1.3,
+    inputs over 1024 channels with lognormal event counts, median 200, 20-4000 per sample, times U(0, 0.1) s) on
+    a slice of 48 samples that spans the whole range of lengths, the longest included: forward bit-identical to
+    the reference kernels with both the per-(tile, sample) and the persistent work-queue forward, and each
+    layer's batch-summed gradient and pre-spike errors within 1e-5 |ref| + 1e-5 sum|terms|."""
+    if not refkern.available():
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    from tests._helpers import uneven_input
+    t_all, n_all, ev_counts = uneven_input(512)
+    order = np.argsort(ev_counts, kind="stable")
+    pick = np.unique(np.r_[order[np.linspace(0, len(order) - 1, 47).astype(int)], order[-1]])
+    t, n_in = np.ascontiguousarray(t_all[pick]), np.ascontiguousarray(n_all[pick])
+    assert ev_counts[pick].max() == ev_counts.max() and ev_counts[pick].min() <= 25
+    rng = np.random.default_rng(12)
+    ws = [rng.uniform(-1, 1, (o, i)).astype(np.float32) for i, o in ((1024, 1024), (1024, 20))]
+    thetas = [0.2, 1.3]
+    tau32 = np.float32(2 * TAU_S)
+    x_ours, x_ref, c_ref = (torch.tensor(t, device="cuda"), torch.tensor(t, device="cuda"),
+                            torch.tensor(n_in, device="cuda"))
+    ours, refs, evs, wts = [], [], [], []
+    for li, (w, th) in enumerate(zip(ws, thetas)):
+        ev = K.sort_events(x_ours, TAU_S, tau32)
+        wt = K.transpose_weights(torch.tensor(w, device="cuda"))
+        o = K.lif_forward_fc(ev, wt, w.shape[0], KP, TAU_S, th, th, MAX_SIM)
+        oq = K.lif_forward_fc(ev, wt, w.shape[0], KP, TAU_S, th, th, MAX_SIM, algo=K.FWD_QUEUE)
+        L = refkern.RefLIF(torch.tensor(w, device="cuda"), TAU_S, th, th, KP)
+        r = L.forward(x_ref, c_ref, MAX_SIM)
+        _assert_same_forward(o, r, f"uneven layer {li + 1}")
+        _assert_same_forward(oq, r, f"uneven layer {li + 1} (work queue)")
+        ours.append(o)
+        refs.append(L)
+        evs.append(ev)
+        wts.append(wt)
+        x_ours, x_ref, c_ref = o[3], r[3], r[0]
+    spikes = [int(o[0].sum()) for o in ours]
+    assert min(spikes) > 100, spikes
+    labels = rng.integers(0, 20, len(pick))
+    err_in = (torch.where(torch.arange(20, device="cuda")[None, :] == torch.as_tensor(labels, device="cuda")[:, None],
+                          15.0, 3.0) - refs[-1].out[0].float())[:, :, None].repeat(1, 1, KP).contiguous()
+    report = []
+    for li in (1, 0):
+        n, a, x, ts, z = ours[li]
+        _, c, dtt = K.lif_constants(TAU_S, thetas[li], thetas[li])
+        tabs = K.backward_prep(ts, a, x, z, err_in.clone(), c, tau32, dtt)
+        n_pre = ws[li].shape[1]
+        g = K.weights_gradient(evs[li], ts, tabs, n_pre, per_sample=False,
+                               group=max(2, K.default_group(len(pick), ws[li].shape[0], n_pre)),
+                               reduce="sum").double().cpu().numpy()
+        g_ref, g_abs, pe_ref, pe_abs = ref_layer_backward(refs[li], err_in.clone(), want_pre=li > 0)
+        st = assert_sum_close(g, g_ref, g_abs, what=f"uneven layer {li + 1} gradient")
+        report.append(f"L{li + 1} gradient: {st[1]}/{st[0]} need sum|terms|, worst {st[2]:.3f}")
+        if li > 0:
+            pe = K.pre_errors(evs[li], wts[li], ts, tabs, TAU_S, tau32)
+            st = assert_sum_close(pe.double().cpu().numpy(), pe_ref.double().cpu().numpy(),
+                                  pe_abs.double().cpu().numpy(), what=f"uneven layer {li + 1} pre errors")
+            report.append(f"L{li + 1} pre errors: {st[1]}/{st[0]}, worst {st[2]:.3f}")
+            err_in = pe_ref.contiguous()
+    print(f"\n[uneven 1024-1024-20 slice of {len(pick)}, events {int(ev_counts[pick].min())}-"
+          f"{int(ev_counts[pick].max())}, spikes per layer {spikes}] " + "; ".join(report))

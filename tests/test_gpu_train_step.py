@@ -192,3 +192,38 @@ def test_programmatic_dependent_launch_keeps_results(cuda, tmp_path):
     pdl = np.load(out)
     for q, w in enumerate(ts.W):
         assert np.array_equal(w.cpu().numpy().view(np.uint32), pdl[f"arr_{q}"].view(np.uint32)), f"layer {q}"
+
+
+@pytest.mark.parametrize("tuned", [False, True])
+def test_c_abi_train_step_equals_the_launch_list(cuda, tuned):
+    """bats_fc_train_step (the whole train step as one call of the C ABI, for foreign callers) enqueues the same
+    entry points with the same arguments as FCTrainStep's launch list: after two steps the weights, their
+    transposed copies, Adam's moments, the gradients and the losses are bit-identical; with the autotuner's
+    variants (work-queue forward, other gradient groups) too, and the call can be captured in a CUDA graph."""
+    t, n, ws, labels = case(B=48, seed=4)
+    a, b = make_step(t, ws, labels), make_step(t, ws, labels)
+    if tuned:
+        choice = a.autotune(Autotuner(path=None), force=True)
+        b.fwd_algo, b.groups = list(a.fwd_algo), list(a.groups)
+        assert choice
+    for _ in range(2):
+        a.step()
+        b.native_step()
+    torch.cuda.synchronize()
+    for name in ("W", "Wt", "m", "v", "grad"):
+        for x, y in zip(getattr(a, name), getattr(b, name)):
+            assert torch.equal(x, y), name
+    assert torch.equal(a.loss, b.loss)
+    # Captured: one foreign call per step inside the graph.
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side):
+            b.native_step()
+    torch.cuda.current_stream().wait_stream(side)
+    g.replay()
+    a.step()
+    torch.cuda.synchronize()
+    for x, y in zip(a.W, b.W):
+        assert torch.equal(x, y)
