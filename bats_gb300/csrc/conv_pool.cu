@@ -212,7 +212,7 @@ conv_backward_cluster_kernel(const Event* __restrict__ ev, const int* __restrict
                              int C, int fx, int fy, int C_out, int Xo, int Yo, const float* __restrict__ post_t,
                              const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
                              int search_top, float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
-                             float* __restrict__ pre_err) {
+                             float* __restrict__ pre_err, int batch, int group) {
     pdl_prologue();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
@@ -222,14 +222,16 @@ conv_backward_cluster_kernel(const Event* __restrict__ ev, const int* __restrict
     const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;
-    const int s = blockIdx.y;
     const int taps = C_out * fx * fy;
     const int total = taps * C;
     const int n_post = Xo * Yo * C_out;
     for (int q = tid; q < total; q += blockDim.x) Gs[q] = 0.0f;
+    __syncthreads();
+    // The cluster's samples (one with group == 1: the per-sample gradient), accumulated in order.
+    const int s_end = min(batch, ((int)blockIdx.y + 1) * group);
+    for (int s = (int)blockIdx.y * group; s < s_end; ++s) {
     const int E = ev_count[s];
     const Event* evs = ev + (long long)s * ev_cap;
-    __syncthreads();
     for (int g = (int)rank; g * 32 < E; g += CONV_BWD_CLUSTER) {
         const int m0 = g * 32;
         const int cnt = min(32, E - m0);
@@ -299,13 +301,14 @@ conv_backward_cluster_kernel(const Event* __restrict__ ev, const int* __restrict
         }
         __syncthreads();
     }
+    }
     cluster.sync();
     const int per = (total + CONV_BWD_CLUSTER - 1) / CONV_BWD_CLUSTER;
     const int q_end = min(total, ((int)rank + 1) * per);
     for (int q = (int)rank * per + tid; q < q_end; q += blockDim.x) {
         float acc = 0.0f;
         for (int r = 0; r < CONV_BWD_CLUSTER; ++r) acc += cluster.map_shared_rank(Gs, r)[q];
-        grad[(long long)s * total + q] = acc;
+        grad[(long long)blockIdx.y * total + q] = acc;
     }
     cluster.sync();  // no CTA leaves while another still reads its shared memory
 }
@@ -324,7 +327,7 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
                              int Xo, int Yo, int k_pre, const float* __restrict__ post_t,
                              const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
                              float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
-                             float* __restrict__ pre_err) {
+                             float* __restrict__ pre_err, int batch, int group) {
     pdl_prologue();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
@@ -335,19 +338,21 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
     const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;
-    const int s = blockIdx.y;
     const int taps = C_out * fx * fy;
     const int total = taps * C;
     int* kcount = reinterpret_cast<int*>(Gs + total);
     const int n_post = Xo * Yo * C_out;
     for (int q = tid; q < total; q += blockDim.x) Gs[q] = 0.0f;
-    const int* bo = boff + (long long)s * (n_pos + 1);
-    const Event* evs = ev_b + (long long)s * ev_cap;
     // At most one tap per thread here (taps <= blockDim checked by the launcher).
     const int tp = tid;
     const bool has_tap = tp < taps;
     const int co = has_tap ? tp / (fx * fy) : 0, dx = has_tap ? (tp / fy) % fx : 0, dy = has_tap ? tp % fy : 0;
     __syncthreads();
+    // The cluster's samples (one with group == 1: the per-sample gradient), accumulated in order.
+    const int s_end = min(batch, ((int)blockIdx.y + 1) * group);
+    for (int s = (int)blockIdx.y * group; s < s_end; ++s) {
+    const int* bo = boff + (long long)s * (n_pos + 1);
+    const Event* evs = ev_b + (long long)s * ev_cap;
     for (int g = (int)rank; g < n_pos; g += CONV_BWD_CLUSTER) {
         const int beg = bo[g], end = bo[g + 1];
         if (beg >= end) continue;  // uniform over the CTA
@@ -399,13 +404,14 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
             __syncthreads();
         }
     }
+    }
     cluster.sync();
     const int per = (total + CONV_BWD_CLUSTER - 1) / CONV_BWD_CLUSTER;
     const int q_end = min(total, ((int)rank + 1) * per);
     for (int q = (int)rank * per + tid; q < q_end; q += blockDim.x) {
         float acc = 0.0f;
         for (int r = 0; r < CONV_BWD_CLUSTER; ++r) acc += cluster.map_shared_rank(Gs, r)[q];
-        grad[(long long)s * total + q] = acc;
+        grad[(long long)blockIdx.y * total + q] = acc;
     }
     cluster.sync();
 }
@@ -555,7 +561,7 @@ extern "C" int bats_conv_backward(const void* events, const int* ev_slot, const 
                                      reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap, weights,
                                      Y, C, fx, fy, C_out, Xo, Yo, post_times,
                                      reinterpret_cast<const float2*>(tables), nvalid, k_post, top, tau_s, tau,
-                                     pre_slots, grad_per_sample, pre_errors));
+                                     pre_slots, grad_per_sample, pre_errors, batch, 1));
         return BATS_OK;
     }
     BATS_CUDA(bats::launch(bats::conv_backward_kernel, batch, threads, 0, stream,
@@ -603,8 +609,92 @@ extern "C" int bats_conv_backward_grouped(const void* events_bucketed, const int
                                  reinterpret_cast<const bats::Event*>(events_bucketed), bucket_offsets, X * Y, ev_cap,
                                  weights, Y, C, fx, fy, C_out, Xo, Yo, k_pre, post_times,
                                  reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots,
-                                 grad_per_sample, pre_errors));
+                                 grad_per_sample, pre_errors, batch, 1));
     return BATS_OK;
+}
+
+// Sum of per-group partial filter gradients (groups, total) in group order, divided by the batch.
+namespace bats {
+__global__ void conv_grad_reduce_kernel(const float* __restrict__ part, int groups, int total, float batch,
+                                        float* __restrict__ grad) {
+    pdl_prologue();
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total) return;
+    float acc = 0.0f;
+    for (int g = 0; g < groups; ++g) acc += part[(long long)g * total + q];
+    grad[q] = acc / batch;
+}
+}  // namespace bats
+
+extern "C" size_t bats_conv_backward_adam_workspace_bytes(int batch, int C, int fx, int fy, int C_out, int group) {
+    if (batch <= 0 || group <= 0) return 0;
+    const long long groups = (batch + group - 1) / group;
+    return ((size_t)groups * C_out * fx * fy * C * sizeof(float) + 255) & ~(size_t)255;
+}
+
+extern "C" int bats_conv_backward_adam(const void* events, const int* ev_slot, const int* ev_count,
+                                       const void* events_bucketed, const int* bucket_offsets, long long ev_cap,
+                                       float* weights, int batch, int X, int Y, int C, int fx, int fy, int C_out,
+                                       int k_pre, const float* post_times, const void* tables, const int* nvalid,
+                                       int k_post, float tau_s, float tau, float* pre_errors, int group, float* grad,
+                                       float* m, float* v, float beta_1, float beta_2, float epsilon,
+                                       float learning_rate, const double* powers, void* workspace,
+                                       size_t workspace_bytes, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0 && X >= fx && Y >= fy && fx > 0 && fy > 0 && C > 0 && C_out > 0 && k_post > 0 &&
+                     k_pre > 0 && group >= 1,
+                 BATS_ERR_BAD_SHAPE, "conv_backward_adam: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(events && ev_slot && ev_count && weights && post_times && tables && nvalid && grad && m && v && powers,
+                 BATS_ERR_NULL, "conv_backward_adam: null pointer");
+    const int groups = (batch + group - 1) / group;
+    BATS_REQUIRE(groups <= 65535, BATS_ERR_BAD_SHAPE, "conv_backward_adam: more than 65535 sample groups");
+    BATS_REQUIRE(workspace && workspace_bytes >= bats_conv_backward_adam_workspace_bytes(batch, C, fx, fy, C_out, group),
+                 BATS_ERR_WORKSPACE, "conv_backward_adam: workspace too small");
+    const int Xo = X - fx + 1, Yo = Y - fy + 1;
+    const long long taps = (long long)C_out * fx * fy;
+    const int total = (int)(taps * C);
+    const long long pre_slots = (long long)X * Y * C * k_pre;
+    float* part = reinterpret_cast<float*>(workspace);
+    if (pre_errors) BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)batch * pre_slots * sizeof(float), stream));
+    const bool grouped = events_bucketed && bucket_offsets && taps <= 1024 && (long long)X * Y <= 255 &&
+                         (size_t)taps * C * sizeof(float) + (size_t)C * sizeof(int) <= 160 * 1024;
+    const size_t gbytes = (size_t)taps * C * sizeof(float) + (grouped ? (size_t)C * sizeof(int) : 0);
+    BATS_REQUIRE(gbytes <= 160 * 1024, BATS_ERR_BAD_SHAPE, "conv_backward_adam: filter gradient too large");
+    const int threads = (int)std::min<long long>(1024, ((taps + 31) / 32) * 32);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(bats::CONV_BWD_CLUSTER, groups);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = gbytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = bats::CONV_BWD_CLUSTER;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1 + (unsigned)bats::pdl_attribute(attr + 1);
+    if (grouped) {
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_grouped_kernel, (int)gbytes));
+        BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_grouped_kernel,
+                                     reinterpret_cast<const bats::Event*>(events_bucketed), bucket_offsets, X * Y,
+                                     ev_cap, (const float*)weights, Y, C, fx, fy, C_out, Xo, Yo, k_pre, post_times,
+                                     reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots,
+                                     part, pre_errors, batch, group));
+    } else {
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_cluster_kernel, (int)gbytes));
+        int top = 1;
+        while (top * 2 <= k_post) top *= 2;
+        BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_cluster_kernel,
+                                     reinterpret_cast<const bats::Event*>(events), ev_slot, ev_count, ev_cap,
+                                     (const float*)weights, Y, C, fx, fy, C_out, Xo, Yo, post_times,
+                                     reinterpret_cast<const float2*>(tables), nvalid, k_post, top, tau_s, tau,
+                                     pre_slots, part, pre_errors, batch, group));
+    }
+    BATS_CUDA(bats::launch(bats::conv_grad_reduce_kernel, (total + 255) / 256, 256, 0, stream, part, groups, total,
+                           (float)batch, grad));
+    BATS_CUDA(cudaGetLastError());
+    return bats_adam_step_device(grad, m, v, total, beta_1, beta_2, epsilon, learning_rate, powers, weights, nullptr,
+                                 0, 0, 0, stream);
 }
 
 extern "C" int bats_pool_forward(const int* n_spikes, const float* times, int batch, int X, int Y, int C, int K,

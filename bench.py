@@ -788,19 +788,52 @@ def conv_network():
     return step, layers, (t, n, labels)
 
 
+def conv_train_step(t, labels, group=2):
+    """The conv network of conv_network as a bats_gb300.conv_train.ConvTrainStep (batch-reduced filter
+    gradients fused with Adam, one CUDA graph), same weights and inputs."""
+    import torch
+    from bats_gb300.conv_train import ConvLayerSpec, ConvTrainStep, PoolLayerSpec
+    from bats_gb300.train import FCLayerSpec
+    Kc = 10
+    w1, w2, w3, w4 = conv_weights()
+    specs = [ConvLayerSpec((5, 5, 15), TAU_S, CONV_THETAS[0], CONV_THETAS[0], Kc), PoolLayerSpec(),
+             ConvLayerSpec((5, 5, 40), TAU_S, CONV_THETAS[1], CONV_THETAS[1], Kc), PoolLayerSpec(),
+             FCLayerSpec(300, TAU_S, CONV_THETAS[2], CONV_THETAS[2], Kc),
+             FCLayerSpec(10, TAU_S, CONV_THETAS[3], CONV_THETAS[3], Kc)]
+    ws = [torch.tensor(w1), None, torch.tensor(w2), None, torch.tensor(w3), torch.tensor(w4)]
+    ts = ConvTrainStep(t.shape[0], (28, 28, 1), 1, specs, ws, TARGET_TRUE, TARGET_FALSE, learning_rate=LR,
+                       max_simulation=MAX_SIM, conv_group=group)
+    ts.set_inputs(torch.tensor(t), torch.tensor(labels))
+    return ts
+
+
 def conv_bench(steps: int = 5):
-    """The conv network's train step (conv_network) timed, next to the same step on the reference's own CUDA
-    kernels."""
+    """The conv network's train step: batch-reduced and graph-captured (ConvTrainStep, `value`), through the
+    drop-in layer API (conv_network, `plain_api`), and on the reference's own CUDA kernels (`refkern`)."""
     import torch
     Bc = 128
     step, layers, (t, n, labels) = conv_network()
     flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    ms, _ = time_steps(step, steps, 3, flush)
+    ms_api, _ = time_steps(step, steps, 3, flush)
     spikes = [int(L.spike_trains[1].sum().item()) for L in layers]
+    del step, layers
+    torch.cuda.empty_cache()
+    ts = conv_train_step(t, labels)
+    graphed = ts.try_capture()
+    ms, _ = time_steps(ts.replay if graphed else ts.step, steps, 3, flush)
+    rec = ts.profile_step()
+    torch.cuda.synchronize()
     res = {"value": Bc * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps, "steps": steps,
-           "batch": Bc, "spikes_per_layer": spikes,
+           "batch": Bc, "graph": graphed, "spikes_per_layer": spikes,
+           "kernels_ms": {k: round(a.elapsed_time(b), 4) for k, (a, b) in rec.items()},
            "network": "28x28x1 -> conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> 300 -> 10, K 10",
-           "what": "full train step through Network/ConvLIFLayer/PoolingLayer/LIFLayer/AdamOptimizer"}
+           "what": "ConvTrainStep: batch-reduced filter gradients fused with Adam, whole step as one CUDA graph",
+           "plain_api": {"value": Bc * steps / (ms_api / 1e3), "unit": "samples/s", "ms_per_step": ms_api / steps,
+                         "what": "Network/ConvLIFLayer/PoolingLayer/LIFLayer/AdamOptimizer drop-in API, per-sample "
+                                 "gradients and the caller's batch mean"}}
+    res["batched_vs_plain"] = res["value"] / res["plain_api"]["value"]
+    del ts
+    torch.cuda.empty_cache()
     res["refkern"] = refkern_conv_rate(t, n, labels, flush)
     return res
 

@@ -381,6 +381,26 @@ int bats_serve_fc_batch(const int* h_indices, const float* h_times, const int* h
                         void* sort_workspace, size_t sort_workspace_bytes, int* h_out_counts, float* h_out_times,
                         int* h_overflow, cudaStream_t stream);
 
+/* Batch-mean filter gradient of a conv layer fused with its Adam update, for a train step: no per-sample
+ * gradient is formed. The backward kernel of bats_conv_backward (bats_conv_backward_grouped's when the
+ * position-bucketed events are given and the layer fits it) runs on clusters that each accumulate `group`
+ * samples into one partial filter gradient in the workspace (bats_conv_backward_adam_workspace_bytes); the
+ * partials are summed in group order and divided by the batch into `grad` (C_out, fx, fy, C_in), then Adam
+ * (bias corrections from `powers`, as bats_adam_step_device) updates m, v and the filters in place. The
+ * pre-spike errors (B, X*Y*C, k_pre), when pre_errors is not NULL, use the filters before the update.
+ * Replaces compute_weights_gradient_conv + the batch mean + AdamOptimizer.step + add_deltas
+ * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient_conv.py:11-32,
+ * experiments/mnist/train_conv.py, bats/Layers/ConvLIFLayer.py:109-137) and propagate_errors_to_pre_spikes_conv
+ * (propagate_errors_to_pre_spikes_conv.py:11-32). */
+size_t bats_conv_backward_adam_workspace_bytes(int batch, int C, int fx, int fy, int C_out, int group);
+int bats_conv_backward_adam(const void* events, const int* ev_slot, const int* ev_count, const void* events_bucketed,
+                            const int* bucket_offsets, long long ev_cap, float* weights, int batch, int X, int Y, int C,
+                            int fx, int fy, int C_out, int k_pre, const float* post_times, const void* tables,
+                            const int* nvalid, int k_post, float tau_s, float tau, float* pre_errors, int group,
+                            float* grad, float* m, float* v, float beta_1, float beta_2, float epsilon,
+                            float learning_rate, const double* powers, void* workspace, size_t workspace_bytes,
+                            cudaStream_t stream);
+
 /* ---- Training step ---------------------------------------------------------------------------- */
 
 /* Forward kernel choices of bats_fc_train_step beyond BATS_FWD_TILE/LANES/TILE64: the persistent work-queue
