@@ -122,7 +122,12 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
                 b = bb;
             } else {
                 // Pass 2: no crossing is possible before the first marked event, so its state is
-                // reached by the plain accumulation; from there on, the reference's event-by-event loop.
+                // reached by the plain accumulation; from there on, the reference's event-by-event loop for
+                // every marked event. An unmarked event keeps the first pass's verdict: before a spike of this
+                // stage its state is the first pass's, and after one the state has the same a and a lower b
+                // (a reset lowers b and the accumulation is monotone in b), for which the reference's computed
+                // spike time can only be later, so a state in the screen's range still has no crossing
+                // (replay_keeps_verdict).
                 const int first = __ffs(cand) - 1;
                 for (int u = 0; u < first; ++u) {
                     const float wu = sm.rows[slot][u][tid];
@@ -134,6 +139,7 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
                     const float wu = sm.rows[slot][u][tid];
                     a = fmaf(wu, e.es, a);
                     b = fmaf(wu, e.e, b);
+                    if (!((cand >> u) & 1u) && replay_keeps_verdict(a, b, sk)) continue;
                     const bool has_next = m0 + u + 1 < E;
                     const float t_next = has_next ? se[u + 1].t : BATS_INF;
                     const float e_next = has_next ? se[u + 1].e : BATS_INF;
