@@ -2,10 +2,13 @@
 drop-in API on the reference's MNIST conv network (28x28x1 -> conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> 300
 -> 10, max_n_spike 10, thresholds 0.04 / 0.8 / 0.6 / 0.3, weights U(-1, 1)), batch 32, Adam lr 3e-3:
 
-* the first step's loss is identical (same forward kernels and loss);
-* after each of 3 steps every layer's weights agree within 1e-6 of the layer's weight scale: the batch mean is
-  the same sum taken in another order (per-group partials accumulated by the backward kernels instead of
-  per-sample gradients and torch.mean), and Adam's first steps move every weight by about the learning rate;
+* the first step's loss and every layer's spike counts are identical (same forward kernels and loss);
+* every layer's batch-mean gradient of the first step agrees within 1e-5 of the layer's largest entry: the
+  batch mean is the same sum taken in another order (per-group partials accumulated by the backward kernels
+  instead of per-sample gradients and torch.mean);
+* the weights after that step agree within 1e-6 of the layer's weight scale wherever the gradient is not tiny
+  (|g| > 1e-3 max|g|): Adam's first step moves a weight by lr g / (|g| + eps), which for a gradient that is a
+  cancelling sum near zero turns last-bit differences of g into differences of the step itself;
 * replaying the captured CUDA graph gives the eager step's weights bit for bit.
 """
 import numpy as np
@@ -71,7 +74,8 @@ def api_steps(ws, t, n, labels, steps):
         g = net.backward(err)
         net.apply_deltas(opt.step([None if x is None else x.mean(0) for x in g]))
         out.append((loss.clone(), [L.weights.clone() for L in (c1, c2, f1, f2)],
-                    [int(L.spike_trains[1].sum()) for L in (c1, c2, f1, f2)]))
+                    [int(L.spike_trains[1].sum()) for L in (c1, c2, f1, f2)],
+                    [x.mean(0) for x in g if x is not None]))
     return out
 
 
@@ -79,18 +83,21 @@ def test_conv_train_step_matches_layer_api(cuda):
     t, n = mnist_like_input(B, seed=7)
     labels = np.random.default_rng(8).integers(0, 10, B).astype(np.int32)
     ws = weights()
-    ref = api_steps(ws, t, n, labels, 3)
+    ref = api_steps(ws, t, n, labels, 1)
     ts = make_step(ws, t, labels)
-    for k in range(3):
-        ts.step()
-        torch.cuda.synchronize()
-        if k == 0:
-            assert torch.equal(ts.loss, ref[0][0]), "first-step loss differs from the layer API"
-            spikes = [c for c, d in zip(ts.spike_counts(), ts.L) if d["kind"] != "pool"]
-            assert spikes == ref[0][2] and min(spikes[:3]) > 0, spikes
-        mine = [w for w in ts.weights if w is not None]
-        for li, (w, rw) in enumerate(zip(mine, ref[k][1])):
-            assert float((w - rw).abs().max()) <= 1e-6 * float(rw.abs().max()), f"step {k}, layer {li}"
+    ts.step()
+    torch.cuda.synchronize()
+    assert torch.equal(ts.loss, ref[0][0]), "first-step loss differs from the layer API"
+    spikes = [c for c, d in zip(ts.spike_counts(), ts.L) if d["kind"] != "pool"]
+    assert spikes == ref[0][2] and min(spikes[:3]) > 0, spikes
+    grads = [d["grad"] for d in ts.L if d["kind"] != "pool"]
+    mine = [w for w in ts.weights if w is not None]
+    for li, (g, rg, w, rw) in enumerate(zip(grads, ref[0][3], mine, ref[0][1])):
+        scale = float(rg.abs().max())
+        assert scale > 0, f"layer {li}: zero gradient"
+        assert float((g - rg).abs().max()) <= 1e-5 * scale, f"layer {li}: gradient"
+        big = rg.abs() > 1e-3 * scale
+        assert float((w - rw)[big].abs().max()) <= 1e-6 * float(rw.abs().max()), f"layer {li}: weights"
 
 
 @pytest.mark.parametrize("group", [1, 3])
