@@ -116,23 +116,6 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_start, flo
     return usable && (level1 || right_of_window || left_of_window);
 }
 
-// Whether an event that no_crossing<false, false> ruled out in a first pass over a stage (on the state
-// accumulated without the stage's resets) can be skipped when the stage is replayed with the exact solver. The
-// replayed state has the same a and a b no larger than the first pass's: each reset subtracts
-// (delta_theta/tau) z with z > 0, and fma(w, e, b) is monotone in b. A lower b that turned negative is
-// rejected by sign as in no_crossing, and so is any b when a <= 0. For 0 <= b <= b_first and a > 0, every step
-// of the reference's root is monotone in b (fl(b*b), the discriminant, sqrtf, x + b, then 2a / (x + b)), so its
-// z is no smaller than the first pass's: a negative discriminant stays negative (level 1), and a root right of
-// the window stays right of it, the right-of-window margin covering __logf's documented error at any larger z
-// (beyond e^8 the logarithm exceeds ln 2980, the right test's limit). The state must stay in the range where
-// those arguments were made (2^-60 <= |b| <= 2^60, |a| <= 2^60); a state outside it is solved exactly. Checked
-// on the host against the reference solver's restatement (tests/test_replay_transfer.py), which also shows that
-// raising b instead breaks it.
-__device__ __forceinline__ bool replay_keeps_verdict(float a, float b, const SolveConst& k) {
-    const float ab = fabsf(b);
-    return k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && fabsf(a) <= 0x1p60f;
-}
-
 // Screen of a run of consecutive events (FC layer, tau = 2 tau_s): true when the reference solver provably
 // accepts no crossing after any event of the run, given the run's states (a_u, b_u) only through
 // amin = min_u a_u and bmax = max_u b_u, and e_first = exp(t/tau) of the run's first event.

@@ -400,21 +400,26 @@ bwd_grad_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, 
     }
 }
 
-// Weight gradient over bucketed events: blockIdx.y is a pre-neuron bucket of JC neurons and the CTA
-// reads only that bucket's events of each sample (bats_sort_events with bucket_width == JC), in time
-// order, instead of filtering the whole event list. Same ownership and write-out as bwd_grad_kernel.
+// Weight gradient over bucketed events: blockIdx.y is a pre-neuron bucket of JC neurons and the CTA reads only
+// that bucket's events of each sample (bats_sort_events with bucket_width == JC), in time order, instead of
+// filtering the whole event list; ownership and write-out as bwd_grad_kernel. The CTA's warps are independent
+// of one another: a warp owns 32 post neurons (columns of the shared-memory gradient tile), reads the bucket's
+// events of each sample of its group itself, 32 at a time into its own slice of shared memory, and skips the
+// samples in which none of its own neurons spiked. There is no barrier between samples (one at the end, for
+// the partial's zero flag), so a warp waiting on a sample's cursor loads does not hold the others back. Every
+// (i, j) entry receives its terms in the order bwd_grad_kernel adds them (events in time order, samples in
+// group order): the results are bit-identical to it.
 template <int TILE, int JC>
 __global__ void __launch_bounds__(TILE)
-bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__ boff, int n_buckets,
-                         long long ev_cap, const float* __restrict__ post_t, const float2* __restrict__ tab,
-                         const int* __restrict__ nvalid, int n_post, int k_post, int n_pre, int batch, int group,
-                         float* __restrict__ out, int* __restrict__ flags) {
+bwd_grad_warp_kernel(const Event* __restrict__ ev_b, const int* __restrict__ boff, int n_buckets, long long ev_cap,
+                     const float* __restrict__ post_t, const float2* __restrict__ tab, const int* __restrict__ nvalid,
+                     int n_post, int k_post, int n_pre, int batch, int group, float* __restrict__ out,
+                     int* __restrict__ flags) {
     pdl_prologue();
     constexpr int WARPS = TILE / 32;
     __shared__ float G[JC][TILE + 1];
-    __shared__ Event sev[BWD_CHUNK];
-    __shared__ int s_beg[32], s_end_[32];
-    __shared__ unsigned s_spk[WARPS];
+    __shared__ Event sev[WARPS][32];
+    __shared__ int s_worked;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int i = blockIdx.x * TILE + tid;
     const bool active = i < n_post;
@@ -422,93 +427,87 @@ bwd_grad_bucketed_kernel(const Event* __restrict__ ev_b, const int* __restrict__
     const int J0 = bucket * JC;
     const int g = blockIdx.z;
     for (int q = tid; q < JC * (TILE + 1); q += TILE) (&G[0][0])[q] = 0.0f;
-
+    if (tid == 0) s_worked = 0;
+    __syncthreads();
+    Event* wev = sev[warp];
     const int s_begin = g * group;
     const int s_end = min(batch, s_begin + group);
-    bool worked = false;  // some sample had events in the bucket and a spike in the tile (CTA-uniform)
+    bool worked = false;  // warp-uniform: some sample had events in the bucket and a spike in this warp
     for (int s0 = s_begin; s0 < s_end; s0 += 32) {
-        // Window of up to 32 samples: their bucket ranges, and for each whether any neuron of the tile
-        // spiked, are read at once (independent loads), so that samples with nothing to do cost nothing.
+        // Up to 32 samples at once: lane q reads sample s0 + q's bucket range, and bit q of spk says whether any
+        // of the warp's neurons spiked in it (independent loads, issued together).
         const int ws = min(32, s_end - s0);
-        __syncthreads();  // the previous window's flags have been read
-        if (tid < ws) {
-            const int* bo = boff + (long long)(s0 + tid) * (n_buckets + 1);
-            s_beg[tid] = bo[bucket];
-            s_end_[tid] = bo[bucket + 1];
+        int beg_l = 0, end_l = 0;
+        if (lane < ws) {
+            const int* bo = boff + (long long)(s0 + lane) * (n_buckets + 1);
+            beg_l = bo[bucket];
+            end_l = bo[bucket + 1];
         }
-        unsigned spk = 0u;  // bit q: some neuron of this warp spiked in sample s0 + q
+        unsigned spk = 0u;
         for (int q = 0; q < ws; ++q) {
             const int nq = active ? nvalid[(long long)(s0 + q) * n_post + i] : 0;
             spk |= __ballot_sync(0xffffffffu, nq > 0) ? (1u << q) : 0u;
         }
-        if (lane == 0) s_spk[warp] = spk;
-        __syncthreads();
-        unsigned any = 0u;
-#pragma unroll
-        for (int w = 0; w < WARPS; ++w) any |= s_spk[w];
         for (int q = 0; q < ws; ++q) {
-            const int s = s0 + q;
-            const int beg = s_beg[q], end = s_end_[q];
-            if (beg >= end || !((any >> q) & 1u)) continue;
+            const int beg = __shfl_sync(0xffffffffu, beg_l, q), end = __shfl_sync(0xffffffffu, end_l, q);
+            if (beg >= end || !((spk >> q) & 1u)) continue;
             worked = true;
+            const int s = s0 + q;
             const long long pn = (long long)s * n_post + (active ? i : 0);
             const int n = active ? nvalid[pn] : 0;
-            const float* tp = post_t + pn * k_post;
-            const float2* tb = tab + pn * (k_post + 1);
             PostCursor cur;
-            cur.init(tp, tb, n);
+            cur.init(post_t + pn * k_post, tab + pn * (k_post + 1), n);
             const Event* evs = ev_b + (long long)s * ev_cap;
-            for (int m0 = beg; m0 < end; m0 += BWD_CHUNK) {
-                const int cnt = min(BWD_CHUNK, end - m0);
-                __syncthreads();
-                for (int r = tid; r < cnt; r += TILE) sev[r] = evs[m0 + r];
-                __syncthreads();
-                if (n == 0) continue;
-                // Four events at a time: their terms are formed in event order (the cursor only moves
-                // forward), then the four shared-memory updates are issued with all loads first when the
-                // four pre neurons differ (the usual case), so that they do not wait on one another. Every
-                // G[j][i] still receives its terms in event order.
-                int m = 0;
-                for (; m + 4 <= cnt; m += 4) {
-                    float v[4];
-                    int jj[4];
+            for (int m0 = beg; m0 < end; m0 += 32) {
+                const int cnt = min(32, end - m0);
+                __syncwarp();
+                if (lane < cnt) wev[lane] = evs[m0 + lane];
+                __syncwarp();
+                if (n > 0) {
+                    // Four events at a time, as in bwd_grad_bucketed_kernel: terms in event order, the four
+                    // shared-memory updates issued with all loads first when the four pre neurons differ.
+                    int m = 0;
+                    for (; m + 4 <= cnt; m += 4) {
+                        float v[4];
+                        int jj[4];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const Event e = sev[m + u];
+                        for (int u = 0; u < 4; ++u) {
+                            const Event e = wev[m + u];
+                            cur.advance_past(e.t);
+                            jj[u] = e.j - J0;
+                            v[u] = cur.valid() ? fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y)) : 0.0f;
+                        }
+                        const bool distinct = jj[0] != jj[1] && jj[0] != jj[2] && jj[0] != jj[3] && jj[1] != jj[2] &&
+                                              jj[1] != jj[3] && jj[2] != jj[3];
+                        if (distinct) {
+                            float gg[4];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) gg[u] = G[jj[u]][tid];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                if (v[u] != 0.0f) G[jj[u]][tid] = gg[u] + v[u];
+                        } else {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                if (v[u] != 0.0f) G[jj[u]][tid] += v[u];
+                        }
+                    }
+                    for (; m < cnt; ++m) {
+                        const Event e = wev[m];
                         cur.advance_past(e.t);
-                        jj[u] = e.j - J0;
-                        v[u] = cur.valid() ? fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y)) : 0.0f;
+                        if (cur.valid()) G[e.j - J0][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
                     }
-                    const bool distinct = jj[0] != jj[1] && jj[0] != jj[2] && jj[0] != jj[3] && jj[1] != jj[2] &&
-                                          jj[1] != jj[3] && jj[2] != jj[3];
-                    if (distinct) {
-                        float g[4];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) g[u] = G[jj[u]][tid];
-#pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            if (v[u] != 0.0f) G[jj[u]][tid] = g[u] + v[u];
-                    } else {
-#pragma unroll
-                        for (int u = 0; u < 4; ++u)
-                            if (v[u] != 0.0f) G[jj[u]][tid] += v[u];
-                    }
-                }
-                for (; m < cnt; ++m) {
-                    const Event e = sev[m];
-                    cur.advance_past(e.t);
-                    if (cur.valid()) G[e.j - J0][tid] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
                 }
             }
         }
     }
-    if (flags) {
-        // A partial that is all zero is not written; the reduction skips it (adding +0 changes nothing:
-        // a partial is a sum of nonzero terms, never -0).
-        if (tid == 0) flags[((long long)g * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = worked ? 1 : 0;
-        if (!worked) return;
-    }
+    if (worked && lane == 0) s_worked = 1;
     __syncthreads();
+    if (flags) {
+        // A partial that is all zero is not written; the reduction skips it.
+        if (tid == 0) flags[((long long)g * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = s_worked;
+        if (!s_worked) return;
+    }
     const long long obase = (long long)g * n_post * n_pre;
     for (int q = tid; q < TILE * JC; q += TILE) {
         const int ii = q / JC, jj = q % JC;
@@ -729,7 +728,7 @@ bwd_pre_err_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_coun
 // With few post neurons, one thread per post neuron leaves most lanes idle and the per-sample CTA
 // serial over all events; here lanes take events instead, and every lane runs over the (few) post
 // neurons. The sample's post-spike times, suffix tables and counts are staged in shared memory.
-// (The weight gradient of narrow layers keeps the thread-per-neuron merge of bwd_grad_bucketed_kernel,
+// (The weight gradient of narrow layers keeps the thread-per-neuron merge of bwd_grad_warp_kernel,
 // which costs a few instructions per event for all neurons at once, with more sample groups instead.)
 
 // Post-spike position of every post neuron for a pre spike at time t: p = number of valid post spikes
@@ -924,7 +923,7 @@ static cudaError_t launch_grad(const void* events, const int* ev_count, const vo
                                float* out, int* flags, cudaStream_t stream) {
     dim3 grid((n_post + TILE - 1) / TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
     if (ev_b)
-        return bats::launch(bats::bwd_grad_bucketed_kernel<TILE, GRAD_JC>, grid, TILE, 0, stream,
+        return bats::launch(bats::bwd_grad_warp_kernel<TILE, GRAD_JC>, grid, TILE, 0, stream,
                             reinterpret_cast<const bats::Event*>(ev_b), boff, n_buckets, ev_cap, post_times,
                             reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out,
                             flags);

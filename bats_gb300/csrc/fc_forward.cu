@@ -31,94 +31,6 @@
 
 namespace bats {
 
-// The exact replay of a stage's candidates, shared by the CTA's consumer warps. After the first pass every
-// neuron with a possible crossing (a marked event) posts its stage-start state; the posted neurons of all
-// consumer warps are then replayed side by side, one per thread, and the results are read back by their
-// owners. Each replaying thread accumulates up to its own next event that needs the solver and the solver
-// calls of all of them coincide, so a stage costs about one solver pass for the whole CTA (the number of
-// marked events of its busiest neuron) instead of one per warp and distinct marked position. The per-neuron
-// arithmetic (accumulation order, solver, windows) is unchanged, so results stay bit-identical.
-// Counts are kept three stages deep and states two, so that no stage's writes can meet a slower warp's reads
-// of an earlier stage (every warp has passed the previous stage's `posted` barrier before any warp writes).
-template <int TILE>
-struct ReplaySmem {
-    uint64_t posted;     // every consumer thread has posted its candidate (if any) of the stage
-    uint64_t replayed;   // every consumer thread has finished its replays of the stage
-    int count[3];        // candidates of a stage, by stage index mod 3
-    float a[2][TILE];    // stage-start state of each candidate, then its state after the stage
-    float b[2][TILE];
-    int owner[2][TILE];  // the candidate's thread (post neuron of the tile)
-    int info[2][TILE];   // spikes so far | marked events << 16; after the replay: spikes | buffer full << 30
-};
-
-struct WorkItem {
-    int s;      // sample, < 0: no work left
-    int tile0;  // first post neuron of the tile
-    int E;      // events of the sample
-    int unused;
-};
-struct ItemMailbox {
-    uint64_t full[2];   // the producer has written item[q] (one arrival)
-    uint64_t empty[2];  // every consumer warp has read item[q] (one arrival per warp)
-    WorkItem item[2];
-};
-
-template <typename Smem>
-__host__ __device__ constexpr size_t mailbox_offset() {
-    return (sizeof(Smem) + 15) / 16 * 16;
-}
-// The replay scratch follows the stage ring (the tile kernel) or the mailbox (the queue kernel).
-template <typename Smem>
-__host__ __device__ constexpr size_t replay_offset() {
-    return mailbox_offset<Smem>() + (sizeof(ItemMailbox) + 15) / 16 * 16;
-}
-template <int TILE, int SEV, int STAGES>
-__host__ __device__ constexpr size_t forward_smem_bytes() {
-    return replay_offset<StreamSmem<TILE, SEV, STAGES>>() + sizeof(ReplaySmem<TILE>);
-}
-
-template <int TILE>
-__device__ __forceinline__ void replay_init(ReplaySmem<TILE>& rs) {
-    if (threadIdx.x == 0) {
-        mbar_init(&rs.posted, TILE);
-        mbar_init(&rs.replayed, TILE);
-        rs.count[0] = rs.count[1] = rs.count[2] = 0;
-    }
-}
-
-// Replays one candidate neuron (owner thread r) over the stage's events 0 .. cnt - 1 from its stage-start
-// state: every event is accumulated; the solver runs at the marked events and, after a spike of this stage, at
-// any state outside the range where the first pass's verdict carries over (replay_keeps_verdict). Returns
-// true when the neuron's spike buffer is full.
-template <int TILE, int SEV, int STAGES>
-__device__ __forceinline__ bool replay_candidate(const StreamSmem<TILE, SEV, STAGES>& sm, int slot, int r, int m0, int E,
-                                                 int cnt, unsigned marked, float& a, float& b, int& n, int k_post,
-                                                 const SolveConst& sk, float* ao, float* xo, float* to, float* zo) {
-    const Event* se = sm.evs[slot];
-    bool spiked = false;
-    int u = 0;
-    while (true) {
-        int v = -1;  // the next event that needs the solver
-        for (; u < cnt; ++u) {
-            const float w = sm.rows[slot][u][r];
-            a = fmaf(w, se[u].es, a);
-            b = fmaf(w, se[u].e, b);
-            if (((marked >> u) & 1u) || (spiked && !replay_keeps_verdict(a, b, sk))) {
-                v = u++;
-                break;
-            }
-        }
-        if (v < 0) return false;
-        const Event e = se[v];
-        const bool has_next = m0 + v + 1 < E;
-        const float t_next = has_next ? se[v + 1].t : BATS_INF;
-        const float e_next = has_next ? se[v + 1].e : BATS_INF;
-        const int n0 = n;
-        if (solve_crossings<false>(a, b, e.t, t_next, e.e, e_next, sk, n, k_post, ao, xo, to, zo)) return true;
-        spiked |= n > n0;
-    }
-}
-
 // Consumer warps' part of one work item (sample s, post neurons tile0 .. tile0 + TILE - 1): thread = post
 // neuron. The item's event stages are stages k0 .. k0 + ceil(E / SEV) - 1 of the CTA's ring (k0 = 0 when the
 // CTA has one item). Returns false when a wait gave up (the CTA is aborting).
@@ -127,8 +39,7 @@ __device__ __forceinline__ bool replay_candidate(const StreamSmem<TILE, SEV, STA
 // its events (quiet neurons: one test per stage instead of one per event); otherwise the stage is
 // evaluated as without SCREEN. The FMA sequence is the same either way, so results are bit-identical.
 template <int TILE, int SEV, int STAGES, bool SCREEN = false>
-__device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>& sm, ReplaySmem<TILE>& rs,
-                                                  int& replays, int k0, int s, int tile0, int E,
+__device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>& sm, int k0, int s, int tile0, int E,
                                                   int n_post, int k_post, const SolveConst& sk,
                                                   int* __restrict__ n_spikes, float* __restrict__ a_out,
                                                   float* __restrict__ x_out, float* __restrict__ t_out,
@@ -153,12 +64,12 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
         const int m0 = k * SEV;
         const int cnt = min(SEV, E - m0);
         const Event* se = sm.evs[slot];
-        unsigned cand = 0u;
         if (!done) {
             // Pass 1: accumulate the stage's events (the reference's FMA sequence) and mark every event
             // after which a crossing cannot be ruled out. Branch-free, so the per-event tests of the
             // stage overlap; events past the sample's end (last stage) leave the state unchanged.
             float aa = a, bb = b;
+            unsigned cand = 0u;
             bool screened = false;
             if (SCREEN && m0 + SEV < E) {
                 float amin = BATS_INF, bmax = -BATS_INF, amag = BATS_INF;
@@ -209,44 +120,26 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
             if (cand == 0u) {
                 a = aa;
                 b = bb;
-            }
-        }
-        // Candidates of the stage: posted, replayed side by side, read back (see ReplaySmem).
-        const int cq = kg % 3, pb = kg & 1;
-        if (threadIdx.x == 0) rs.count[(kg + 1) % 3] = 0;  // every warp has read it (stage kg - 2)
-        int my_q = -1;
-        if (cand != 0u) {
-            my_q = atomicAdd(&rs.count[cq], 1);
-            rs.a[pb][my_q] = a;
-            rs.b[pb][my_q] = b;
-            rs.owner[pb][my_q] = tid;
-            rs.info[pb][my_q] = n | (int)(cand << 16);
-        }
-        mbar_arrive(&rs.posted);
-        if (!mbar_wait(&rs.posted, kg & 1, &sm.abort, status)) return false;
-        const int n_cand = rs.count[cq];
-        if (n_cand > 0) {
-            for (int q = tid; q < n_cand; q += TILE) {
-                const int r = rs.owner[pb][q];
-                const int info = rs.info[pb][q];
-                float ra = rs.a[pb][q], rb = rs.b[pb][q];
-                int rn = info & 0xffff;
-                const long long rbase = ((long long)s * n_post + tile0 + r) * k_post;
-                const bool full = replay_candidate(sm, slot, r, m0, E, cnt, (unsigned)info >> 16, ra, rb, rn, k_post,
-                                                   sk, a_out + rbase, x_out + rbase, t_out + rbase, z_out + rbase);
-                rs.a[pb][q] = ra;
-                rs.b[pb][q] = rb;
-                rs.info[pb][q] = rn | (full ? (1 << 30) : 0);
-            }
-            mbar_arrive(&rs.replayed);
-            if (!mbar_wait(&rs.replayed, replays & 1, &sm.abort, status)) return false;
-            ++replays;
-            if (my_q >= 0) {
-                a = rs.a[pb][my_q];
-                b = rs.b[pb][my_q];
-                const int info = rs.info[pb][my_q];
-                n = info & 0xffff;
-                done = (info >> 30) & 1;
+            } else {
+                // Pass 2: no crossing is possible before the first marked event, so its state is
+                // reached by the plain accumulation; from there on, the reference's event-by-event loop.
+                const int first = __ffs(cand) - 1;
+                for (int u = 0; u < first; ++u) {
+                    const float wu = sm.rows[slot][u][tid];
+                    a = fmaf(wu, se[u].es, a);
+                    b = fmaf(wu, se[u].e, b);
+                }
+                for (int u = first; u < cnt; ++u) {
+                    const Event e = se[u];
+                    const float wu = sm.rows[slot][u][tid];
+                    a = fmaf(wu, e.es, a);
+                    b = fmaf(wu, e.e, b);
+                    const bool has_next = m0 + u + 1 < E;
+                    const float t_next = has_next ? se[u + 1].t : BATS_INF;
+                    const float e_next = has_next ? se[u + 1].e : BATS_INF;
+                    done = solve_crossings<false>(a, b, e.t, t_next, e.e, e_next, sk, n, k_post, ao, xo, to, zo);
+                    if (done) break;
+                }
             }
         }
         stream_release(sm, kg);
@@ -277,7 +170,6 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
     extern __shared__ __align__(128) unsigned char smem_raw[];
     using Smem = StreamSmem<TILE, SEV, STAGES>;
     Smem& sm = *reinterpret_cast<Smem*>(smem_raw);
-    ReplaySmem<TILE>& rs = *reinterpret_cast<ReplaySmem<TILE>*>(smem_raw + replay_offset<Smem>());
     constexpr int CONSUMER_WARPS = TILE / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s = blockIdx.y;
@@ -285,16 +177,14 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
     const int E = ev_count[s];
     const int n_stages = (E + SEV - 1) / SEV;
     const Event* evs = ev + (long long)s * ev_cap;
-    replay_init(rs);
-    stream_init(sm, CONSUMER_WARPS);  // thread 0: the stage barriers, then the barrier-init fence
+    stream_init(sm, CONSUMER_WARPS);
     __syncthreads();
     if (warp == CONSUMER_WARPS) {
         stream_produce(sm, evs, E, wt, ld, tile0, n_stages, lane, status);
         return;
     }
-    int replays = 0;
-    forward_tile_item<TILE, SEV, STAGES, SCREEN>(sm, rs, replays, 0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out,
-                                                x_out, t_out, z_out, status, pad);
+    forward_tile_item<TILE, SEV, STAGES, SCREEN>(sm, 0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out, x_out, t_out,
+                                                z_out, status, pad);
 }
 
 // Persistent variant over a work queue, for batches whose samples carry very different numbers of events.
@@ -307,6 +197,23 @@ lif_fc_forward_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_c
 // on across items), so no CTA start-up or pipeline fill sits between items. Items reach the consumers
 // through a two-slot mailbox with its own full/empty mbarriers. Each item computes exactly what the
 // one-item-per-CTA kernel computes for it, so results are bit-identical to lif_fc_forward_kernel's.
+struct WorkItem {
+    int s;      // sample, < 0: no work left
+    int tile0;  // first post neuron of the tile
+    int E;      // events of the sample
+    int unused;
+};
+struct ItemMailbox {
+    uint64_t full[2];   // the producer has written item[q] (one arrival)
+    uint64_t empty[2];  // every consumer warp has read item[q] (one arrival per warp)
+    WorkItem item[2];
+};
+
+template <typename Smem>
+__host__ __device__ constexpr size_t mailbox_offset() {
+    return (sizeof(Smem) + 15) / 16 * 16;
+}
+
 template <int TILE, int SEV, int STAGES, bool SCREEN>
 __global__ void __launch_bounds__(TILE + 32)
 lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict__ ev_count, long long ev_cap,
@@ -321,14 +228,12 @@ lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict_
     ItemMailbox& box = *reinterpret_cast<ItemMailbox*>(smem_raw + mailbox_offset<Smem>());
     constexpr int CONSUMER_WARPS = TILE / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    ReplaySmem<TILE>& rs = *reinterpret_cast<ReplaySmem<TILE>*>(smem_raw + replay_offset<Smem>());
     if (threadIdx.x == 0) {
         for (int q = 0; q < 2; ++q) {
             mbar_init(&box.full[q], 1);
             mbar_init(&box.empty[q], CONSUMER_WARPS);
         }
     }
-    replay_init(rs);
     stream_init(sm, CONSUMER_WARPS);  // thread 0: the stage barriers, then the barrier-init fence
     __syncthreads();
     if (warp == CONSUMER_WARPS) {
@@ -362,7 +267,6 @@ lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict_
         return;
     }
     int k0 = 0;  // the current item's first stage in the ring
-    int replays = 0;
     for (int it = 0;; ++it) {
         const int q = it & 1;
         const bool ok = mbar_wait(&box.full[q], (it >> 1) & 1, &sm.abort, status);
@@ -372,7 +276,7 @@ lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict_
         __syncwarp();
         if (lane == 0) mbar_arrive(&box.empty[q]);
         if (s < 0) return;
-        if (!forward_tile_item<TILE, SEV, STAGES, SCREEN>(sm, rs, replays, k0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out,
+        if (!forward_tile_item<TILE, SEV, STAGES, SCREEN>(sm, k0, s, tile0, E, n_post, k_post, sk, n_spikes, a_out,
                                                          x_out, t_out, z_out, status, pad))
             return;
         k0 += (E + SEV - 1) / SEV;
@@ -561,7 +465,7 @@ template <int TILE, int SEV, int STAGES, bool SCREEN>
 static int launch_forward(const void* events, const int* ev_count, long long ev_cap, const float* wt, int ld, int batch,
                           int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a, float* x,
                           float* times, float* post_exp_tau, int* status, int pad, cudaStream_t stream) {
-    const size_t smem = forward_smem_bytes<TILE, SEV, STAGES>();
+    const size_t smem = sizeof(StreamSmem<TILE, SEV, STAGES>);
     BATS_CUDA((cudaError_t)max_dynamic_smem_set((const void*)lif_fc_forward_kernel<TILE, SEV, STAGES, SCREEN>,
                                                 (int)smem));
     dim3 grid((n_post + TILE - 1) / TILE, batch);
@@ -579,7 +483,8 @@ static int launch_forward_queue(const void* events, const int* ev_count, long lo
                                 int batch, int n_post, int k_post, const SolveConst& sk, int* n_spikes, float* a,
                                 float* x, float* times, float* post_exp_tau, int* status, int pad, int* order,
                                 int* head, cudaStream_t stream) {
-    const size_t smem = forward_smem_bytes<TILE, SEV, STAGES>();
+    using Smem = StreamSmem<TILE, SEV, STAGES>;
+    const size_t smem = mailbox_offset<Smem>() + sizeof(ItemMailbox);
     const void* kern = (const void*)lif_fc_forward_queue_kernel<TILE, SEV, STAGES, SCREEN>;
     BATS_CUDA((cudaError_t)max_dynamic_smem_set(kern, (int)smem));
     int dev = 0, n_sm = 0, per_sm = 0;
