@@ -159,4 +159,5 @@ def test_workspace_queries(lib):
     parts = (16 * 800 * 784 * 4 + 255) // 256 * 256
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == parts + 16 * 13 * 7 * 4
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 1) == 0
-    assert L.bats_pre_errors_workspace_bytes(2, 100, 300) == 2 * 100 * 3 * 2 * 4
+    # one float partial per (event, post tile of 128)
+    assert L.bats_pre_errors_workspace_bytes(2, 100, 300) == 2 * 100 * 3 * 4
