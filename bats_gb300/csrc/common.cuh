@@ -116,6 +116,42 @@ __device__ __forceinline__ bool no_crossing(float a, float b, float e_start, flo
     return usable && (level1 || right_of_window || left_of_window);
 }
 
+// The window constants of one event for no_crossing_at, formed once per stage for all neurons of a tile by
+// the same float operations as no_crossing: Z and (2c) Z of the right-of-window test ((2c) Z = +inf where the
+// test does not apply, Z >= 2980), and Zl and (2c) Zl of the left-of-window test (NaN where it does not apply:
+// every comparison with them is false). no_crossing_at<LEFT>(a, b, event_window(e_start, e_next, k), k) ==
+// no_crossing<false, LEFT>(a, b, e_start, e_next, k) for every a, b.
+struct __align__(16) EventWindow {
+    float Z, tcZ, Zl, tcZl;
+};
+__device__ __forceinline__ EventWindow event_window(float e_start, float e_next, const SolveConst& k) {
+    EventWindow w;
+    w.Z = fminf(e_next, k.e_max) * (1.0f + 0x1.8p-19f);
+    w.tcZ = w.Z < 2980.0f ? (2.0f * k.c) * w.Z : BATS_INF;
+    const float zl = e_start * (1.0f - 0x1p-17f);
+    w.Zl = (zl > 0.0f && zl < 2981.0f) ? zl : __int_as_float(0x7fc00000);
+    w.tcZl = (2.0f * k.c) * w.Zl;
+    return w;
+}
+template <bool LEFT>
+__device__ __forceinline__ bool no_crossing_at(float a, float b, const EventWindow& w, const SolveConst& k) {
+    const float ab = fabsf(b);
+    const bool usable = k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && fabsf(a) <= 0x1p60f;
+    const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), k.c);
+    const float B2 = __fmul_rn(b, b);
+    const bool level1 = a <= 0.0f || b < 0.0f || B2 < p_hi;
+    const float q = fmaf(fmaf(k.c, w.Z, -b), w.Z, a);
+    const float err = 0x1p-21f * fmaf(fmaf(k.c, w.Z, b), w.Z, a);
+    const bool right_of_window = w.tcZ < b * (1.0f - 0x1p-21f) && q > err;
+    bool left_of_window = false;
+    if (LEFT) {
+        const float ql = fmaf(fmaf(k.c, w.Zl, -b), w.Zl, a);
+        const float errl = 0x1p-21f * fmaf(fmaf(k.c, w.Zl, b), w.Zl, a);
+        left_of_window = ql < -errl || (ql > errl && w.tcZl > b * (1.0f + 0x1p-21f));
+    }
+    return usable && (level1 || right_of_window || left_of_window);
+}
+
 // Screen of a run of consecutive events (FC layer, tau = 2 tau_s): true when the reference solver provably
 // accepts no crossing after any event of the run, given the run's states (a_u, b_u) only through
 // amin = min_u a_u and bmax = max_u b_u, and e_first = exp(t/tau) of the run's first event.
@@ -176,6 +212,34 @@ __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t,
         } else {
             tmp = fc_discriminant(__fmul_rn(b, b), a, k.c);  // == (float)((double)fl(b*b) - 4.0*a*c)
         }
+        if (tmp < 0) return false;
+        const float x_tmp = sqrtf(tmp);
+        tmp = x_tmp + b;
+        if (tmp == 0.0f) return false;
+        const float inside_log = 2 * a / tmp;
+        if (inside_log < 0) return false;
+        tmp = k.tau * __logf(inside_log);
+        if (tmp <= last_t || tmp > k.max_sim || tmp > next_t) return false;
+        a_out[n] = a;
+        x_out[n] = x_tmp;
+        t_out[n] = tmp;
+        z_out[n] = inside_log;
+        last_t = tmp;
+        b -= k.dtt * inside_log;
+        n++;
+        if (n >= k_post) return true;
+    }
+}
+
+// solve_crossings<false> with the event's window constants formed once per stage (event_window).
+__device__ __forceinline__ bool solve_crossings_at(float a, float& b, float last_t, float next_t, const EventWindow& w,
+                                                const SolveConst& k, int& n, int k_post,
+                                                float* __restrict__ a_out, float* __restrict__ x_out,
+                                                float* __restrict__ t_out, float* __restrict__ z_out) {
+    while (true) {
+        if (no_crossing_at<true>(a, b, w, k)) return false;
+        float tmp;
+        tmp = fc_discriminant(__fmul_rn(b, b), a, k.c);  // == (float)((double)fl(b*b) - 4.0*a*c)
         if (tmp < 0) return false;
         const float x_tmp = sqrtf(tmp);
         tmp = x_tmp + b;

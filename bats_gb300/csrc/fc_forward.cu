@@ -38,6 +38,8 @@ namespace bats {
 // b of its states, and skips the per-event tests when stage_no_crossing rules out a crossing after any of
 // its events (quiet neurons: one test per stage instead of one per event); otherwise the stage is
 // evaluated as without SCREEN. The FMA sequence is the same either way, so results are bit-identical.
+// Each warp forms the window constants of the stage's events once (event_window, lane u for event u) and every
+// neuron's per-event test reads them (no_crossing_at: the answers of no_crossing, with fewer instructions).
 template <int TILE, int SEV, int STAGES, bool SCREEN = false>
 __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>& sm, int k0, int s, int tile0, int E,
                                                   int n_post, int k_post, const SolveConst& sk,
@@ -57,6 +59,8 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
     float a = 0.0f, b = 0.0f;
     int n = 0;
     bool done = !active;
+    __shared__ EventWindow s_win[TILE / 32][SEV];
+    EventWindow* wv = s_win[warp];
     for (int k = 0; k < n_stages; ++k) {
         const int kg = k0 + k;  // the stage's place in the CTA's ring
         const int slot = kg % STAGES;
@@ -64,6 +68,12 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
         const int m0 = k * SEV;
         const int cnt = min(SEV, E - m0);
         const Event* se = sm.evs[slot];
+        // The window constants of the stage's events, formed once per warp (lane u: event u).
+        if (lane < SEV) {
+            const float e_nx = (m0 + lane + 1 < E) ? se[lane + 1].e : BATS_INF;
+            wv[lane] = event_window(se[lane].e, e_nx, sk);
+        }
+        __syncwarp();
         if (!done) {
             // Pass 1: accumulate the stage's events (the reference's FMA sequence) and mark every event
             // after which a crossing cannot be ruled out. Branch-free, so the per-event tests of the
@@ -95,25 +105,22 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
 #pragma unroll
                 for (int u = 0; u < SEV; ++u) {
                     const float4 e4 = *reinterpret_cast<const float4*>(&se[u]);  // (t, j, es, e)
-                    const float e_nx = se[u + 1].e;
                     const float w = sm.rows[slot][u][tid];
                     aa = fmaf(w, e4.z, aa);
                     bb = fmaf(w, e4.w, bb);
-                    cand |= no_crossing<false, false>(aa, bb, e4.w, e_nx, sk) ? 0u : (1u << u);
+                    cand |= no_crossing_at<false>(aa, bb, wv[u], sk) ? 0u : (1u << u);
                 }
             } else {
 #pragma unroll
                 for (int u = 0; u < SEV; ++u) {
                     const float4 e4 = *reinterpret_cast<const float4*>(&se[u]);
-                    const float e_nx = se[u + 1].e;
                     const float w = sm.rows[slot][u][tid];
                     const bool in = u < cnt;
                     const float a2 = fmaf(w, e4.z, aa);
                     const float b2 = fmaf(w, e4.w, bb);
                     aa = in ? a2 : aa;
                     bb = in ? b2 : bb;
-                    const float e_next = (m0 + u + 1 < E) ? e_nx : BATS_INF;
-                    const bool maybe = !no_crossing<false, false>(aa, bb, e4.w, e_next, sk);
+                    const bool maybe = !no_crossing_at<false>(aa, bb, wv[u], sk);
                     cand |= (in && maybe) ? (1u << u) : 0u;
                 }
             }
@@ -134,10 +141,8 @@ __device__ __forceinline__ bool forward_tile_item(StreamSmem<TILE, SEV, STAGES>&
                     const float wu = sm.rows[slot][u][tid];
                     a = fmaf(wu, e.es, a);
                     b = fmaf(wu, e.e, b);
-                    const bool has_next = m0 + u + 1 < E;
-                    const float t_next = has_next ? se[u + 1].t : BATS_INF;
-                    const float e_next = has_next ? se[u + 1].e : BATS_INF;
-                    done = solve_crossings<false>(a, b, e.t, t_next, e.e, e_next, sk, n, k_post, ao, xo, to, zo);
+                    const float t_next = m0 + u + 1 < E ? se[u + 1].t : BATS_INF;
+                    done = solve_crossings_at(a, b, e.t, t_next, wv[u], sk, n, k_post, ao, xo, to, zo);
                     if (done) break;
                 }
             }

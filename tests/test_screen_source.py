@@ -34,7 +34,8 @@ static const uint3 threadIdx = {0, 0, 0};
 
 // stdin: int32 mode, int64 n, then the fields as float32 arrays of n; stdout: n bytes (0/1).
 // mode 0: no_crossing<FC, left test>(a, b, e_start, e_next; c, e_max); mode 1: the conv form (same fields);
-// mode 2: stage_no_crossing(amin, bmax, amag, a_last, b_last, e_first; c).
+// mode 2: stage_no_crossing(amin, bmax, amag, a_last, b_last, e_first; c); mode 3: whether no_crossing_at with
+// event_window(e_start, e_next) agrees with no_crossing (bit 0: with the left test, bit 1: without).
 int main() {
     int mode;
     long long n;
@@ -52,6 +53,17 @@ int main() {
         k.inv_c = k.c > 0.0f ? 1.0f / k.c : 0.0f;
         k.fast = k.c > 0.0f;
         bool r;
+        if (mode == 3) {
+            // no_crossing_at with the stage's precomputed window against no_crossing, with and without the left
+            // test: 1 | 2 when both agree.
+            const bats::EventWindow w = bats::event_window(v[2 * n + i], v[3 * n + i], k);
+            const bool left = bats::no_crossing_at<true>(v[i], v[n + i], w, k) ==
+                              bats::no_crossing<false, true>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
+            const bool right = bats::no_crossing_at<false>(v[i], v[n + i], w, k) ==
+                               bats::no_crossing<false, false>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
+            out[i] = (left ? 1 : 0) | (right ? 2 : 0);
+            continue;
+        }
         if (mode == 0) r = bats::no_crossing<false>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
         else if (mode == 1) r = bats::no_crossing<true>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
         else r = bats::stage_no_crossing(v[i], v[n + i], v[2 * n + i], v[3 * n + i], v[4 * n + i], v[5 * n + i], k);
@@ -97,6 +109,15 @@ def _run(exe, mode, fields):
     return np.frombuffer(r.stdout, dtype=np.uint8).astype(bool)
 
 
+def _run_raw(exe, mode, fields):
+    n = len(fields[0])
+    payload = (np.int32(mode).tobytes() + np.int64(n).tobytes()
+               + b"".join(np.ascontiguousarray(x, dtype=F).tobytes() for x in fields))
+    r = subprocess.run([exe], input=payload, capture_output=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return np.frombuffer(r.stdout, dtype=np.uint8)
+
+
 def _wild(rng, n):
     """float32 operands of every magnitude and sign, with zeros, subnormals, infinities and NaN mixed in."""
     x = (np.exp(rng.uniform(np.log(1e-44), np.log(3e38), n)) * rng.choice([-1.0, 1.0], n)).astype(F)
@@ -137,6 +158,24 @@ def test_event_screen_model_equals_the_device_source(screen_exe, mode):
     assert want.sum() > 100_000 and (~want).sum() > 100_000
     bad = np.flatnonzero(got != want)
     assert bad.size == 0, [tuple(float(f[i]) for f in fields) for i in bad[:5]]
+
+
+def test_precomputed_window_screen_equals_the_event_screen(screen_exe):
+    """The forward's tile kernels form each event's window constants once per stage (event_window) and test
+    every neuron with no_crossing_at; that must give no_crossing's answer on every input, with and without the
+    left-of-window test, so the kernels' results stay those of the per-event form."""
+    rng = np.random.default_rng(60)
+    parts = [_edge_states(rng, 100_000) for _ in range(10)]
+    fields = [np.concatenate([p[i] for p in parts]) for i in range(6)]
+    n = 1_000_000
+    wild = [_wild(rng, n), _wild(rng, n), np.abs(_wild(rng, n)), np.abs(_wild(rng, n)),
+            np.abs(_wild(rng, n)), np.abs(_wild(rng, n))]
+    fields = [np.concatenate([f, w]) for f, w in zip(fields, wild)]
+    n_all = len(fields[0])
+    payload_ok = _run_raw(screen_exe, 3, fields)
+    assert payload_ok.size == n_all
+    bad = np.flatnonzero(payload_ok != 3)
+    assert bad.size == 0, [(int(payload_ok[i]),) + tuple(float(f[i]) for f in fields) for i in bad[:5]]
 
 
 def test_stage_screen_model_equals_the_device_source(screen_exe):
