@@ -95,7 +95,8 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
                 ce.t = e.t;
                 ce.es = e.es;
                 ce.e = e.e;
-                ce.xyc = xx | (yy << 10) | (cc << 20);
+                // bit 31: an exponential is not finite (the event is relevant to every neuron)
+                ce.xyc = xx | (yy << 10) | (cc << 20) | ((isfinite(e.es) && isfinite(e.e)) ? 0 : (int)0x80000000u);
             }
             const unsigned bal = __ballot_sync(0xffffffffu, keep);
             if (lane == 0) swarp[warp] = __popc(bal);
@@ -116,12 +117,12 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
             const ConvEvent e = sev[m];
             const int dx = (e.xyc & 1023) - xo, dy = ((e.xyc >> 10) & 1023) - yo;
             const bool in_field = dx >= 0 && dx < fx && dy >= 0 && dy < fy;
-            if (!in_field && isfinite(e.es) && isfinite(e.e)) continue;  // weight 0 times a finite value
+            if (!in_field && e.xyc >= 0) continue;  // weight 0 times a finite value
             if (has_prev) {
                 done = solve_crossings<true>(a, b, last_t, e.t, 0.0f, e.e, sk, n, k_post, ao, xo_, to, zo);
                 if (done) break;
             }
-            const float w = in_field ? Wsrc[((co * fx + dx) * fy + dy) * C + (e.xyc >> 20)] : 0.0f;
+            const float w = in_field ? Wsrc[((co * fx + dx) * fy + dy) * C + ((e.xyc >> 20) & 2047)] : 0.0f;
             a += w * e.es;
             b += w * e.e;
             last_t = e.t;
@@ -335,6 +336,8 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
     __shared__ Event sev[32];
     __shared__ float sred[32][33];
     __shared__ int sslot[32];
+    __shared__ int scc[32];
+    const float inv_tau_s = 1.0f / tau_s, inv_tau = 1.0f / tau;  // the error terms' factors, as reciprocals
     const unsigned rank = cluster.block_rank();
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -366,34 +369,48 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
         __syncthreads();
         for (int m0 = beg; m0 < end; m0 += 32) {
             const int cnt = min(32, end - m0);
-            if (tid < cnt) sev[tid] = evs[m0 + tid];
-            __syncthreads();
-            if (tid == 0) {
-                // Slots of the chunk's spikes: j * k_pre + (order of appearance of j in the group).
-                for (int q = 0; q < cnt; ++q) {
-                    const int j = sev[q].j;
-                    const int c = j % C;
-                    sslot[q] = j * k_pre + kcount[c];
-                    ++kcount[c];
+            if (warp == 0) {
+                // Stage the chunk; the spikes' slots: j * k_pre + the order of appearance of j in the group (all
+                // events of a position share x and y, so j is fixed by the channel: earlier chunks' counts plus
+                // the rank among this chunk's events of the same channel).
+                Event e;
+                int c = -1;
+                if (lane < cnt) {
+                    e = evs[m0 + lane];
+                    c = e.j % C;
+                    sev[lane] = e;
+                    scc[lane] = c;
+                }
+                const unsigned peers = __match_any_sync(0xffffffffu, c);
+                const int rank = __popc(peers & lanemask_lt());
+                int base = 0;
+                if (lane < cnt) base = kcount[c];
+                __syncwarp();
+                if (lane < cnt) {
+                    sslot[lane] = e.j * k_pre + base + rank;
+                    if (rank == __popc(peers) - 1) kcount[c] = base + __popc(peers);
                 }
             }
-            for (int q = 0; q < cnt; ++q) {
-                const Event e = sev[q];
-                float term = 0.0f;
-                if (in) {
+            __syncthreads();
+            float term[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) {
+                term[q] = 0.0f;
+                if (q < cnt && in) {
+                    const Event e = sev[q];
                     cur.advance_past(e.t);
                     if (cur.valid()) {
-                        const int cc = e.j % C;
+                        const int cc = scc[q];
                         Gs[tp * C + cc] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
                         if (pre_err)
-                            term = W[(long long)tp * C + cc] * (cur.AB.x * e.es / tau_s - cur.AB.y * e.e / tau);
+                            term[q] = W[(long long)tp * C + cc] * (cur.AB.x * e.es * inv_tau_s - cur.AB.y * e.e * inv_tau);
                     }
                 }
-                if (pre_err) {
-#pragma unroll
-                    for (int o = 16; o >= 1; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
-                    if (lane == 0) sred[q][warp] = term;
-                }
+            }
+            if (pre_err) {
+                // The chunk's 32 error terms summed over the warp at once (lane q: event q), then over the warps.
+                const float v = warp_transpose_reduce<32>(term);
+                sred[lane][warp] = v;
             }
             __syncthreads();
             if (pre_err && tid < cnt) {
