@@ -377,11 +377,17 @@ def run_ours(args, dist, rank, world):
 
 
 def profile_one_step(workload):
-    """One eager train step inside an NVTX range "step", with a nested range per launch (L1.sort, L1.forward,
-    ...), after set-up, autotuning and 3 warm-up steps, for targeted ncu captures:
+    """One eager train step (literal, active, batching or conv workload) inside an NVTX range "step", with a
+    nested range per launch (L1.sort, L1.forward, ...), after set-up, autotuning and 3 warm-up steps, for
+    targeted ncu captures:
     ncu --nvtx --nvtx-include "step/" (the step's launch list) or --nvtx-include "step/L2.forward/"."""
     import torch
-    if workload == "batching":
+    if workload == "conv":
+        step, layers, (t, n, labels) = conv_network()
+        del step, layers
+        torch.cuda.empty_cache()
+        ts = conv_train_step(t, labels)
+    elif workload == "batching":
         from bats_gb300.train import FCLayerSpec, FCTrainStep
         t, labels, _ = batching_inputs()
         ws_np, ths = batching_weights()
@@ -392,7 +398,8 @@ def profile_one_step(workload):
         ts.set_inputs(torch.tensor(t), torch.tensor(labels))
     else:
         ts = build_train_step(workload)
-    ts.autotune()
+    if hasattr(ts, "autotune"):
+        ts.autotune()
     for _ in range(3):
         ts.step()
     flush = torch.zeros(128 * 1024 * 1024, dtype=torch.float32, device="cuda")
