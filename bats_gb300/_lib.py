@@ -59,16 +59,17 @@ SIGNATURES = {
     "bats_pool_forward": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_vp, c_vp, c_vp, c_vp]),
     "bats_backward_prep": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                    c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "bats_cursor_heads_bytes": (c_size, [c_int, c_int]),
     "bats_backward_prep_counted": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float,
-                                           c_float, c_vp, c_vp, c_vp]),
+                                           c_float, c_vp, c_vp, c_vp, c_vp]),
     "bats_backward_prep_layer": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_float,
                                          c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_weights_gradient_workspace_bytes": (c_size, [c_int, c_int, c_int, c_int]),
-    "bats_weights_gradient": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
-                                      c_int, c_int, c_vp, c_vp, c_size, c_vp]),
-    "bats_weights_gradient_adam": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
-                                           c_int, c_vp, c_vp, c_vp, c_float, c_float, c_float, c_float, c_vp, c_vp,
-                                           c_vp, c_int, c_vp, c_size, c_vp]),
+    "bats_weights_gradient": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int,
+                                      c_int, c_int, c_int, c_vp, c_vp, c_size, c_vp]),
+    "bats_weights_gradient_adam": (c_int, [c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_vp, c_int, c_int, c_int,
+                                           c_int, c_int, c_vp, c_vp, c_vp, c_float, c_float, c_float, c_float, c_vp,
+                                           c_vp, c_vp, c_int, c_vp, c_size, c_vp]),
     "bats_weights_gradient_noalloc_capacity": (c_ll, []),
     "bats_weights_gradient_mean_noalloc": (c_int, [c_vp, c_vp, c_ll, c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int,
                                                    c_int, c_vp, c_vp]),
@@ -141,7 +142,7 @@ class BatsFcTrainLayer(ctypes.Structure):
     """struct BatsFcTrainLayer of include/bats_gb300.h (one layer of bats_fc_train_step)."""
     _fields_ = [("fwd", BatsFcLayer), ("weights", c_vp), ("adam_m", c_vp), ("adam_v", c_vp), ("grad", c_vp),
                 ("events_bucketed", c_vp), ("bucket_offsets", c_vp), ("tables", c_vp), ("nvalid", c_vp),
-                ("f1", c_vp), ("f2", c_vp), ("pre_errors", c_vp), ("grad_group", c_int)]
+                ("cursor_heads", c_vp), ("f1", c_vp), ("f2", c_vp), ("pre_errors", c_vp), ("grad_group", c_int)]
 
 
 def call(name: str, *args):

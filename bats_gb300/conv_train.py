@@ -111,7 +111,8 @@ class ConvTrainStep:
                          out=(torch.empty((B, N), dtype=i32, device=dev),
                               *(torch.empty((B, N, Kp), dtype=f32, device=dev) for _ in range(4))),
                          tables=torch.empty((B, N, Kp + 1, 2), dtype=f32, device=dev),
-                         nvalid=torch.empty((B, N), dtype=i32, device=dev))
+                         nvalid=torch.empty((B, N), dtype=i32, device=dev),
+                         heads=K.alloc_cursor_heads(B, N, dev) if d["kind"] == "fc" else None)
                 assert Kp <= 32, "the train step's counted backward prep handles at most 32 spikes per neuron"
                 k_prev = Kp
             # Errors of this layer's input spikes (the incoming errors of the layer below); none for the first.
@@ -198,7 +199,7 @@ class ConvTrainStep:
             L.append((f"{tag}.prep", lambda s, d=d, e=errors: call(
                 "bats_backward_prep_counted", ptr(d["out"][3]), ptr(d["out"][0]), ptr(d["out"][1]), ptr(d["out"][2]),
                 ptr(d["out"][4]), ptr(e), B, d["n"], d["k"], float(d["c"]), float(d["tau32"]), float(d["dtt"]),
-                ptr(d["tables"]), ptr(d["nvalid"]), s)))
+                ptr(d["tables"]), ptr(d["nvalid"]), ptr(d["heads"]), s)))
             ev = d["ev"]
             if d["kind"] == "conv":
                 X, Y, C = d["in_shape"]
@@ -218,8 +219,9 @@ class ConvTrainStep:
                         ev.n_neurons, ev.k, tau_s, float(d["tau32"]), ptr(pe), ws, wsb, s)))
                 L.append((f"{tag}.grad_adam", lambda s, d=d, ev=ev: call(
                     "bats_weights_gradient_adam", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed),
-                    ptr(ev.bucket_offsets), ev.cap, ptr(d["out"][3]), ptr(d["tables"]), ptr(d["nvalid"]), B, d["n"],
-                    d["k"], ev.n_neurons, d["group"], ptr(d["grad"]), ptr(d["m"]), ptr(d["v"]), float(self.b1),
+                    ptr(ev.bucket_offsets), ev.cap, ptr(d["out"][3]), ptr(d["tables"]), ptr(d["nvalid"]),
+                    ptr(d["heads"]), B, d["n"], d["k"], ev.n_neurons, d["group"], ptr(d["grad"]), ptr(d["m"]),
+                    ptr(d["v"]), float(self.b1),
                     float(self.b2), float(self.eps), float(self.lr), ptr(self.powers), ptr(d["W"]), ptr(d["Wt"]),
                     d["Wt"].shape[1], ws, wsb, s)))
             if pe is not None:

@@ -279,6 +279,18 @@ struct PostCursor {
         tn1 = n > 1 ? tp[1] : BATS_INF;
         AB1 = n > 1 ? tb[1] : make_float2(0.0f, 0.0f);
     }
+    // The same state as init() from the neuron's cursor head (first two spike times, first two table entries;
+    // +inf and zeros past n), which the backward prep writes for every (sample, neuron) in one coalesced array.
+    __device__ __forceinline__ void init_head(const float* tp_, const float2* tb_, int n_, float2 ht, float4 hab) {
+        tp = tp_;
+        tb = tb_;
+        n = n_;
+        p = 0;
+        tn = ht.x;
+        tn1 = ht.y;
+        AB = make_float2(hab.x, hab.y);
+        AB1 = make_float2(hab.z, hab.w);
+    }
     __device__ __forceinline__ void advance_past(float t) {
         while (tn <= t) {
             ++p;

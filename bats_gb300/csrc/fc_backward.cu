@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(PREPC_WARPS * 32)
 bwd_prep_counted_kernel(const float* __restrict__ t, const int* __restrict__ n_spikes, const float* __restrict__ a,
                         const float* __restrict__ x, const float* __restrict__ z, float* __restrict__ err,
                         long long total, int K, float c, float tau, float dtt, float2* __restrict__ tab,
-                        int* __restrict__ nvalid) {
+                        int* __restrict__ nvalid, float2* __restrict__ head_t, float4* __restrict__ head_ab) {
     pdl_prologue();
     __shared__ PrepCompact sm_all[PREPC_WARPS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -281,6 +281,7 @@ bwd_prep_counted_kernel(const float* __restrict__ t, const int* __restrict__ n_s
         cp_async_wait_all();
         __syncwarp();
         int n = 0;
+        float h_t0 = BATS_INF, h_t1 = BATS_INF;  // the cursor head's spike times (read before the tables overwrite them)
         if (mine) {
             float* rt = sm.t + off;
             float* rz = sm.z + off;
@@ -293,6 +294,8 @@ bwd_prep_counted_kernel(const float* __restrict__ t, const int* __restrict__ n_s
                     n = k;
                     break;
                 }
+            h_t0 = n > 0 ? rt[0] : BATS_INF;
+            h_t1 = n > 1 ? rt[1] : BATS_INF;
             float cum = 0.0f;
             for (int k = n - 1; k >= 0; --k) {
                 const float ek = re[k] + cum * rz[k];
@@ -325,7 +328,17 @@ bwd_prep_counted_kernel(const float* __restrict__ t, const int* __restrict__ n_s
                 }
             }
         }
-        if (mine && lane < cnt) nvalid[nb + lane] = n;
+        if (mine && lane < cnt) {
+            nvalid[nb + lane] = n;
+            if (head_t) {
+                // Cursor head: what PostCursor::init reads from this row, in one coalesced record per pair.
+                const float* ra = sm.t + off;
+                const float* rb = sm.x + off;
+                head_t[nb + lane] = make_float2(h_t0, h_t1);
+                head_ab[nb + lane] = make_float4(n > 0 ? ra[0] : 0.0f, n > 0 ? rb[0] : 0.0f, n > 1 ? ra[1] : 0.0f,
+                                                 n > 1 ? rb[1] : 0.0f);
+            }
+        }
         __syncwarp();
         for (int q0 = 0; q0 < V; q0 += 32) {
             const int q = q0 + lane;
@@ -414,7 +427,7 @@ __global__ void __launch_bounds__(TILE)
 bwd_grad_warp_kernel(const Event* __restrict__ ev_b, const int* __restrict__ boff, int n_buckets, long long ev_cap,
                      const float* __restrict__ post_t, const float2* __restrict__ tab, const int* __restrict__ nvalid,
                      int n_post, int k_post, int n_pre, int batch, int group, float* __restrict__ out,
-                     int* __restrict__ flags) {
+                     int* __restrict__ flags, const float2* __restrict__ head_t, const float4* __restrict__ head_ab) {
     pdl_prologue();
     constexpr int WARPS = TILE / 32;
     __shared__ float G[JC][TILE + 1];
@@ -456,16 +469,21 @@ bwd_grad_warp_kernel(const Event* __restrict__ ev_b, const int* __restrict__ bof
             const long long pn = (long long)s * n_post + (active ? i : 0);
             const int n = active ? nvalid[pn] : 0;
             PostCursor cur;
-            cur.init(post_t + pn * k_post, tab + pn * (k_post + 1), n);
+            if (head_t)
+                cur.init_head(post_t + pn * k_post, tab + pn * (k_post + 1), n, head_t[pn], head_ab[pn]);
+            else
+                cur.init(post_t + pn * k_post, tab + pn * (k_post + 1), n);
             const Event* evs = ev_b + (long long)s * ev_cap;
             for (int m0 = beg; m0 < end; m0 += 32) {
                 const int cnt = min(32, end - m0);
                 __syncwarp();
                 if (lane < cnt) wev[lane] = evs[m0 + lane];
                 __syncwarp();
-                if (n > 0) {
-                    // Four events at a time, as in bwd_grad_bucketed_kernel: terms in event order, the four
-                    // shared-memory updates issued with all loads first when the four pre neurons differ.
+                {
+                    // Four events at a time: terms in event order, the four shared-memory updates issued with all
+                    // loads first when the four pre neurons differ. Lanes of silent neurons and lanes past their
+                    // neuron's last spike add 0, which leaves every entry unchanged (an entry starts at +0 and a
+                    // sum is -0 only when both addends are), so the adds need no predicate.
                     int m = 0;
                     for (; m + 4 <= cnt; m += 4) {
                         float v[4];
@@ -484,12 +502,10 @@ bwd_grad_warp_kernel(const Event* __restrict__ ev_b, const int* __restrict__ bof
 #pragma unroll
                             for (int u = 0; u < 4; ++u) gg[u] = G[jj[u]][tid];
 #pragma unroll
-                            for (int u = 0; u < 4; ++u)
-                                if (v[u] != 0.0f) G[jj[u]][tid] = gg[u] + v[u];
+                            for (int u = 0; u < 4; ++u) G[jj[u]][tid] = gg[u] + v[u];
                         } else {
 #pragma unroll
-                            for (int u = 0; u < 4; ++u)
-                                if (v[u] != 0.0f) G[jj[u]][tid] += v[u];
+                            for (int u = 0; u < 4; ++u) G[jj[u]][tid] += v[u];
                         }
                     }
                     for (; m < cnt; ++m) {
@@ -816,7 +832,7 @@ __global__ void pre_err_scatter_kernel(const float* __restrict__ partial, const 
 // ---------------------------------------------------------------------------------------------
 // C-ABI
 constexpr int GRAD_TILE = 128;
-constexpr int GRAD_JC = 64;
+constexpr int GRAD_JC = BATS_GRAD_BUCKET_WIDTH;  // 16.5 KB gradient tile: 12 CTAs of 128 threads per SM
 
 extern "C" int bats_backward_prep(const float* post_times, const float* a, const float* x, const float* post_exp_tau,
                                   float* errors, int batch, int n_post, int k_post, float c, float tau,
@@ -864,11 +880,30 @@ extern "C" int bats_backward_prep_layer(const float* post_times, const float* a,
     return BATS_OK;
 }
 
+// Cursor heads of `pairs` (sample, neuron) pairs: the first two spike times (float2 per pair), then, from the
+// next 16-byte boundary, the first two suffix-table entries (float4 per pair).
+struct CursorHeads {
+    float2* t;
+    float4* ab;
+};
+static size_t heads_times_bytes(long long pairs) { return ((size_t)pairs * sizeof(float2) + 15) & ~(size_t)15; }
+static CursorHeads cursor_heads_of(const void* base, long long pairs) {
+    if (!base) return {nullptr, nullptr};
+    char* b = static_cast<char*>(const_cast<void*>(base));
+    return {reinterpret_cast<float2*>(b), reinterpret_cast<float4*>(b + heads_times_bytes(pairs))};
+}
+extern "C" size_t bats_cursor_heads_bytes(int batch, int n_post) {
+    const long long pairs = (long long)std::max(batch, 0) * std::max(n_post, 0);
+    return heads_times_bytes(pairs) + (size_t)pairs * sizeof(float4);
+}
+
 extern "C" int bats_backward_prep_counted(const float* post_times, const int* n_spikes, const float* a, const float* x,
                                           const float* post_exp_tau, float* errors, int batch, int n_post, int k_post,
                                           float c, float tau, float delta_theta_tau, void* tables, int* nvalid,
-                                          cudaStream_t stream) {
+                                          void* cursor_heads, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && k_post > 0, BATS_ERR_BAD_SHAPE, "backward_prep_counted: bad shape");
+    BATS_REQUIRE(((uintptr_t)cursor_heads & 15) == 0, BATS_ERR_BAD_SHAPE,
+                 "backward_prep_counted: cursor_heads not 16-byte aligned");
     BATS_REQUIRE(k_post <= 32, BATS_ERR_BAD_SHAPE, "backward_prep_counted: k_post > 32 (use bats_backward_prep_layer)");
     const long long total = (long long)batch * n_post;
     if (total == 0) return BATS_OK;
@@ -876,9 +911,10 @@ extern "C" int bats_backward_prep_counted(const float* post_times, const int* n_
                  "backward_prep_counted: null pointer");
     const long long warps = (total + 31) / 32;
     const int blocks = (int)((warps + bats::PREPC_WARPS - 1) / bats::PREPC_WARPS);
+    const CursorHeads h = cursor_heads_of(cursor_heads, total);
     BATS_CUDA(bats::launch(bats::bwd_prep_counted_kernel, blocks, bats::PREPC_WARPS * 32, 0, stream, post_times,
         n_spikes, a, x, post_exp_tau, errors, total, k_post, c, tau, delta_theta_tau, reinterpret_cast<float2*>(tables),
-        nvalid));
+        nvalid, h.t, h.ab));
     BATS_CUDA(cudaGetLastError());
     return BATS_OK;
 }
@@ -912,14 +948,15 @@ extern "C" size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, i
 template <int TILE>
 static cudaError_t launch_grad(const void* events, const int* ev_count, const void* ev_b, const int* boff,
                                int n_buckets, long long ev_cap, const float* post_times, const void* tables,
-                               const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, int groups,
-                               float* out, int* flags, cudaStream_t stream) {
+                               const int* nvalid, const void* heads, int batch, int n_post, int k_post, int n_pre,
+                               int group, int groups, float* out, int* flags, cudaStream_t stream) {
     dim3 grid((n_post + TILE - 1) / TILE, (n_pre + GRAD_JC - 1) / GRAD_JC, groups);
+    const CursorHeads h = cursor_heads_of(heads, (long long)batch * n_post);
     if (ev_b)
         return bats::launch(bats::bwd_grad_warp_kernel<TILE, GRAD_JC>, grid, TILE, 0, stream,
                             reinterpret_cast<const bats::Event*>(ev_b), boff, n_buckets, ev_cap, post_times,
                             reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out,
-                            flags);
+                            flags, (const float2*)h.t, (const float4*)h.ab);
     return bats::launch(bats::bwd_grad_kernel<TILE, GRAD_JC>, grid, TILE, 0, stream,
                         reinterpret_cast<const bats::Event*>(events), ev_count, ev_cap, post_times,
                         reinterpret_cast<const float2*>(tables), nvalid, n_post, k_post, n_pre, batch, group, out);
@@ -927,11 +964,13 @@ static cudaError_t launch_grad(const void* events, const int* ev_count, const vo
 
 extern "C" int bats_weights_gradient(const void* events, const int* ev_count, const void* events_bucketed,
                                      const int* bucket_offsets, long long ev_cap, const float* post_times,
-                                     const void* tables, const int* nvalid, int batch, int n_post, int k_post,
-                                     int n_pre, int group, int mean, float* grad, void* workspace,
+                                     const void* tables, const int* nvalid, const void* cursor_heads, int batch,
+                                     int n_post, int k_post, int n_pre, int group, int mean, float* grad, void* workspace,
                                      size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 1, BATS_ERR_BAD_SHAPE,
                  "weights_gradient: bad shape");
+    BATS_REQUIRE(((uintptr_t)cursor_heads & 15) == 0, BATS_ERR_BAD_SHAPE,
+                 "weights_gradient: cursor_heads not 16-byte aligned");
     if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
     BATS_REQUIRE(post_times && tables && nvalid && grad &&
                      ((events && ev_count) || (events_bucketed && bucket_offsets)),
@@ -952,13 +991,16 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
     const int tile = grad_tile_for(n_post);
     if (tile == 32)
         BATS_CUDA(launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
-                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+                                  tables, nvalid, cursor_heads, batch, n_post, k_post, n_pre, group, groups, part,
+                                  flags, stream));
     else if (tile == 64)
         BATS_CUDA(launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
-                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+                                  tables, nvalid, cursor_heads, batch, n_post, k_post, n_pre, group, groups, part,
+                                  flags, stream));
     else
         BATS_CUDA(launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
-                                   tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+                                   tables, nvalid, cursor_heads, batch, n_post, k_post, n_pre, group, groups, part,
+                                   flags, stream));
     if (group == 1) return BATS_OK;  // per-sample gradient (B, N_post, N_pre)
     BATS_CUDA(launch_reduce(part, n_post, n_pre, groups, mean ? (float)batch : 1.0f, grad, flags, tile,
                             (n_post + tile - 1) / tile, n_buckets, stream));
@@ -967,13 +1009,16 @@ extern "C" int bats_weights_gradient(const void* events, const int* ev_count, co
 
 extern "C" int bats_weights_gradient_adam(const void* events, const int* ev_count, const void* events_bucketed,
                                           const int* bucket_offsets, long long ev_cap, const float* post_times,
-                                          const void* tables, const int* nvalid, int batch, int n_post, int k_post,
-                                          int n_pre, int group, float* grad, float* m, float* v, float beta_1,
+                                          const void* tables, const int* nvalid, const void* cursor_heads, int batch,
+                                          int n_post, int k_post, int n_pre, int group, float* grad, float* m, float* v,
+                                          float beta_1,
                                           float beta_2, float epsilon, float learning_rate, const double* powers,
                                           float* weights, float* weights_t, int ld, void* workspace,
                                           size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_post >= 0 && n_pre >= 0 && k_post > 0 && group >= 2 && ld >= n_post,
                  BATS_ERR_BAD_SHAPE, "weights_gradient_adam: bad shape (group >= 2, ld >= n_post)");
+    BATS_REQUIRE(((uintptr_t)cursor_heads & 15) == 0, BATS_ERR_BAD_SHAPE,
+                 "weights_gradient_adam: cursor_heads not 16-byte aligned");
     if (batch == 0 || n_post == 0 || n_pre == 0) return BATS_OK;
     BATS_REQUIRE(post_times && tables && nvalid && m && v && powers && weights && weights_t &&
                      ((events && ev_count) || (events_bucketed && bucket_offsets)),
@@ -996,13 +1041,16 @@ extern "C" int bats_weights_gradient_adam(const void* events, const int* ev_coun
     const int tile = grad_tile_for(n_post);
     if (tile == 32)
         BATS_CUDA(launch_grad<32>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
-                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+                                  tables, nvalid, cursor_heads, batch, n_post, k_post, n_pre, group, groups, part,
+                                  flags, stream));
     else if (tile == 64)
         BATS_CUDA(launch_grad<64>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
-                                  tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+                                  tables, nvalid, cursor_heads, batch, n_post, k_post, n_pre, group, groups, part,
+                                  flags, stream));
     else
         BATS_CUDA(launch_grad<128>(events, ev_count, events_bucketed, bucket_offsets, n_buckets, ev_cap, post_times,
-                                   tables, nvalid, batch, n_post, k_post, n_pre, group, groups, part, flags, stream));
+                                   tables, nvalid, cursor_heads, batch, n_post, k_post, n_pre, group, groups, part,
+                                   flags, stream));
     dim3 grid((n_pre + 31) / 32, (n_post + 31) / 32), block(32, 8);
     if (grad && groups > 1 && (long long)grid.x * grid.y < 2 * 152) {
         // Few weight tiles (a narrow layer) for many partials: the tile grid would leave most SMs idle while

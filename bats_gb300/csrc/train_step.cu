@@ -10,7 +10,7 @@
 
 namespace {
 
-constexpr int TRAIN_BUCKET_WIDTH = 64;  // pre-neuron buckets of the gradient kernel (its GRAD_JC)
+constexpr int TRAIN_BUCKET_WIDTH = BATS_GRAD_BUCKET_WIDTH;  // pre-neuron buckets of the gradient kernel (its GRAD_JC)
 
 bool is_queue(int algo) {
     const int base = algo & ~(BATS_FWD_NO_PAD | BATS_FWD_STAGE_SCREEN);
@@ -103,9 +103,12 @@ extern "C" int bats_fc_train_step(const float* in_times, const int* labels, int 
     for (int l = n_layers - 1; l >= 0; --l) {
         const BatsFcTrainLayer& L = layers[l];
         const BatsFcLayer& F = L.fwd;
+        // The cursor heads (optional) come from the counted prep only.
+        const void* heads = F.k_post <= 32 ? L.cursor_heads : nullptr;
         if (F.k_post <= 32)
             rc = bats_backward_prep_counted(F.times, F.n_spikes, F.a, F.x, F.post_exp_tau, err, batch, F.n_post,
-                                            F.k_post, F.c, F.tau, F.delta_theta_tau, L.tables, L.nvalid, stream);
+                                            F.k_post, F.c, F.tau, F.delta_theta_tau, L.tables, L.nvalid,
+                                            L.cursor_heads, stream);
         else
             rc = bats_backward_prep_layer(F.times, F.a, F.x, F.post_exp_tau, err, batch, F.n_post, F.k_post, F.c,
                                           F.tau, F.delta_theta_tau, L.f1, L.f2, L.tables, L.nvalid, stream);
@@ -118,7 +121,8 @@ extern "C" int bats_fc_train_step(const float* in_times, const int* labels, int 
             if (rc != BATS_OK) return rc;
         }
         rc = bats_weights_gradient_adam(F.events, F.ev_count, L.events_bucketed, L.bucket_offsets, cap, F.times,
-                                        L.tables, L.nvalid, batch, F.n_post, F.k_post, F.n_pre, L.grad_group, L.grad,
+                                        L.tables, L.nvalid, heads, batch, F.n_post, F.k_post, F.n_pre, L.grad_group,
+                                        L.grad,
                                         L.adam_m, L.adam_v, beta_1, beta_2, epsilon, learning_rate, powers, L.weights,
                                         const_cast<float*>(F.weights_t), F.ld, workspace, workspace_bytes, stream);
         if (rc != BATS_OK) return rc;

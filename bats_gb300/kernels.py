@@ -64,7 +64,7 @@ def transpose_weights(weights, out=None):
     return out
 
 
-BUCKET_WIDTH = 64  # pre neurons per bucket of the weight-gradient kernel
+BUCKET_WIDTH = 32  # pre neurons per bucket of the weight-gradient kernel
 
 
 @dataclass
@@ -80,7 +80,7 @@ class Events:
     k: int
     bucketed: torch.Tensor | None = None
     bucket_offsets: torch.Tensor | None = None
-    bucket_width: int = 64
+    bucket_width: int = BUCKET_WIDTH
 
     @property
     def cap(self) -> int:
@@ -305,6 +305,13 @@ class BackwardTables:
     f2: torch.Tensor
     tables: torch.Tensor  # (B, N, K+1, 2)
     nvalid: torch.Tensor  # (B, N)
+    heads: torch.Tensor | None = None  # cursor heads (bats_cursor_heads_bytes), written by the counted prep
+
+
+def alloc_cursor_heads(batch: int, n_post: int, device="cuda") -> torch.Tensor:
+    """Buffer for the cursor heads of bats_backward_prep_counted / bats_weights_gradient (uint8, 16-byte
+    aligned as torch allocations are)."""
+    return torch.empty(max(1, call_size("bats_cursor_heads_bytes", batch, n_post)), dtype=torch.uint8, device=device)
 
 
 def backward_prep(post_times, a, x, post_exp_tau, errors, c: float, tau: float, delta_theta_tau: float,
@@ -317,15 +324,19 @@ def backward_prep(post_times, a, x, post_exp_tau, errors, c: float, tau: float, 
     B, N, K = post_times.shape
     dev = post_times.device
     need_f = want_factors or K > 32 or not recurrent
+    counted = recurrent and n_spikes is not None and not need_f
     if out is None:
         out = BackwardTables(torch.empty((B, N, K), dtype=F32, device=dev) if need_f else None,
                              torch.empty((B, N, K), dtype=F32, device=dev) if need_f else None,
                              torch.empty((B, N, K + 1, 2), dtype=F32, device=dev),
-                             torch.empty((B, N), dtype=I32, device=dev))
-    if recurrent and n_spikes is not None and not need_f:
+                             torch.empty((B, N), dtype=I32, device=dev),
+                             alloc_cursor_heads(B, N, dev) if counted else None)
+    if not counted:
+        out.heads = None  # only the counted prep writes the cursor heads
+    if counted:
         call("bats_backward_prep_counted", ptr(post_times), ptr(_c(n_spikes, I32)), ptr(a), ptr(x),
              ptr(post_exp_tau), ptr(errors), B, N, K, float(c), float(tau), float(delta_theta_tau),
-             ptr(out.tables), ptr(out.nvalid), stream_ptr())
+             ptr(out.tables), ptr(out.nvalid), ptr(out.heads), stream_ptr())
     elif recurrent:
         call("bats_backward_prep_layer", ptr(post_times), ptr(a), ptr(x), ptr(post_exp_tau), ptr(errors), B, N, K,
              float(c), float(tau), float(delta_theta_tau), ptr(out.f1), ptr(out.f2), ptr(out.tables),
@@ -390,7 +401,7 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
     by_bucket = events.bucketed is not None and events.bucket_width == BUCKET_WIDTH
     call("bats_weights_gradient", ptr(events.events), ptr(events.counts), ptr(events.bucketed if by_bucket else None),
          ptr(events.bucket_offsets if by_bucket else None), events.cap, ptr(post_times), ptr(tabs.tables),
-         ptr(tabs.nvalid), B, n_post,
+         ptr(tabs.nvalid), ptr(tabs.heads), B, n_post,
          k_post, n_pre, g, int(reduce == "mean"), ptr(out), ptr(ws), ws_bytes, stream_ptr())
     return out
 

@@ -66,7 +66,8 @@ class FCTrainStep:
             self.tabs.append(K.BackwardTables(torch.empty((B, N, Kp), dtype=f32, device=dev) if need_f else None,
                                               torch.empty((B, N, Kp), dtype=f32, device=dev) if need_f else None,
                                               torch.empty((B, N, Kp + 1, 2), dtype=f32, device=dev),
-                                              torch.empty((B, N), dtype=i32, device=dev)))
+                                              torch.empty((B, N), dtype=i32, device=dev),
+                                              K.alloc_cursor_heads(B, N, dev) if not need_f else None))
             self.grad.append(torch.empty((N, n_prev), dtype=f32, device=dev))
             self.pre_err.append(torch.empty((B, n_prev, k_prev), dtype=f32, device=dev))
             n_prev, k_prev = N, Kp
@@ -151,7 +152,7 @@ class FCTrainStep:
                 L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt,
                           tb=tb: call("bats_backward_prep_counted", ptr(o[3]), ptr(o[0]), ptr(o[1]), ptr(o[2]),
                                       ptr(o[4]), ptr(e), B, spec.n_neurons, spec.max_n_spike, float(c),
-                                      float(tau32), float(dtt), ptr(tb.tables), ptr(tb.nvalid), s)))
+                                      float(tau32), float(dtt), ptr(tb.tables), ptr(tb.nvalid), ptr(tb.heads), s)))
             else:
                 L.append((f"{tag}.prep", lambda s, o=self.out[li], e=errors, spec=spec, c=c, tau32=tau32, dtt=dtt,
                           tb=tb: call("bats_backward_prep_layer", ptr(o[3]), ptr(o[1]), ptr(o[2]), ptr(o[4]),
@@ -167,8 +168,8 @@ class FCTrainStep:
                 errors = pe
             L.append((f"{tag}.grad_adam", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
                 "bats_weights_gradient_adam", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed),
-                ptr(ev.bucket_offsets), ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), B, spec.n_neurons,
-                spec.max_n_spike, ev.n_neurons, self.groups[li], ptr(self.grad[li]), ptr(self.m[li]),
+                ptr(ev.bucket_offsets), ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), ptr(tb.heads), B,
+                spec.n_neurons, spec.max_n_spike, ev.n_neurons, self.groups[li], ptr(self.grad[li]), ptr(self.m[li]),
                 ptr(self.v[li]), float(self.b1), float(self.b2), float(self.eps), float(self.lr), ptr(self.powers),
                 ptr(self.W[li]), ptr(self.Wt[li]), self.Wt[li].shape[1], ws, wsb, s)))
         return L
@@ -191,7 +192,8 @@ class FCTrainStep:
                               ptr(ev.counts), ptr(n), ptr(a), ptr(x), ptr(t), ptr(z))
             arr[li] = BatsFcTrainLayer(fwd, ptr(self.W[li]), ptr(self.m[li]), ptr(self.v[li]), ptr(self.grad[li]),
                                        ptr(ev.bucketed), ptr(ev.bucket_offsets), ptr(tb.tables), ptr(tb.nvalid),
-                                       ptr(tb.f1), ptr(tb.f2), ptr(self.pre_err[li]) if li > 0 else None,
+                                       ptr(tb.heads), ptr(tb.f1), ptr(tb.f2),
+                                       ptr(self.pre_err[li]) if li > 0 else None,
                                        int(self.groups[li]))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
         return arr
@@ -216,8 +218,8 @@ class FCTrainStep:
         spec, ev = self.specs[li], self.ev[li]
         t, tb = self.out[li][3], self.tabs[li]
         call("bats_weights_gradient", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets),
-             ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), self.B, spec.n_neurons, spec.max_n_spike, ev.n_neurons,
-             group, 1, ptr(self.grad[li]), ptr(self.ws), self.ws.numel(), s)
+             ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), ptr(tb.heads), self.B, spec.n_neurons,
+             spec.max_n_spike, ev.n_neurons, group, 1, ptr(self.grad[li]), ptr(self.ws), self.ws.numel(), s)
 
     @property
     def launches_per_step(self) -> int:

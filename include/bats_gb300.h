@@ -30,6 +30,8 @@ extern "C" {
 #endif
 
 #define BATS_ABI_VERSION 1
+/* Pre neurons per bucket of the bucketed events that bats_weights_gradient(_adam) and the train step read. */
+#define BATS_GRAD_BUCKET_WIDTH 32
 
 #define BATS_OK 0
 #define BATS_ERR_BAD_SHAPE 1
@@ -203,22 +205,31 @@ int bats_backward_prep_layer(const float* post_times, const float* a, const floa
  * errors, tables and nvalid are identical to bats_backward_prep_layer's (nvalid = the first +inf time below
  * the count, or the count). No f1/f2 output; k_post <= 32. Replaces propagate_recurrent_errors and
  * compute_factors (bats/CudaKernels/Wrappers/Backpropagation/propagate_recurrent_errors.py:9-16,
- * compute_factors.py:11-22), which the reference runs over all N_post * K slots. */
+ * compute_factors.py:11-22), which the reference runs over all N_post * K slots.
+ * cursor_heads (optional, NULL to skip; 16-byte aligned, bats_cursor_heads_bytes(batch, n_post) bytes):
+ * per (sample, neuron) the first two spike times and the first two table entries in one coalesced array,
+ * which the weight gradient reads instead of the start of each table row (same results, fewer memory
+ * sectors). No counterpart in the reference. */
+size_t bats_cursor_heads_bytes(int batch, int n_post);
 int bats_backward_prep_counted(const float* post_times, const int* n_spikes, const float* a, const float* x,
                                const float* post_exp_tau, float* errors, int batch, int n_post, int k_post, float c,
-                               float tau, float delta_theta_tau, void* tables, int* nvalid, cudaStream_t stream);
+                               float tau, float delta_theta_tau, void* tables, int* nvalid, void* cursor_heads,
+                               cudaStream_t stream);
 
 /* Weight gradient of a fully-connected layer. group == 1: per-sample gradient (B, N_post, N_pre) like the
  * reference; group > 1: the batch mean (mean != 0) or sum (N_post, N_pre), accumulated per group of samples
- * and reduced in a fixed order (deterministic). Reads the events grouped in pre-neuron buckets of 64
- * (events_bucketed + bucket_offsets from bats_sort_events with bucket_width 64) when given, else filters the
- * time-sorted events (events + ev_count). Replaces compute_weights_gradient (+ the caller's mean over the
- * batch) (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24). */
+ * and reduced in a fixed order (deterministic). Reads the events grouped in pre-neuron buckets of
+ * BATS_GRAD_BUCKET_WIDTH (events_bucketed + bucket_offsets from bats_sort_events with bucket_width
+ * BATS_GRAD_BUCKET_WIDTH) when given, else filters the
+ * time-sorted events (events + ev_count). cursor_heads: NULL, or the array bats_backward_prep_counted wrote
+ * with these tables (used with the bucketed events). Replaces compute_weights_gradient (+ the caller's mean
+ * over the batch) (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24). */
 size_t bats_weights_gradient_workspace_bytes(int batch, int n_post, int n_pre, int group);
 int bats_weights_gradient(const void* events, const int* ev_count, const void* events_bucketed,
                           const int* bucket_offsets, long long ev_cap, const float* post_times, const void* tables,
-                          const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, int mean,
-                          float* grad, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+                          const int* nvalid, const void* cursor_heads, int batch, int n_post, int k_post, int n_pre,
+                          int group, int mean, float* grad, void* workspace, size_t workspace_bytes,
+                          cudaStream_t stream);
 
 /* The batch-mean weight gradient (bats_weights_gradient with group >= 2, mean) and the Adam update of the
  * weights (bats_adam_step_device) in one call: the group partials are summed, divided by the batch and fed to
@@ -231,10 +242,12 @@ int bats_weights_gradient(const void* events, const int* ev_count, const void* e
  * (bats/CudaKernels/Wrappers/Backpropagation/compute_weights_gradient.py:10-24, train_spike_count.py:167) and
  * AdamOptimizer.step + Network.apply_deltas (bats/Optimizers/AdamOptimizer.py:35-55,
  * bats/Layers/LIFLayer.py:112-113). The weights change, so a caller that propagates errors through this
- * layer (bats_pre_errors) does so before this call. Workspace: bats_weights_gradient_workspace_bytes. */
+ * layer (bats_pre_errors) does so before this call. Workspace: bats_weights_gradient_workspace_bytes.
+ * cursor_heads as for bats_weights_gradient. */
 int bats_weights_gradient_adam(const void* events, const int* ev_count, const void* events_bucketed,
                                const int* bucket_offsets, long long ev_cap, const float* post_times, const void* tables,
-                               const int* nvalid, int batch, int n_post, int k_post, int n_pre, int group, float* grad,
+                               const int* nvalid, const void* cursor_heads, int batch, int n_post, int k_post,
+                               int n_pre, int group, float* grad,
                                float* m, float* v, float beta_1, float beta_2, float epsilon, float learning_rate,
                                const double* powers, float* weights, float* weights_t, int ld, void* workspace,
                                size_t workspace_bytes, cudaStream_t stream);
@@ -412,9 +425,12 @@ int bats_conv_backward_adam(const void* events, const int* ev_slot, const int* e
  * transposed weights, which Adam keeps in sync, constants, forward variant, events, slots, counts and outputs
  * for `batch` samples), and the backward and optimizer state, all device buffers owned by the caller:
  *   weights (n_post, n_pre), adam_m, adam_v (same shape), grad (same shape: the last step's batch-mean gradient);
- *   events_bucketed (batch, n_pre*k_pre records) and bucket_offsets (batch, ceil(n_pre/64) + 1): the events
- *     grouped by 64-neuron pre buckets for the gradient (both NULL: the gradient reads the time-sorted events);
+ *   events_bucketed (batch, n_pre*k_pre records) and bucket_offsets (batch, ceil(n_pre/BATS_GRAD_BUCKET_WIDTH)
+ *     + 1): the events grouped by pre buckets of BATS_GRAD_BUCKET_WIDTH neurons for the gradient (both NULL: the
+ *     gradient reads the time-sorted events);
  *   tables (batch, n_post, k_post + 1, 2 floats), nvalid (batch, n_post): the backward's suffix tables;
+ *   cursor_heads (bats_cursor_heads_bytes(batch, n_post) bytes, 16-byte aligned; NULL: not used): written by
+ *     the counted prep (k_post <= 32) and read by the gradient;
  *   f1, f2 (batch, n_post, k_post): factors, needed only when k_post > 32 (else may be NULL);
  *   pre_errors (batch, n_pre, k_pre): errors of the layer's input spikes, filled for every layer but the first
  *     (NULL there); they are the incoming errors of the layer below, whose reset-error step changes them;
@@ -429,6 +445,7 @@ typedef struct BatsFcTrainLayer {
     int* bucket_offsets;
     void* tables;
     int* nvalid;
+    void* cursor_heads;
     float* f1;
     float* f2;
     float* pre_errors;

@@ -257,7 +257,7 @@ def test_fused_gradient_adam_equals_gradient_then_adam(cuda, group, bucketed, n_
         for _ in range(2):
             call("bats_adam_powers_advance", ptr(powers), 0.9, 0.999, stream_ptr())
             common = (ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed), ptr(ev.bucket_offsets), ev.cap, ptr(ts),
-                      ptr(tabs.tables), ptr(tabs.nvalid), B, n_post, 20, n_in, group)
+                      ptr(tabs.tables), ptr(tabs.nvalid), ptr(tabs.heads), B, n_post, 20, n_in, group)
             if fused:
                 call("bats_weights_gradient_adam", *common, ptr(g), ptr(m), ptr(v), 0.9, 0.999, 1e-8, 3e-3,
                      ptr(powers), ptr(w), ptr(wtt), wtt.shape[1], ptr(ws), ws_bytes, stream_ptr())

@@ -58,9 +58,9 @@ def test_work_queue_forward_argument_checks(lib):
     assert b"workspace" in L.bats_last_error()
 
 
-def _grad_adam(L, group=8, ld=128, n_post=100, batch=32, ws_bytes=0, grad=True):
+def _grad_adam(L, group=8, ld=128, n_post=100, batch=32, ws_bytes=0, grad=True, heads=None):
     fake = ctypes.c_void_p(256)
-    return L.bats_weights_gradient_adam(fake, fake, None, None, 1000, fake, fake, fake, batch, n_post, 4, 50, group,
+    return L.bats_weights_gradient_adam(fake, fake, None, None, 1000, fake, fake, fake, heads, batch, n_post, 4, 50, group,
                                         fake if grad else None, fake, fake, 0.9, 0.999, 1e-8, 1e-3, fake, fake, fake,
                                         ld, fake if ws_bytes else None, ws_bytes, None)
 
@@ -72,6 +72,7 @@ def test_fused_gradient_adam_argument_checks(lib):
     assert _grad_adam(L, batch=0) == 0
     assert _grad_adam(L) == WORKSPACE                       # 4 partials need the workspace
     assert _grad_adam(L, group=64, grad=False) == NULLPTR   # one partial lives in grad
+    assert _grad_adam(L, heads=ctypes.c_void_p(264)) == BAD_SHAPE  # cursor heads not 16-byte aligned
 
 
 def _step_stand_in(batch, sizes, groups, algos):
