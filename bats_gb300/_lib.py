@@ -90,6 +90,7 @@ SIGNATURES = {
                                       c_int, c_int, c_int, c_vp]),
     "bats_add_deltas": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_vp]),
     "bats_transpose": (c_int, [c_vp, c_int, c_int, c_vp, c_int, c_vp]),
+    "bats_copy_device": (c_int, [c_vp, c_vp, c_size, c_vp]),
     "bats_conv_backward_adam_workspace_bytes": (c_size, [c_int, c_int, c_int, c_int, c_int, c_int]),
     "bats_conv_backward_adam": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_int,
                                         c_int, c_int, c_int, c_vp, c_vp, c_vp, c_int, c_float, c_float, c_vp, c_int,

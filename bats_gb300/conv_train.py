@@ -23,7 +23,7 @@ import torch
 
 from . import kernels as K
 from ._lib import call, ptr, stream_ptr
-from .train import FCLayerSpec
+from .train import FCLayerSpec, enqueue_launches
 
 
 @dataclass
@@ -123,6 +123,14 @@ class ConvTrainStep:
         self.loss = torch.empty((B,), dtype=f32, device=dev)
         self.errors = torch.empty((B, last["n"], last["k"]), dtype=f32, device=dev)
         self.ws = torch.empty(ws, dtype=torch.uint8, device=dev)
+        # The gradient + Adam of the fully-connected layers that propagate errors below them runs on a second
+        # stream beside the rest of the backward (as in FCTrainStep): it writes the layer's new transposed
+        # weights into a staging copy, copied over Wt at the end of the step, and uses its own workspace.
+        for li, d in enumerate(self.L):
+            if d["kind"] == "fc" and li > 0:
+                d["Wt_next"] = d["Wt"].clone()
+        self.ws2 = torch.empty_like(self.ws)
+        self.aux = torch.cuda.Stream(device=dev) if torch.cuda.is_available() else None
         self.powers = torch.tensor([1.0, 1.0, 0.0, 0.0], dtype=torch.float64, device=dev)
         self.graph: Optional[torch.cuda.CUDAGraph] = None
         self.capture_error = None
@@ -217,22 +225,31 @@ class ConvTrainStep:
                         "bats_pre_errors", ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ev.cap, ptr(d["Wt"]),
                         d["Wt"].shape[1], ptr(d["out"][3]), ptr(d["tables"]), ptr(d["nvalid"]), B, d["n"], d["k"],
                         ev.n_neurons, ev.k, tau_s, float(d["tau32"]), ptr(pe), ws, wsb, s)))
-                L.append((f"{tag}.grad_adam", lambda s, d=d, ev=ev: call(
+                staged = "Wt_next" in d
+                wt_out = d["Wt_next"] if staged else d["Wt"]
+                gws, gwsb = (ptr(self.ws2), self.ws2.numel()) if staged else (ws, wsb)
+                L.append((f"{tag}.grad_adam", lambda s, d=d, ev=ev, wt_out=wt_out, gws=gws, gwsb=gwsb: call(
                     "bats_weights_gradient_adam", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed),
                     ptr(ev.bucket_offsets), ev.cap, ptr(d["out"][3]), ptr(d["tables"]), ptr(d["nvalid"]),
                     ptr(d["heads"]), B, d["n"], d["k"], ev.n_neurons, d["group"], ptr(d["grad"]), ptr(d["m"]),
                     ptr(d["v"]), float(self.b1),
-                    float(self.b2), float(self.eps), float(self.lr), ptr(self.powers), ptr(d["W"]), ptr(d["Wt"]),
-                    d["Wt"].shape[1], ws, wsb, s)))
+                    float(self.b2), float(self.eps), float(self.lr), ptr(self.powers), ptr(d["W"]), ptr(wt_out),
+                    d["Wt"].shape[1], gws, gwsb, s)))
             if pe is not None:
                 errors = pe
+        for li in range(len(self.L) - 1, -1, -1):
+            d = self.L[li]
+            if "Wt_next" in d:
+                L.append((f"L{li + 1}.wt_copy", lambda s, d=d: K.copy_on_stream(d["Wt"], d["Wt_next"], s)))
         return L
+
+    def _side_launches(self):
+        """{gradient launch: its layer's prep} for the layers whose transposed weights are staged."""
+        return {f"L{li + 1}.grad_adam": f"L{li + 1}.prep" for li, d in enumerate(self.L) if "Wt_next" in d}
 
     # -- running ----------------------------------------------------------------------------------------
     def step(self) -> None:
-        s = stream_ptr()
-        for _, fn in self.launches:
-            fn(s)
+        enqueue_launches(self.launches, self._side_launches(), torch.cuda.current_stream(), self.aux)
         self.t += 1
 
     def try_capture(self) -> bool:
@@ -245,9 +262,7 @@ class ConvTrainStep:
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):
                 with torch.cuda.graph(g, stream=side):
-                    s = stream_ptr()
-                    for _, fn in self.launches:
-                        fn(s)
+                    enqueue_launches(self.launches, self._side_launches(), side, self.aux)
             torch.cuda.current_stream().wait_stream(side)
             torch.cuda.synchronize()
             self.graph = g

@@ -396,6 +396,13 @@ extern "C" int bats_transpose(const float* in, int rows, int cols, float* out, i
     return BATS_OK;
 }
 
+extern "C" int bats_copy_device(void* dst, const void* src, size_t bytes, cudaStream_t stream) {
+    if (bytes == 0) return BATS_OK;
+    BATS_REQUIRE(dst && src, BATS_ERR_NULL, "copy_device: null pointer");
+    BATS_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, stream));
+    return BATS_OK;
+}
+
 extern "C" int bats_add_deltas(float* weights, const float* delta, long long count, float* weights_t, int n_pre,
                                int ld, cudaStream_t stream) {
     BATS_REQUIRE(count >= 0, BATS_ERR_BAD_SHAPE, "add_deltas: bad shape");

@@ -131,6 +131,13 @@ def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=N
     return out
 
 
+def copy_on_stream(dst: torch.Tensor, src: torch.Tensor, stream: int) -> None:
+    """dst <- src (same shape, contiguous: one device-to-device copy) enqueued on the raw CUDA stream
+    `stream`, the stream argument of a train step's launches."""
+    assert dst.shape == src.shape and dst.dtype == src.dtype and dst.is_contiguous() and src.is_contiguous()
+    call("bats_copy_device", ptr(dst), ptr(src), dst.numel() * dst.element_size(), stream)
+
+
 def call_size(name, *args) -> int:
     from ._lib import load
     return int(getattr(load(), name)(*args))
@@ -407,12 +414,12 @@ def weights_gradient(events: Events, post_times, tabs: BackwardTables, n_pre: in
 
 
 def grad_tile(n_post: int) -> int:
-    return 32 if n_post <= 32 else (64 if n_post <= 64 else 128)
+    return 32 if n_post <= 32 else 64
 
 
-def default_group(batch: int, n_post: int, n_pre: int, target_ctas: int = 1216) -> int:
-    """Samples per group of the batch-reduced weight gradient: enough groups for ~8 CTAs per SM of a
-    152-SM GB300, but at most 32 partial gradients (narrow layers, N_post <= 32, whose partials are small
+def default_group(batch: int, n_post: int, n_pre: int, target_ctas: int = 2432) -> int:
+    """Samples per group of the batch-reduced weight gradient: enough groups for ~16 two-warp CTAs per SM of
+    a 152-SM GB300, but at most 32 partial gradients (narrow layers, N_post <= 32, whose partials are small
     and whose kernel runs one warp per bucket and group: up to 4 warps per SM, any number of partials)."""
     if n_post <= 32:
         buckets = (n_pre + BUCKET_WIDTH - 1) // BUCKET_WIDTH

@@ -86,6 +86,13 @@ class FCTrainStep:
                      K.call_size("bats_pre_errors_workspace_bytes", B, n_prev * k_prev, spec.n_neurons))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
         self.ws = torch.empty(max(ws, 256), dtype=torch.uint8, device=dev)
+        # The gradient + Adam of every layer above the first runs on a second stream, beside the pre-spike
+        # errors that read the layer's old transposed weights: it writes the new ones into a staging copy
+        # (copied over Wt at the end of the step) and uses its own workspace (as large as the first, so that
+        # every gradient group the autotuner may pick fits both).
+        self.Wt_next = [wt.clone() if li > 0 else None for li, wt in enumerate(self.Wt)]
+        self.ws2 = torch.empty_like(self.ws)
+        self.aux = torch.cuda.Stream(device=dev) if torch.cuda.is_available() else None
         self.graph: Optional[torch.cuda.CUDAGraph] = None
         self.capture_error = None
         # beta_1^t, beta_2^t on the device, advanced by one launch per step (keeps the step capturable).
@@ -166,13 +173,28 @@ class FCTrainStep:
                     spec.max_n_spike, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32), ptr(pe), ws,
                     wsb, s)))
                 errors = pe
-            L.append((f"{tag}.grad_adam", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li: call(
+            # Above the first layer: the staging copy of Wt and the second workspace (see __init__).
+            wt_out = self.Wt_next[li] if li > 0 else self.Wt[li]
+            gws, gwsb = (ptr(self.ws2), self.ws2.numel()) if li > 0 else (ws, wsb)
+            L.append((f"{tag}.grad_adam", lambda s, ev=ev, t=t, tb=tb, spec=spec, li=li, wt_out=wt_out, gws=gws,
+                      gwsb=gwsb: call(
                 "bats_weights_gradient_adam", ptr(ev.events), ptr(ev.counts), ptr(ev.bucketed),
                 ptr(ev.bucket_offsets), ev.cap, ptr(t), ptr(tb.tables), ptr(tb.nvalid), ptr(tb.heads), B,
                 spec.n_neurons, spec.max_n_spike, ev.n_neurons, self.groups[li], ptr(self.grad[li]), ptr(self.m[li]),
                 ptr(self.v[li]), float(self.b1), float(self.b2), float(self.eps), float(self.lr), ptr(self.powers),
-                ptr(self.W[li]), ptr(self.Wt[li]), self.Wt[li].shape[1], ws, wsb, s)))
+                ptr(self.W[li]), ptr(wt_out), self.Wt[li].shape[1], gws, gwsb, s)))
+        for li in range(len(self.specs) - 1, 0, -1):
+            L.append((f"L{li + 1}.wt_copy", lambda s, li=li: K.copy_on_stream(self.Wt[li], self.Wt_next[li], s)))
         return L
+
+    def _side_launches(self):
+        """{gradient launch: the launch it waits for}: each layer's gradient + Adam above the first, which
+        needs only its layer's prep (and what came before it)."""
+        return {f"L{li + 1}.grad_adam": f"L{li + 1}.prep" for li in range(1, len(self.specs))}
+
+    def _enqueue(self, main, aux=None) -> None:
+        """Enqueue one step on the torch stream `main` (and `aux`: see enqueue_launches)."""
+        enqueue_launches(self.launches, self._side_launches(), main, aux)
 
     # -- the same step as one foreign call (bats_fc_train_step) -------------------------------------
     def native_layers(self):
@@ -236,6 +258,8 @@ class FCTrainStep:
             return 2 if K.is_queue_algo(self.fwd_algo[li]) else 1
         if kind == "pre_err":  # narrow layers: one event-parallel kernel; else the tile kernel and the scatter
             return 1 if spec.n_neurons <= 32 else 2
+        if kind == "wt_copy":  # a device-to-device copy, no kernel
+            return 0
         if kind == "grad_adam":  # the gradient, then the fused reduce-Adam, or for few weight tiles and
             groups = -(-self.B // self.groups[li])  # several partials the reduction and the tiled Adam
             tiles = -(-n_pre // 32) * -(-spec.n_neurons // 32)
@@ -246,10 +270,9 @@ class FCTrainStep:
         return sum(self._kernels_of(name) for name, _ in self.launches)
 
     def step(self) -> None:
-        """One training step on the device-resident inputs (in_times, labels), launched eagerly."""
-        s = stream_ptr()
-        for _, fn in self.launches:
-            fn(s)
+        """One training step on the device-resident inputs (in_times, labels), launched eagerly (with the
+        gradients above the first layer on the second stream, as in the graph)."""
+        self._enqueue(torch.cuda.current_stream(), self.aux)
         self.t += 1
 
     def autotune(self, tuner: Optional[Autotuner] = None, force: bool = False) -> dict:
@@ -259,7 +282,8 @@ class FCTrainStep:
         tuner = tuner or get_tuner()
         s = stream_ptr()
         for name, fn in self.launches:
-            if not name.endswith("grad_adam") and name != "adam.powers":  # leave the weights and Adam state alone
+            # leave the weights and Adam state alone (no update, no staged transposed weights copied in)
+            if not name.endswith(("grad_adam", "wt_copy")) and name != "adam.powers":
                 fn(s)
         torch.cuda.synchronize()
         B = self.B
@@ -319,9 +343,7 @@ class FCTrainStep:
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(side):
                 with torch.cuda.graph(g, stream=side):
-                    s = stream_ptr()
-                    for _, fn in self.launches:
-                        fn(s)
+                    self._enqueue(side, self.aux)
             torch.cuda.current_stream().wait_stream(side)
             torch.cuda.synchronize()
             self.graph = g
@@ -458,3 +480,35 @@ class FCTrainStep:
     @property
     def d2h_bytes(self) -> int:
         return self.h_loss.numel() * 4
+
+
+def enqueue_launches(launches, side, main, aux=None) -> None:
+    """Enqueue a step's launch list on the torch stream `main`. With `aux`, the launches named in `side`
+    ({launch: the launch it waits for}) run on `aux`, each after its dependency has been enqueued on `main`,
+    and `main` waits for `aux` before the first `.wt_copy` launch (which copies the staged transposed weights
+    that those launches wrote) or at the end. The launches on `aux` read only what their dependency and the
+    launches before it wrote, and write nothing that `main` reads before the join, so the results are those
+    of the list run in order on one stream."""
+    sm = main.cuda_stream
+    if aux is None:
+        for _, fn in launches:
+            fn(sm)
+        return
+    forks = set(side.values())
+    events = {}
+    joined = False
+    for name, fn in launches:
+        if name in side:
+            aux.wait_event(events[side[name]])
+            fn(aux.cuda_stream)
+            continue
+        if name.endswith(".wt_copy") and not joined:
+            main.wait_stream(aux)
+            joined = True
+        fn(sm)
+        if name in forks:
+            e = torch.cuda.Event()
+            e.record(main)
+            events[name] = e
+    if not joined:
+        main.wait_stream(aux)

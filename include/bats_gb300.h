@@ -361,6 +361,10 @@ int bats_add_deltas(float* weights, const float* delta, long long count, float* 
 /* out (cols, ld) = in (rows, cols)^T. Builds the transposed weights read by the FC kernels. */
 int bats_transpose(const float* in, int rows, int cols, float* out, int ld, cudaStream_t stream);
 
+/* One device-to-device copy of `bytes` bytes, enqueued on `stream` (a memcpy node when the stream is being
+ * captured): the train steps copy staged transposed weights with it. */
+int bats_copy_device(void* dst, const void* src, size_t bytes, cudaStream_t stream);
+
 /* One fully-connected layer of a served network, for bats_serve_fc_batch: shapes, transposed weights
  * (n_pre, ld), constants as for bats_lif_forward_fc (tau = 2 tau_s, c = theta/tau, delta_theta/tau), the
  * forward kernel variant, and the layer's device buffers for `batch` samples: sorted events

@@ -155,9 +155,9 @@ def test_workspace_queries(lib):
     # two 4-byte key and two 2-byte slot buffers per slot when the slots fit 16 bits, 4-byte slots above
     assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 30000 * 12
     assert L.bats_sort_events_workspace_bytes(2, 4000, 20) == 2 * 80000 * 16
-    # 16 partial gradients, 256-byte aligned, then one flag per (partial, pre bucket of 32, post tile of 128)
+    # 16 partial gradients, 256-byte aligned, then one flag per (partial, pre bucket of 32, 32 post neurons)
     parts = (16 * 800 * 784 * 4 + 255) // 256 * 256
-    assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == parts + 16 * 25 * 7 * 4
+    assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 16) == parts + 16 * 25 * 25 * 4
     assert L.bats_weights_gradient_workspace_bytes(256, 800, 784, 1) == 0
     # cursor heads: a float2 per (sample, neuron), then from the next 16-byte boundary a float4 per pair
     assert L.bats_cursor_heads_bytes(3, 5) == 128 + 15 * 16
