@@ -150,3 +150,49 @@ def test_caller_outputs_are_checked_before_any_call():
     with pytest.raises(ValueError, match="contiguous CUDA"):
         K.pre_errors(ev, None, post, None, 0.13, 0.26, out=torch.zeros((2, 5, 2)))
     assert K._out.__doc__
+
+
+def test_two_stream_enqueue_order(monkeypatch):
+    """enqueue_launches: the side launches run on the second stream, each after an event recorded on the
+    main stream right after its dependency; the main stream waits for the second before the first staged
+    weights copy; everything else keeps the list's order on the main stream; without a second stream the
+    list runs in order on the main one."""
+    import torch
+    from bats_gb300 import train
+
+    log = []
+
+    class FakeEvent:
+        def __init__(self, *a, **k):
+            self.after = None
+
+        def record(self, stream):
+            self.after = list(log)
+            log.append(("record", stream.name))
+
+    class FakeStream:
+        def __init__(self, name, handle):
+            self.name, self.cuda_stream = name, handle
+
+        def wait_event(self, e):
+            log.append(("wait_event", self.name, e.after[-1]))
+
+        def wait_stream(self, other):
+            log.append(("wait_stream", self.name, other.name))
+
+    monkeypatch.setattr(torch.cuda, "Event", FakeEvent)
+    names = ["L3.prep", "L3.pre_err", "L3.grad_adam", "L2.prep", "L2.pre_err", "L2.grad_adam", "L1.prep",
+             "L1.grad_adam", "L3.wt_copy", "L2.wt_copy"]
+    launches = [(n, (lambda s, n=n: log.append((n, s)))) for n in names]
+    side = {"L3.grad_adam": "L3.prep", "L2.grad_adam": "L2.prep"}
+    main, aux = FakeStream("main", 1), FakeStream("aux", 2)
+    train.enqueue_launches(launches, side, main, aux)
+    assert log == [("L3.prep", 1), ("record", "main"), ("L3.pre_err", 1),
+                   ("wait_event", "aux", ("L3.prep", 1)), ("L3.grad_adam", 2),
+                   ("L2.prep", 1), ("record", "main"), ("L2.pre_err", 1),
+                   ("wait_event", "aux", ("L2.prep", 1)), ("L2.grad_adam", 2),
+                   ("L1.prep", 1), ("L1.grad_adam", 1), ("wait_stream", "main", "aux"),
+                   ("L3.wt_copy", 1), ("L2.wt_copy", 1)]
+    log.clear()
+    train.enqueue_launches(launches, side, main, None)
+    assert log == [(n, 1) for n in names]
