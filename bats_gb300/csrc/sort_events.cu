@@ -19,29 +19,41 @@
 
 namespace bats {
 
-constexpr int SORT_THREADS = 256;
-constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int SORT_BINS = 256;  // digit values of a counting pass; threads tid < SORT_BINS own one bin each
 constexpr int SORT_MAX_BUCKETS = 255;
+// Threads per CTA: 512 for layers of more than SORT_WIDE_CAP slots (each round of a counting pass ranks 512
+// items: 0.88 -> 0.71 ms on the 4096-sample uneven batch's second sort, 0.093 -> 0.081 ms on 800 x 30 slots
+// at batch 256), 256 below (samples of a few hundred items, which a larger block only spreads thinner).
+constexpr int SORT_WIDE_CAP = 1024;
 // Items held in shared memory (two key buffers and two value buffers): slot values are 16-bit when the
 // layer has at most 65536 slots (cap = n_pre * k_pre), else 32-bit. Batches of at most SORT_SMALL_BATCH
 // samples (no more CTAs than a GB300 has SMs: one CTA per SM costs no parallelism) get as many items as
-// 227 KB holds (SORT_SMEM_MAX_U16 / _U32); larger batches keep two CTAs per SM (SORT_SMEM_U16 / _U32 items,
-// 110 KB or 82 KB with the counters). Samples with more valid slots than that sort in global scratch.
+// 227 KB holds (SortCaps max_u16 / max_u32); larger batches keep two CTAs per SM (u16 / u32 items, at most
+// 113 KB with the counters). Samples with more valid slots than that sort in global scratch. The capacities
+// leave room for the counters (SortShared: 18.5 KB at 256 threads, 34.9 KB at 512).
 constexpr int SORT_SMALL_BATCH = 152;
-constexpr int SORT_SMEM_MAX_U16 = 17408;  // 12 B per item + the counters <= 227 KB
-constexpr int SORT_SMEM_MAX_U32 = 13312;  // 16 B per item
-constexpr int SORT_SMEM_U16 = 7680;
-constexpr int SORT_SMEM_U32 = 4096;
-
-struct SortShared {
-    int hist[256];
-    int base[256];
-    int wcnt[SORT_WARPS][256];
-    int wofs[SORT_WARPS][256];
-    int warp_tot[SORT_WARPS];
+template <int T>
+struct SortCaps;
+template <>
+struct SortCaps<256> {
+    static constexpr int max_u16 = 17408, max_u32 = 13312, u16 = 7680, u32 = 4096;
+};
+template <>
+struct SortCaps<512> {
+    static constexpr int max_u16 = 16448, max_u32 = 12320, u16 = 6720, u32 = 4096;
 };
 
-__device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh, int& block_total) {
+template <int T>
+struct SortShared {
+    int hist[SORT_BINS];
+    int base[SORT_BINS];
+    int wcnt[T / 32][SORT_BINS];
+    int wofs[T / 32][SORT_BINS];
+    int warp_tot[T / 32];
+};
+
+template <int T>
+__device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared<T>& sh, int& block_total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned bal = __ballot_sync(0xffffffffu, f);
     const int in_warp = __popc(bal & lanemask_lt());
@@ -49,7 +61,7 @@ __device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh,
     __syncthreads();
     int off = 0, tot = 0;
 #pragma unroll
-    for (int w = 0; w < SORT_WARPS; ++w) {
+    for (int w = 0; w < T / 32; ++w) {
         const int c = sh.warp_tot[w];
         off += (w < warp) ? c : 0;
         tot += c;
@@ -60,7 +72,8 @@ __device__ __forceinline__ int block_exclusive_flag_scan(bool f, SortShared& sh,
 }
 
 // Block-wide exclusive scan of one int per thread (in thread order); block_total gets the sum.
-__device__ __forceinline__ int block_exclusive_scan(int v, SortShared& sh, int& block_total) {
+template <int T>
+__device__ __forceinline__ int block_exclusive_scan(int v, SortShared<T>& sh, int& block_total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int incl = v;
 #pragma unroll
@@ -72,7 +85,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, SortShared& sh, int& 
     __syncthreads();
     int off = 0, tot = 0;
 #pragma unroll
-    for (int w = 0; w < SORT_WARPS; ++w) {
+    for (int w = 0; w < T / 32; ++w) {
         const int c = sh.warp_tot[w];
         off += (w < warp) ? c : 0;
         tot += c;
@@ -82,34 +95,38 @@ __device__ __forceinline__ int block_exclusive_scan(int v, SortShared& sh, int& 
     return off + incl - v;
 }
 
-// Exclusive scan of sh.hist (256 bins, one per thread) into sh.base; clears sh.wcnt.
-__device__ __forceinline__ void scan_bins(SortShared& sh) {
+// Exclusive scan of sh.hist (SORT_BINS bins, one per thread tid < SORT_BINS) into sh.base; clears sh.wcnt.
+template <int T>
+__device__ __forceinline__ void scan_bins(SortShared<T>& sh) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int v = sh.hist[tid];
+    const bool bin = tid < SORT_BINS;
+    const int v = bin ? sh.hist[tid] : 0;
     int incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
     }
-    if (lane == 31) sh.warp_tot[warp] = incl;
+    if (lane == 31 && bin) sh.warp_tot[warp] = incl;
     __syncthreads();
-    int woff = 0;
-    for (int w = 0; w < warp; ++w) woff += sh.warp_tot[w];
-    sh.base[tid] = woff + incl - v;
+    if (bin) {
+        int woff = 0;
+        for (int w = 0; w < warp; ++w) woff += sh.warp_tot[w];
+        sh.base[tid] = woff + incl - v;
 #pragma unroll
-    for (int w = 0; w < SORT_WARPS; ++w) sh.wcnt[w][tid] = 0;
+        for (int w = 0; w < T / 32; ++w) sh.wcnt[w][tid] = 0;
+    }
     __syncthreads();
 }
 
 // One stable counting pass (digit < 256) of n (key, val) pairs from (ka, va) into (kb, vb), using the
-// bin bases already in sh.base. Items are ranked in rounds of SORT_THREADS in their current order;
-// inside a warp, items of equal digit are ranked by __match_any_sync, across warps by a per-digit scan.
-template <typename V, typename DigitFn>
+// bin bases already in sh.base. Items are ranked in rounds of T in their current order; inside a warp,
+// items of equal digit are ranked by __match_any_sync, across warps by a per-digit scan.
+template <int T, typename V, typename DigitFn>
 __device__ __forceinline__ void stable_pass(const uint32_t* ka, const V* va, uint32_t* kb, V* vb, int n,
-                                            SortShared& sh, DigitFn digit) {
+                                            SortShared<T>& sh, DigitFn digit) {
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int r0 = 0; r0 < n; r0 += SORT_THREADS) {
+    for (int r0 = 0; r0 < n; r0 += T) {
         const int i = r0 + tid;
         const bool valid = i < n;
         uint32_t key = 0;
@@ -124,10 +141,10 @@ __device__ __forceinline__ void stable_pass(const uint32_t* ka, const V* va, uin
         const int rank = __popc(peers & lanemask_lt());
         if (valid && rank == 0) sh.wcnt[warp][d] = __popc(peers);
         __syncthreads();
-        {
+        if (tid < SORT_BINS) {
             int off = sh.base[tid];
 #pragma unroll
-            for (int w = 0; w < SORT_WARPS; ++w) {
+            for (int w = 0; w < T / 32; ++w) {
                 sh.wofs[w][tid] = off;
                 off += sh.wcnt[w][tid];
                 sh.wcnt[w][tid] = 0;
@@ -178,8 +195,8 @@ struct BucketDigit {
 };
 
 // V: type of the slot values (uint16_t when n_slots <= 65536). smem_cap: items held in shared memory.
-template <typename V>
-__global__ void __launch_bounds__(SORT_THREADS)
+template <typename V, int T>
+__global__ void __launch_bounds__(T)
 sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_counts, int n_slots, int k_pre,
                    float tau_s, float tau,
                    const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out,
@@ -188,8 +205,9 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
                    unsigned char* __restrict__ scratch) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SortShared& sh = *reinterpret_cast<SortShared*>(smem_raw);
-    unsigned char* smem_items = smem_raw + sizeof(SortShared);
+    constexpr int SORT_THREADS = T, SORT_WARPS = T / 32;
+    SortShared<T>& sh = *reinterpret_cast<SortShared<T>*>(smem_raw);
+    unsigned char* smem_items = smem_raw + sizeof(SortShared<T>);
 
     const int s = blockIdx.x;
     const int tid = threadIdx.x;
@@ -327,10 +345,11 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
         const uint32_t key = tid < n ? ka[tid] : 0u;
         const V val = tid < n ? va[tid] : V(0);
         int rank = 0;
-        for (int q = 0; q < n; ++q) {
-            const uint32_t kq = ka[q];
-            rank += (kq < key || (kq == key && q < tid)) ? 1 : 0;
-        }
+        if (tid < n)
+            for (int q = 0; q < n; ++q) {
+                const uint32_t kq = ka[q];
+                rank += (kq < key || (kq == key && q < tid)) ? 1 : 0;
+            }
         if (tid < n) {
             kb[rank] = key;
             vb[rank] = val;
@@ -341,13 +360,13 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
     }
     // LSD radix sort on the time key, 4 passes of 8 bits; passes whose digit is uniform are skipped.
     for (int shift = 0; n > SORT_THREADS && shift < 32; shift += 8) {
-        sh.hist[tid] = 0;
+        if (tid < SORT_BINS) sh.hist[tid] = 0;
         __syncthreads();
         for (int i = tid; i < n; i += SORT_THREADS) atomicAdd(&sh.hist[(ka[i] >> shift) & 255u], 1);
         __syncthreads();
-        if (__syncthreads_or(sh.hist[tid] == n)) continue;
-        scan_bins(sh);
-        stable_pass(ka, va, kb, vb, n, sh, TimeDigit{shift});
+        if (__syncthreads_or(tid < SORT_BINS && sh.hist[tid] == n)) continue;
+        scan_bins<T>(sh);
+        stable_pass<T>(ka, va, kb, vb, n, sh, TimeDigit{shift});
         uint32_t* t0 = ka; ka = kb; kb = t0;
         V* t1 = va; va = vb; vb = t1;
     }
@@ -363,16 +382,16 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
     if (ev_bucketed) {
         // Stable counting pass by pre-neuron bucket over the time-sorted items.
         const int div = k_pre * bucket_width;
-        sh.hist[tid] = 0;
+        if (tid < SORT_BINS) sh.hist[tid] = 0;
         __syncthreads();
         for (int i = tid; i < n; i += SORT_THREADS) atomicAdd(&sh.hist[(int)va[i] / div], 1);
         __syncthreads();
-        scan_bins(sh);
+        scan_bins<T>(sh);
         int* bo = bucket_off + (long long)s * (n_buckets + 1);
         if (tid < n_buckets) bo[tid] = sh.base[tid];
         if (tid == 0) bo[n_buckets] = n;
         __syncthreads();
-        stable_pass(ka, va, kb, vb, n, sh, BucketDigit{div});
+        stable_pass<T>(ka, va, kb, vb, n, sh, BucketDigit{div});
         Event* be = ev_bucketed + (long long)s * cap;
         for (int m = tid; m < n; m += SORT_THREADS)
             be[m] = make_event(kb[m], (uint32_t)vb[m], k_pre, sample_off, exp_s_in, exp_in, tau_s, tau);
@@ -387,11 +406,15 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
 #include "abi_util.h"
 
 // Shared-memory items and value width for a batch of samples with cap slots each (see SORT_SMALL_BATCH).
+template <int T>
+static int sort_room(bool small, bool u16) {
+    using C = bats::SortCaps<T>;
+    return u16 ? (small ? C::max_u16 : C::u16) : (small ? C::max_u32 : C::u32);
+}
 static void sort_plan(int batch, long long cap, int* smem_cap, bool* u16) {
     *u16 = cap <= 65536;
     const bool small = batch <= bats::SORT_SMALL_BATCH;
-    const int room = *u16 ? (small ? bats::SORT_SMEM_MAX_U16 : bats::SORT_SMEM_U16)
-                          : (small ? bats::SORT_SMEM_MAX_U32 : bats::SORT_SMEM_U32);
+    const int room = cap > bats::SORT_WIDE_CAP ? sort_room<512>(small, *u16) : sort_room<256>(small, *u16);
     *smem_cap = (int)std::min<long long>(room, (cap + 31) / 32 * 32);
 }
 
@@ -403,6 +426,22 @@ extern "C" size_t bats_sort_events_workspace_bytes(int batch, int n_pre, int k_p
     if (cap <= smem_cap) return 0;
     return (size_t)(batch > 0 ? batch : 0) * (size_t)cap * (u16 ? 12 : 16);
 }
+
+template <typename V, int T>
+static cudaError_t launch_sort(const float* pre_times, const int* pre_counts, int batch, long long cap, int k_pre,
+                               float tau_s, float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out,
+                               int* slot_out, int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
+                               int n_buckets, int smem_cap, unsigned char* scratch, cudaStream_t stream) {
+    const size_t smem = sizeof(bats::SortShared<T>) + (size_t)smem_cap * (8 + 2 * sizeof(V));
+    cudaError_t e = (cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel<V, T>, (int)smem);
+    if (e != cudaSuccess) return e;
+    return bats::launch(bats::sort_events_kernel<V, T>, batch, T, smem, stream, pre_times, pre_counts, (int)cap, k_pre,
+                        tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out, ev_count,
+                        reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets, cap,
+                        smem_cap, scratch);
+}
+#define SORT_ARGS pre_times, pre_counts, batch, cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out, slot_out, \
+                  ev_count, ev_bucketed, bucket_offsets, bucket_width, n_buckets, smem_cap, scratch, stream
 
 static int sort_events_impl(const float* pre_times, const int* pre_counts, int batch, int n_pre, int k_pre,
                             float tau_s, float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out,
@@ -427,21 +466,14 @@ static int sort_events_impl(const float* pre_times, const int* pre_counts, int b
     int smem_cap;
     bool u16;
     sort_plan(batch, cap, &smem_cap, &u16);
-    const size_t smem = sizeof(bats::SortShared) + (size_t)smem_cap * (8 + 2 * (u16 ? 2 : 4));
     unsigned char* scratch = reinterpret_cast<unsigned char*>(workspace);
-    if (u16) {
-        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel<uint16_t>, (int)smem));
-        BATS_CUDA(bats::launch(bats::sort_events_kernel<uint16_t>, batch, bats::SORT_THREADS, smem, stream, pre_times,
-            pre_counts, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out),
-            slot_out, ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets,
-            cap, smem_cap, scratch));
-    } else {
-        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel<uint32_t>, (int)smem));
-        BATS_CUDA(bats::launch(bats::sort_events_kernel<uint32_t>, batch, bats::SORT_THREADS, smem, stream, pre_times,
-            pre_counts, (int)cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out),
-            slot_out, ev_count, reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets,
-            cap, smem_cap, scratch));
-    }
+    const bool wide = cap > bats::SORT_WIDE_CAP;
+    cudaError_t err;
+    if (u16)
+        err = wide ? launch_sort<uint16_t, 512>(SORT_ARGS) : launch_sort<uint16_t, 256>(SORT_ARGS);
+    else
+        err = wide ? launch_sort<uint32_t, 512>(SORT_ARGS) : launch_sort<uint32_t, 256>(SORT_ARGS);
+    BATS_CUDA(err);
     return BATS_OK;
 }
 

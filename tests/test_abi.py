@@ -151,7 +151,10 @@ def test_workspace_queries(lib):
     assert L.bats_sort_events_workspace_bytes(4, 10, 3) == 0  # fits in shared memory
     assert L.bats_sort_events_workspace_bytes(4, 512, 30) == 0  # 15360 slots: the whole layer in shared memory
     assert L.bats_sort_events_workspace_bytes(256, 512, 30) == 256 * 15360 * 12  # large batch: 7680 items
-    assert L.bats_sort_events_workspace_bytes(256, 256, 30) == 0
+    # layers above 1024 slots sort with 512 threads, whose counters leave 6720 items at two CTAs per SM
+    assert L.bats_sort_events_workspace_bytes(256, 256, 30) == 256 * 7680 * 12
+    assert L.bats_sort_events_workspace_bytes(256, 200, 30) == 0
+    assert L.bats_sort_events_workspace_bytes(256, 1024, 1) == 0  # 256 threads: room for 7680 items
     # two 4-byte key and two 2-byte slot buffers per slot when the slots fit 16 bits, 4-byte slots above
     assert L.bats_sort_events_workspace_bytes(4, 1000, 30) == 4 * 30000 * 12
     assert L.bats_sort_events_workspace_bytes(2, 4000, 20) == 2 * 80000 * 16

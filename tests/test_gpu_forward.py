@@ -161,13 +161,15 @@ def test_sort_events_small_samples_with_ties(cuda, k):
 @pytest.mark.parametrize("shape,fill", [((2, 1000, 6), (6000, 3000)), ((2, 512, 30), (15360, 4000)),
                                         ((2, 1000, 20), (20000, 5000)), ((2, 5000, 14), (70000, 3000)),
                                         ((2, 1000, 16), (16000, 13000)), ((160, 512, 30), (15360, 7000)),
+                                        ((160, 512, 30), (6720, 6721)), ((160, 1000, 1), (1000, 999)),
                                         ((160, 4000, 20), (80000, 4000))])
 def test_sort_events_large_sample_uses_global_path(cuda, shape, fill):
-    """Samples of every size class of the sort. Small batches (<= 152 samples): up to 17408 items in shared
-    memory with 16-bit slot values (layers of at most 65536 slots), 13312 with 32-bit values; larger
-    batches: 7680 and 4096. Samples above that sort in the global workspace. Events and slots equal the
-    oracle's sort; the bucketed copy is each bucket's events in time order. The samples not listed in
-    `fill` hold 37 spikes."""
+    """Samples of every size class of the sort. Layers of more than 1024 slots sort with 512 threads: small
+    batches (<= 152 samples) hold up to 16448 items in shared memory with 16-bit slot values (layers of at
+    most 65536 slots), 12320 with 32-bit values; larger batches 6720 and 4096 (the boundary exactly: 6720 and
+    6721 items). Smaller layers sort with 256 threads (17408 / 13312 / 7680 / 4096 items). Samples above
+    that sort in the global workspace. Events and slots equal the oracle's sort; the bucketed copy is each
+    bucket's events in time order. The samples not listed in `fill` hold 37 spikes."""
     rng = np.random.default_rng(4)
     B, N, Kp = shape
     t = np.full(shape, np.inf, np.float32)
