@@ -13,9 +13,10 @@ void set_last_error(int status, const char* where, const char* what) {
     std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s (status %d)", where, what, status);
 }
 
-// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (kernel, device). Returns a cudaError_t.
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per (kernel, device), for any dynamic size: a kernel's
+// static shared memory counts toward the 48 KB that needs no opt-in. Returns a cudaError_t.
 int max_dynamic_smem_set(const void* func, int bytes) {
-    if (bytes <= 48 * 1024) return (int)cudaSuccess;
+    if (bytes <= 0) return (int)cudaSuccess;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return (int)e;

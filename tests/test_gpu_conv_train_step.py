@@ -116,3 +116,31 @@ def test_conv_train_step_graph_replay_equals_eager(cuda, group):
         if a is not None:
             assert torch.equal(a, b)
     assert torch.equal(eager.loss, graphed.loss)
+
+
+def test_conv_train_step_second_stream_keeps_results(cuda):
+    """The fully-connected layers' gradient + Adam on the second stream (staged transposed weights copied in
+    at the end of the step) gives the weights, transposed weights and losses of the launch list run in order
+    on one stream, bit for bit, eagerly and under graph capture."""
+    t, _ = mnist_like_input(B, seed=5)
+    labels = np.random.default_rng(6).integers(0, 10, B).astype(np.int32)
+    ws = weights(seed=7)
+    one, two, graphed = make_step(ws, t, labels), make_step(ws, t, labels), make_step(ws, t, labels)
+    one.aux = None
+    assert two.aux is not None and any("Wt_next" in d for d in two.L)
+    assert graphed.try_capture(), graphed.capture_error
+    one.step()
+    two.step()
+    for _ in range(2):
+        one.step()
+        two.step()
+        graphed.replay()
+    torch.cuda.synchronize()
+    for a, b, c in zip(one.weights, two.weights, graphed.weights):
+        if a is not None:
+            assert torch.equal(a, b) and torch.equal(a, c)
+    for da, db in zip(one.L, two.L):
+        if "Wt" in da:
+            assert torch.equal(da["Wt"], db["Wt"])
+    assert torch.equal(one.loss, two.loss) and torch.equal(one.loss, graphed.loss)
+

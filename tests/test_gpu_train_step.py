@@ -227,3 +227,20 @@ def test_c_abi_train_step_equals_the_launch_list(cuda, tuned):
     torch.cuda.synchronize()
     for x, y in zip(a.W, b.W):
         assert torch.equal(x, y)
+
+
+def test_second_stream_keeps_results(cuda):
+    """Each upper layer's gradient + Adam on the second stream gives the weights, transposed weights, Adam
+    moments and losses of the launch list run in order on one stream, bit for bit."""
+    t, n, ws, labels = case(seed=8)
+    one, two = make_step(t, ws, labels), make_step(t, ws, labels)
+    one.aux = None
+    for _ in range(3):
+        one.step()
+        two.step()
+    torch.cuda.synchronize()
+    for name in ("W", "Wt", "m", "v", "grad"):
+        for x, y in zip(getattr(one, name), getattr(two, name)):
+            assert torch.equal(x, y), name
+    assert torch.equal(one.loss, two.loss)
+
