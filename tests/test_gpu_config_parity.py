@@ -172,7 +172,7 @@ def test_train_step_equals_kernel_chain_784_800_800_10_batch_256(cuda, variant):
 def test_uneven_batch_slice_vs_reference_kernels(cuda):
     """The uneven-batch configuration (1024-1024-20, max_n_spike 30, weights U(-1, 1), thresholds 0.2 / 1.3,
     inputs over 1024 channels with lognormal event counts, median 200, 20-4000 per sample, times U(0, 0.1) s) on
-    a slice of 48 samples that spans the whole range of lengths, the longest included: forward bit-identical to
+    a slice of 47 samples at evenly spaced length ranks, the longest included: forward bit-identical to
     the reference kernels with both the per-(tile, sample) and the persistent work-queue forward, and each
     layer's batch-summed gradient and pre-spike errors within 1e-5 |ref| + 1e-5 sum|terms|."""
     if not refkern.available():
