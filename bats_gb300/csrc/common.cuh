@@ -198,14 +198,14 @@ __device__ __forceinline__ bool stage_no_crossing(float amin, float bmax, float 
 // compute_spike_times_conv.cu:59-90 for the conv layer, whose discriminant is evaluated in float
 // instead of double): the FC discriminant through fc_discriminant, which reproduces the reference's
 // double expression without FP64 on its common path, everything else operation for operation.
-template <bool CONV>
-__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_start,
-                                                float e_next,
-                                                const SolveConst& k, int& n, int k_post,
-                                                float* __restrict__ a_out, float* __restrict__ x_out,
-                                                float* __restrict__ t_out, float* __restrict__ z_out) {
+template <bool CONV, typename Screen>
+__device__ __forceinline__ bool solve_crossings_screened(float a, float& b, float last_t, float next_t,
+                                                         Screen no_crossing_here, const SolveConst& k, int& n,
+                                                         int k_post, float* __restrict__ a_out,
+                                                         float* __restrict__ x_out, float* __restrict__ t_out,
+                                                         float* __restrict__ z_out) {
     while (true) {
-        if (no_crossing<CONV>(a, b, e_start, e_next, k)) return false;
+        if (no_crossing_here(a, b)) return false;
         float tmp;
         if (CONV) {
             tmp = b * b - 4 * a * k.c;
@@ -229,6 +229,46 @@ __device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t,
         n++;
         if (n >= k_post) return true;
     }
+}
+
+template <bool CONV>
+__device__ __forceinline__ bool solve_crossings(float a, float& b, float last_t, float next_t, float e_start,
+                                                float e_next, const SolveConst& k, int& n, int k_post,
+                                                float* __restrict__ a_out, float* __restrict__ x_out,
+                                                float* __restrict__ t_out, float* __restrict__ z_out) {
+    return solve_crossings_screened<CONV>(
+        a, b, last_t, next_t, [&](float a_, float b_) { return no_crossing<CONV>(a_, b_, e_start, e_next, k); }, k,
+        n, k_post, a_out, x_out, t_out, z_out);
+}
+
+// The conv form of the right-of-window constants, formed once per staged event (the window that ends at it):
+// Z = min(e_next, e_max)(1 + 1.5 2^-19) and (2c) Z, +inf where the test does not apply (Z >= 2980), by the
+// float operations of no_crossing<true>. no_crossing_conv_at(a, b, conv_window(e_next, k), k) ==
+// no_crossing<true>(a, b, 0, e_next, k) for every a, b.
+__device__ __forceinline__ float2 conv_window(float e_next, const SolveConst& k) {
+    const float Z = fminf(e_next, k.e_max) * (1.0f + 0x1.8p-19f);
+    return make_float2(Z, Z < 2980.0f ? (2.0f * k.c) * Z : BATS_INF);
+}
+__device__ __forceinline__ bool no_crossing_conv_at(float a, float b, float2 zw, const SolveConst& k) {
+    const float ab = fabsf(b);
+    const bool usable = k.fast && ab >= 0x1p-60f && ab <= 0x1p60f && fabsf(a) <= 0x1p60f;
+    const float p_hi = __fmul_rn(__fmul_rn(4.0f, a), k.c);
+    const float B2 = __fmul_rn(b, b);
+    const bool level1 = a <= 0.0f || b < 0.0f || B2 < p_hi;
+    const float q = fmaf(fmaf(k.c, zw.x, -b), zw.x, a);
+    float err = 0x1p-21f * fmaf(fmaf(k.c, zw.x, b), zw.x, a);
+    err = fmaf(0x1p-23f * B2, k.inv_c, err);
+    const bool right_of_window = zw.y < b * (1.0f - 0x1p-21f) && q > err;
+    return usable && (level1 || right_of_window);
+}
+// solve_crossings<true> with the window's constants from conv_window.
+__device__ __forceinline__ bool solve_crossings_conv_at(float a, float& b, float last_t, float next_t, float2 zw,
+                                                        const SolveConst& k, int& n, int k_post,
+                                                        float* __restrict__ a_out, float* __restrict__ x_out,
+                                                        float* __restrict__ t_out, float* __restrict__ z_out) {
+    return solve_crossings_screened<true>(
+        a, b, last_t, next_t, [&](float a_, float b_) { return no_crossing_conv_at(a_, b_, zw, k); }, k, n, k_post,
+        a_out, x_out, t_out, z_out);
 }
 
 // solve_crossings<false> with the event's window constants formed once per stage (event_window).

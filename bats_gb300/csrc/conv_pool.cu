@@ -47,7 +47,8 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ConvEvent* sev = reinterpret_cast<ConvEvent*>(smem_raw);
-    int* swarp = reinterpret_cast<int*>(sev + CONV_CHUNK);
+    float2* szw = reinterpret_cast<float2*>(sev + CONV_CHUNK);  // each kept event's window constants
+    int* swarp = reinterpret_cast<int*>(szw + CONV_CHUNK);
     float* sW = reinterpret_cast<float*>(swarp + 32);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = (blockDim.x + 31) >> 5;
@@ -107,7 +108,11 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
                 if (w < warp) off += swarp[w];
                 tot += swarp[w];
             }
-            if (keep) sev[off + __popc(bal & lanemask_lt())] = ce;
+            if (keep) {
+                const int pos = off + __popc(bal & lanemask_lt());
+                sev[pos] = ce;
+                szw[pos] = conv_window(ce.e, sk);  // the window that ends at this event, once per CTA
+            }
             __syncthreads();
             kept += tot;
         }
@@ -119,7 +124,7 @@ __global__ void conv_forward_kernel(const Event* __restrict__ ev, const int* __r
             const bool in_field = dx >= 0 && dx < fx && dy >= 0 && dy < fy;
             if (!in_field && e.xyc >= 0) continue;  // weight 0 times a finite value
             if (has_prev) {
-                done = solve_crossings<true>(a, b, last_t, e.t, 0.0f, e.e, sk, n, k_post, ao, xo_, to, zo);
+                done = solve_crossings_conv_at(a, b, last_t, e.t, szw[m], sk, n, k_post, ao, xo_, to, zo);
                 if (done) break;
             }
             const float w = in_field ? Wsrc[((co * fx + dx) * fy + dy) * C + ((e.xyc >> 20) & 2047)] : 0.0f;
@@ -526,7 +531,7 @@ extern "C" int bats_conv_forward(const void* events, const int* ev_count, long l
     const int threads = ((TX * TY * C_out + 31) / 32) * 32;
     const int tiles_x = (Xo + TX - 1) / TX, tiles_y = (Yo + TY - 1) / TY;
     const size_t nw = (size_t)C_out * fx * fy * C;
-    const size_t base_smem = bats::CONV_CHUNK * sizeof(bats::ConvEvent) + 32 * sizeof(int);
+    const size_t base_smem = bats::CONV_CHUNK * (sizeof(bats::ConvEvent) + sizeof(float2)) + 32 * sizeof(int);
     const int w_in_smem = (base_smem + nw * sizeof(float)) <= 200 * 1024;
     const size_t smem = base_smem + (w_in_smem ? nw * sizeof(float) : 0);
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_forward_kernel, (int)smem));

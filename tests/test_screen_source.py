@@ -35,7 +35,8 @@ static const uint3 threadIdx = {0, 0, 0};
 // stdin: int32 mode, int64 n, then the fields as float32 arrays of n; stdout: n bytes (0/1).
 // mode 0: no_crossing<FC, left test>(a, b, e_start, e_next; c, e_max); mode 1: the conv form (same fields);
 // mode 2: stage_no_crossing(amin, bmax, amag, a_last, b_last, e_first; c); mode 3: whether no_crossing_at with
-// event_window(e_start, e_next) agrees with no_crossing (bit 0: with the left test, bit 1: without).
+// event_window(e_start, e_next) agrees with no_crossing (bit 0: with the left test, bit 1: without; bit 2: the
+// conv form, no_crossing_conv_at with conv_window(e_next)).
 int main() {
     int mode;
     long long n;
@@ -61,7 +62,10 @@ int main() {
                               bats::no_crossing<false, true>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
             const bool right = bats::no_crossing_at<false>(v[i], v[n + i], w, k) ==
                                bats::no_crossing<false, false>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
-            out[i] = (left ? 1 : 0) | (right ? 2 : 0);
+            // bit 2: the conv form with its window from conv_window(e_next) against no_crossing<true>.
+            const bool conv = bats::no_crossing_conv_at(v[i], v[n + i], bats::conv_window(v[3 * n + i], k), k) ==
+                              bats::no_crossing<true>(v[i], v[n + i], 0.0f, v[3 * n + i], k);
+            out[i] = (left ? 1 : 0) | (right ? 2 : 0) | (conv ? 4 : 0);
             continue;
         }
         if (mode == 0) r = bats::no_crossing<false>(v[i], v[n + i], v[2 * n + i], v[3 * n + i], k);
@@ -163,7 +167,8 @@ def test_event_screen_model_equals_the_device_source(screen_exe, mode):
 def test_precomputed_window_screen_equals_the_event_screen(screen_exe):
     """The forward's tile kernels form each event's window constants once per stage (event_window) and test
     every neuron with no_crossing_at; that must give no_crossing's answer on every input, with and without the
-    left-of-window test, so the kernels' results stay those of the per-event form."""
+    left-of-window test, so the kernels' results stay those of the per-event form. The same for the conv
+    kernel's window constants, formed once per staged event (conv_window, no_crossing_conv_at)."""
     rng = np.random.default_rng(60)
     parts = [_edge_states(rng, 100_000) for _ in range(10)]
     fields = [np.concatenate([p[i] for p in parts]) for i in range(6)]
@@ -174,7 +179,7 @@ def test_precomputed_window_screen_equals_the_event_screen(screen_exe):
     n_all = len(fields[0])
     payload_ok = _run_raw(screen_exe, 3, fields)
     assert payload_ok.size == n_all
-    bad = np.flatnonzero(payload_ok != 3)
+    bad = np.flatnonzero(payload_ok != 7)
     assert bad.size == 0, [(int(payload_ok[i]),) + tuple(float(f[i]) for f in fields) for i in bad[:5]]
 
 

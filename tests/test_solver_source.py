@@ -232,7 +232,8 @@ int main(int argc, char** argv) {
             const bool finite = std::isfinite(es[i]) && std::isfinite(e[i]);
             if (!rel[i] && (finite || old_rule)) continue;
             if (has_prev) {
-                done = bats::solve_crossings<true>(a2, b2, last, t[i], 0.0f, e[i], k, n2, K, ao2, xo2, to2, zo2);
+                done = bats::solve_crossings_conv_at(a2, b2, last, t[i], bats::conv_window(e[i], k), k, n2, K, ao2,
+                                                     xo2, to2, zo2);
                 if (done) break;
             }
             const float wi = rel[i] ? w[i] : 0.0f;
