@@ -333,7 +333,7 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
                              int Xo, int Yo, int k_pre, const float* __restrict__ post_t,
                              const float2* __restrict__ tab, const int* __restrict__ nvalid, int k_post,
                              float tau_s, float tau, long long pre_slots, float* __restrict__ grad,
-                             float* __restrict__ pre_err, int batch, int group) {
+                             float* __restrict__ pre_err, int batch, int group, int w_in_smem) {
     pdl_prologue();
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
@@ -351,6 +351,14 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
     int* kcount = reinterpret_cast<int*>(Gs + total);
     const int n_post = Xo * Yo * C_out;
     for (int q = tid; q < total; q += blockDim.x) Gs[q] = 0.0f;
+    // The filters, for the pre-spike error terms: in shared memory after the counters when they fit (a
+    // thread's weight reads are C floats apart, one cache sector per lane from global memory).
+    const float* Wk = W;
+    if (w_in_smem) {
+        float* sWf = reinterpret_cast<float*>(kcount + C);
+        for (int q = tid; q < total; q += blockDim.x) sWf[q] = W[q];
+        Wk = sWf;
+    }
     // At most one tap per thread here (taps <= blockDim checked by the launcher).
     const int tp = tid;
     const bool has_tap = tp < taps;
@@ -370,11 +378,17 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
         PostCursor cur;
         const long long pn = in ? (long long)s * n_post + (xo * Yo + yo) * C_out + co : 0;
         cur.init(post_t + pn * k_post, tab + pn * (k_post + 1), in ? nvalid[pn] : 0);
-        for (int q = tid; q < C; q += blockDim.x) kcount[q] = 0;
-        __syncthreads();
+        // Two barriers per chunk: after warp 0 stages it (every thread reads it), and after the error terms are in
+        // sred (every thread is done with the chunk's records; the chunk's events then sum the terms). The next
+        // chunk's first barrier orders those sums' reads of sred and sslot before anything overwrites them (warp 0
+        // sums, then stages; the other warps write sred only after that barrier).
         for (int m0 = beg; m0 < end; m0 += 32) {
             const int cnt = min(32, end - m0);
             if (warp == 0) {
+                if (m0 == beg) {  // the position's spike counters per channel: warp 0's alone
+                    for (int q = lane; q < C; q += 32) kcount[q] = 0;
+                    __syncwarp();
+                }
                 // Stage the chunk; the spikes' slots: j * k_pre + the order of appearance of j in the group (all
                 // events of a position share x and y, so j is fixed by the channel: earlier chunks' counts plus
                 // the rank among this chunk's events of the same channel).
@@ -408,7 +422,7 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
                         const int cc = scc[q];
                         Gs[tp * C + cc] += fmaf(e.es, cur.AB.x, -(e.e * cur.AB.y));
                         if (pre_err)
-                            term[q] = W[(long long)tp * C + cc] * (cur.AB.x * e.es * inv_tau_s - cur.AB.y * e.e * inv_tau);
+                            term[q] = Wk[tp * C + cc] * (cur.AB.x * e.es * inv_tau_s - cur.AB.y * e.e * inv_tau);
                     }
                 }
             }
@@ -417,13 +431,12 @@ conv_backward_grouped_kernel(const Event* __restrict__ ev_b, const int* __restri
                 const float v = warp_transpose_reduce<32>(term);
                 sred[lane][warp] = v;
             }
-            __syncthreads();
+            __syncthreads();  // every thread is done with the chunk's records (warp 0 may restage them next)
             if (pre_err && tid < cnt) {
                 float acc = 0.0f;
                 for (int w = 0; w < nwarps; ++w) acc += sred[tid][w];
                 pre_err[(long long)s * pre_slots + sslot[tid]] = acc;
             }
-            __syncthreads();
         }
     }
     }
@@ -610,8 +623,10 @@ extern "C" int bats_conv_backward_grouped(const void* events_bucketed, const int
                  "conv_backward_grouped: needs at most 1024 taps and 255 input positions");
     const int Xo = X - fx + 1, Yo = Y - fy + 1;
     const long long pre_slots = (long long)X * Y * C * k_pre;
-    const size_t smem = (size_t)taps * C * sizeof(float) + (size_t)C * sizeof(int);
-    BATS_REQUIRE(smem <= 160 * 1024, BATS_ERR_BAD_SHAPE, "conv_backward_grouped: filter gradient too large");
+    const size_t gsmem = (size_t)taps * C * sizeof(float) + (size_t)C * sizeof(int);
+    BATS_REQUIRE(gsmem <= 160 * 1024, BATS_ERR_BAD_SHAPE, "conv_backward_grouped: filter gradient too large");
+    const int w_in_smem = pre_errors && gsmem + (size_t)taps * C * sizeof(float) <= 200 * 1024;
+    const size_t smem = gsmem + (w_in_smem ? (size_t)taps * C * sizeof(float) : 0);
     if (pre_errors) BATS_CUDA(cudaMemsetAsync(pre_errors, 0, (size_t)batch * pre_slots * sizeof(float), stream));
     BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_grouped_kernel, (int)smem));
     const int threads = (int)(((taps + 31) / 32) * 32);
@@ -631,7 +646,7 @@ extern "C" int bats_conv_backward_grouped(const void* events_bucketed, const int
                                  reinterpret_cast<const bats::Event*>(events_bucketed), bucket_offsets, X * Y, ev_cap,
                                  weights, Y, C, fx, fy, C_out, Xo, Yo, k_pre, post_times,
                                  reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots,
-                                 grad_per_sample, pre_errors, batch, 1));
+                                 grad_per_sample, pre_errors, batch, 1, w_in_smem));
     return BATS_OK;
 }
 
@@ -696,12 +711,15 @@ extern "C" int bats_conv_backward_adam(const void* events, const int* ev_slot, c
     cfg.attrs = attr;
     cfg.numAttrs = 1 + (unsigned)bats::pdl_attribute(attr + 1);
     if (grouped) {
-        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_grouped_kernel, (int)gbytes));
+        const int w_in_smem = pre_errors && gbytes + (size_t)taps * C * sizeof(float) <= 200 * 1024;
+        if (w_in_smem) cfg.dynamicSmemBytes = gbytes + (size_t)taps * C * sizeof(float);
+        BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_grouped_kernel,
+                                                          (int)cfg.dynamicSmemBytes));
         BATS_CUDA(cudaLaunchKernelEx(&cfg, bats::conv_backward_grouped_kernel,
                                      reinterpret_cast<const bats::Event*>(events_bucketed), bucket_offsets, X * Y,
                                      ev_cap, (const float*)weights, Y, C, fx, fy, C_out, Xo, Yo, k_pre, post_times,
                                      reinterpret_cast<const float2*>(tables), nvalid, k_post, tau_s, tau, pre_slots,
-                                     part, pre_errors, batch, group));
+                                     part, pre_errors, batch, group, w_in_smem));
     } else {
         BATS_CUDA((cudaError_t)bats::max_dynamic_smem_set((const void*)bats::conv_backward_cluster_kernel, (int)gbytes));
         int top = 1;
