@@ -1,7 +1,7 @@
 """Float64 NumPy oracle of the BATS hot path: event-based LIF forward and exact multi-spike backward.
 
-TEST INFRASTRUCTURE ONLY. This module is the checker for the CUDA kernels of bats_gb300 and the
-CPU baseline of bench.py; nothing in the product imports it. It restates the reference's
+TEST INFRASTRUCTURE ONLY. This module is the reference against which the tests check the CUDA kernels of
+bats_gb300, and the CPU baseline of bench.py; nothing in the product imports it. It restates the reference's
 algorithm (Florian-BACHO/bats, CuPy + CUDA) in plain NumPy float64, one function per reference
 kernel, each citing the file:line it follows. Parity is pinned by running the reference's own
 unit tests against these functions (tests/golden/make_golden.py, which imports the reference test

@@ -8,7 +8,7 @@ Perturbations that change any spike count (threshold grazing) are reported as su
 differentiable there. The work is spread over a `spawn` process pool (safe after CUDA has started in
 the parent).
 
-Only the tests call this module; it is a checker, not part of the product path.
+Only the tests call this module; it is test infrastructure, not part of the product path.
 """
 from __future__ import annotations
 

@@ -14,8 +14,8 @@ and then
      known-answer arrays and CPU-loop oracles;
   2. evaluates the tests' CPU-loop oracles (pure NumPy methods of the test classes) on seeded
      inputs of the tests' shapes and saves inputs + expected outputs as .npz fixtures, together
-     with the known-answer arrays the tests hold, for the GPU parity tests (the GPU machine has no
-     reference checkout).
+     with the known-answer arrays the tests hold, for the GPU parity tests (the machines that run them
+     hold no reference checkout).
 Tests that need brian2 (the simulator ground truth) are recorded as skipped; the oracle is
 cross-checked against a fixed-step integrator instead (tests/test_oracle.py).
 """
