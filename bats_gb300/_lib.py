@@ -32,6 +32,9 @@ SIGNATURES = {
                                  c_vp, c_int, c_vp, c_size, c_vp]),
     "bats_sort_events_counted": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_vp, c_vp, c_vp, c_vp,
                                          c_vp, c_vp, c_vp, c_int, c_vp, c_size, c_vp]),
+    "bats_sort_events_counted_ordered": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_float, c_float, c_vp, c_vp,
+                                                 c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_size, c_vp]),
+    "bats_sample_order": (c_int, [c_vp, c_int, c_vp, c_vp]),
     "bats_lif_forward_fc": (c_int, [c_vp, c_vp, c_ll, c_vp, c_int, c_int, c_int, c_int, c_float, c_float, c_float,
                                     c_float, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "bats_lif_forward_fc_default_algo": (c_int, [c_int, c_int, c_int]),

@@ -291,7 +291,8 @@ lif_fc_forward_queue_kernel(const Event* __restrict__ ev, const int* __restrict_
 // Longest-first order of the samples for lif_fc_forward_queue_kernel, and the reset of its queue head. The
 // samples are ranked by descending event count in 512 logarithmic classes (16 per octave: the exponent and
 // top four mantissa bits of the float count + 1); the order inside a class is whatever the atomics give,
-// which changes only the schedule, never a result. One CTA of 1024 threads.
+// which changes only the schedule, never a result. One CTA of 1024 threads. head may be null (bats_sample_order:
+// the order alone, for the sort of the layer's output spikes).
 __device__ __forceinline__ int count_class(int c) {
     const int key = (int)(__float_as_uint((float)(c + 1)) >> 19) - (127 << 4);  // increasing in c, >= 0
     return 511 - min(511, max(0, key));
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(1024) work_order_kernel(const int* __restrict_
     __shared__ int warp_sum[16];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid < 512) off[tid] = 0;
-    if (tid == 0) *head = 0;
+    if (tid == 0 && head) *head = 0;
     __syncthreads();
     for (int s = tid; s < batch; s += blockDim.x) atomicAdd(&off[count_class(ev_count[s])], 1);
     __syncthreads();
@@ -599,6 +600,15 @@ extern "C" int bats_lif_forward_fc_algo(const void* events, const int* ev_count,
                                         cudaStream_t stream) {
     return forward_fc_impl(events, ev_count, ev_cap, weights_t, ld, batch, n_post, k_post, c, delta_theta_tau, tau,
                            max_simulation, n_spikes, a, x, times, post_exp_tau, algo, stream);
+}
+
+extern "C" int bats_sample_order(const int* ev_count, int batch, int* order, cudaStream_t stream) {
+    BATS_REQUIRE(batch >= 0, BATS_ERR_BAD_SHAPE, "sample_order: bad shape");
+    if (batch == 0) return BATS_OK;
+    BATS_REQUIRE(ev_count && order, BATS_ERR_NULL, "sample_order: null pointer");
+    BATS_CUDA(bats::launch(bats::work_order_kernel, 1, 1024, 0, stream, ev_count, batch, (int*)nullptr, order));
+    BATS_CUDA(cudaGetLastError());
+    return BATS_OK;
 }
 
 extern "C" size_t bats_lif_forward_fc_queue_workspace_bytes(int batch) {

@@ -9,8 +9,12 @@
 // The reference sorts every (neuron, slot) of the batch on the device with argpartition after a
 // host sync on the largest spike count; here every sample's valid slots (time < +inf) are
 // compacted and sorted by a stable LSD radix sort in shared memory (8-bit digits, warp ranks
-// from __match_any_sync ballots), so the event list needs no host sync and no padding to the
+// from nine ballots per digit), so the event list needs no host sync and no padding to the
 // batch maximum. Ties keep slot order, which makes the order deterministic.
+//
+// CTA b sorts sample b, or sample sample_order[b] when an order is given (the samples longest first: on a
+// batch of uneven samples wider than the resident CTAs, the long samples then start in the first wave
+// instead of setting the kernel's tail). The order changes the schedule only, never a result.
 //
 // For the backward pass the same kernel can also emit the events grouped by pre-neuron bucket
 // (neuron / bucket_width), each bucket still in time order (one more stable counting pass), with
@@ -121,7 +125,8 @@ __device__ __forceinline__ void scan_bins(SortShared<T>& sh) {
 
 // One stable counting pass (digit < 256) of n (key, val) pairs from (ka, va) into (kb, vb), using the
 // bin bases already in sh.base. Items are ranked in rounds of T in their current order; inside a warp,
-// items of equal digit are ranked by __match_any_sync, across warps by a per-digit scan.
+// items of equal digit are ranked by their peer mask (the AND of nine ballots, one per bit of the digit or
+// the out-of-range 256: faster here than __match_any_sync), across warps by a per-digit scan.
 template <int T, typename V, typename DigitFn>
 __device__ __forceinline__ void stable_pass(const uint32_t* ka, const V* va, uint32_t* kb, V* vb, int n,
                                             SortShared<T>& sh, DigitFn digit) {
@@ -137,7 +142,13 @@ __device__ __forceinline__ void stable_pass(const uint32_t* ka, const V* va, uin
             val = va[i];
             d = digit(key, (uint32_t)val);
         }
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        unsigned peers = 0xffffffffu;
+#pragma unroll
+        for (int bit = 0; bit < 9; ++bit) {
+            const bool on = (d >> bit) & 1;
+            const unsigned bal = __ballot_sync(0xffffffffu, on);
+            peers &= on ? bal : ~bal;
+        }
         const int rank = __popc(peers & lanemask_lt());
         if (valid && rank == 0) sh.wcnt[warp][d] = __popc(peers);
         __syncthreads();
@@ -161,12 +172,19 @@ __device__ __forceinline__ void stable_pass(const uint32_t* ka, const V* va, uin
     __syncthreads();
 }
 
-// Valid (finite) times among the first pre_counts[j] slots of pre neuron j.
+// Valid (finite) times among the first pre_counts[j] slots of pre neuron j (loads eight at a time, so that a
+// thread's scattered loads are in flight together).
 __device__ __forceinline__ int leading_valid(const int* cnt_src, const float* tsrc, int j, int k_pre) {
     const int c = min(max(cnt_src[j], 0), k_pre);
     const float* tj = tsrc + (long long)j * k_pre;
     int v = 0;
-    for (int q = 0; q < c; ++q) v += tj[q] < BATS_INF;
+    for (int q0 = 0; q0 < c; q0 += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + u;
+            if (q < c) v += tj[q] < BATS_INF;
+        }
+    }
     return v;
 }
 
@@ -202,14 +220,15 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
                    const float* __restrict__ exp_s_in, const float* __restrict__ exp_in, Event* __restrict__ ev_out,
                    int* __restrict__ slot_out, int* __restrict__ ev_count, Event* __restrict__ ev_bucketed,
                    int* __restrict__ bucket_off, int bucket_width, int n_buckets, long long cap, int smem_cap,
-                   unsigned char* __restrict__ scratch) {
+                   unsigned char* __restrict__ scratch, const int* __restrict__ sample_order) {
     pdl_prologue();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int SORT_THREADS = T, SORT_WARPS = T / 32;
     SortShared<T>& sh = *reinterpret_cast<SortShared<T>*>(smem_raw);
     unsigned char* smem_items = smem_raw + sizeof(SortShared<T>);
 
-    const int s = blockIdx.x;
+    const int s = sample_order ? __ldg(sample_order + blockIdx.x) : (int)blockIdx.x;
+    if ((unsigned)s >= gridDim.x) return;  // not a sample of the batch: the order is not a permutation
     const int tid = threadIdx.x;
     const long long sample_off = (long long)s * n_slots;
     const float* tsrc = times + sample_off;
@@ -284,12 +303,17 @@ sort_events_kernel(const float* __restrict__ times, const int* __restrict__ pre_
             int pos = base + block_exclusive_scan(c, sh, tot);
             const int slot0 = j * k_pre;
             const int lim = c > 0 ? min(max(cnt_src[j], 0), k_pre) : 0;
-            for (int q = 0; q < lim; ++q) {
-                const float t = tsrc[slot0 + q];
-                if (t < BATS_INF) {
-                    ka[pos] = float_to_key(t);
-                    va[pos] = (V)(slot0 + q);
-                    ++pos;
+            for (int q0 = 0; q0 < lim; q0 += 8) {
+                float tv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) tv[u] = q0 + u < lim ? tsrc[slot0 + q0 + u] : BATS_INF;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    if (tv[u] < BATS_INF) {
+                        ka[pos] = float_to_key(tv[u]);
+                        va[pos] = (V)(slot0 + q0 + u);
+                        ++pos;
+                    }
                 }
             }
             base += tot;
@@ -431,22 +455,24 @@ template <typename V, int T>
 static cudaError_t launch_sort(const float* pre_times, const int* pre_counts, int batch, long long cap, int k_pre,
                                float tau_s, float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out,
                                int* slot_out, int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
-                               int n_buckets, int smem_cap, unsigned char* scratch, cudaStream_t stream) {
+                               int n_buckets, int smem_cap, unsigned char* scratch, const int* sample_order,
+                               cudaStream_t stream) {
     const size_t smem = sizeof(bats::SortShared<T>) + (size_t)smem_cap * (8 + 2 * sizeof(V));
     cudaError_t e = (cudaError_t)bats::max_dynamic_smem_set((const void*)bats::sort_events_kernel<V, T>, (int)smem);
     if (e != cudaSuccess) return e;
     return bats::launch(bats::sort_events_kernel<V, T>, batch, T, smem, stream, pre_times, pre_counts, (int)cap, k_pre,
                         tau_s, tau, exp_tau_s, exp_tau, reinterpret_cast<bats::Event*>(ev_out), slot_out, ev_count,
                         reinterpret_cast<bats::Event*>(ev_bucketed), bucket_offsets, bucket_width, n_buckets, cap,
-                        smem_cap, scratch);
+                        smem_cap, scratch, sample_order);
 }
 #define SORT_ARGS pre_times, pre_counts, batch, cap, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out, slot_out, \
-                  ev_count, ev_bucketed, bucket_offsets, bucket_width, n_buckets, smem_cap, scratch, stream
+                  ev_count, ev_bucketed, bucket_offsets, bucket_width, n_buckets, smem_cap, scratch, sample_order, \
+                  stream
 
 static int sort_events_impl(const float* pre_times, const int* pre_counts, int batch, int n_pre, int k_pre,
                             float tau_s, float tau, const float* exp_tau_s, const float* exp_tau, void* ev_out,
                             int* slot_out, int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
-                            void* workspace, size_t workspace_bytes, cudaStream_t stream) {
+                            const int* sample_order, void* workspace, size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(batch >= 0 && n_pre >= 0 && k_pre > 0, BATS_ERR_BAD_SHAPE, "sort_events: bad shape");
     if (batch == 0) return BATS_OK;
     BATS_REQUIRE(pre_times && ev_out && ev_count, BATS_ERR_NULL, "sort_events: null pointer");
@@ -482,7 +508,8 @@ extern "C" int bats_sort_events(const float* pre_times, int batch, int n_pre, in
                                 int* ev_count, void* ev_bucketed, int* bucket_offsets, int bucket_width,
                                 void* workspace, size_t workspace_bytes, cudaStream_t stream) {
     return sort_events_impl(pre_times, nullptr, batch, n_pre, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out, slot_out,
-                            ev_count, ev_bucketed, bucket_offsets, bucket_width, workspace, workspace_bytes, stream);
+                            ev_count, ev_bucketed, bucket_offsets, bucket_width, nullptr, workspace, workspace_bytes,
+                            stream);
 }
 
 extern "C" int bats_sort_events_counted(const float* pre_times, const int* pre_counts, int batch, int n_pre,
@@ -492,6 +519,19 @@ extern "C" int bats_sort_events_counted(const float* pre_times, const int* pre_c
                                         size_t workspace_bytes, cudaStream_t stream) {
     BATS_REQUIRE(pre_counts || batch == 0, BATS_ERR_NULL, "sort_events_counted: null pre_counts");
     return sort_events_impl(pre_times, pre_counts, batch, n_pre, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out,
-                            slot_out, ev_count, ev_bucketed, bucket_offsets, bucket_width, workspace, workspace_bytes,
-                            stream);
+                            slot_out, ev_count, ev_bucketed, bucket_offsets, bucket_width, nullptr, workspace,
+                            workspace_bytes, stream);
+}
+
+extern "C" int bats_sort_events_counted_ordered(const float* pre_times, const int* pre_counts, int batch, int n_pre,
+                                                int k_pre, float tau_s, float tau, const float* exp_tau_s,
+                                                const float* exp_tau, void* ev_out, int* slot_out, int* ev_count,
+                                                void* ev_bucketed, int* bucket_offsets, int bucket_width,
+                                                const int* sample_order, void* workspace, size_t workspace_bytes,
+                                                cudaStream_t stream) {
+    BATS_REQUIRE(pre_counts || batch == 0, BATS_ERR_NULL, "sort_events_counted_ordered: null pre_counts");
+    BATS_REQUIRE(sample_order || batch == 0, BATS_ERR_NULL, "sort_events_counted_ordered: null sample_order");
+    return sort_events_impl(pre_times, pre_counts, batch, n_pre, k_pre, tau_s, tau, exp_tau_s, exp_tau, ev_out,
+                            slot_out, ev_count, ev_bucketed, bucket_offsets, bucket_width, sample_order, workspace,
+                            workspace_bytes, stream);
 }

@@ -104,12 +104,31 @@ def alloc_events(batch: int, n_neurons: int, k: int, device="cuda", bucketed: bo
     return ev
 
 
+def sample_order(ev_count) -> torch.Tensor:
+    """The samples longest first by their event counts ev_count (B,) int32 (bats_sample_order), as an int32
+    permutation of 0 .. B-1 on ev_count's device."""
+    c = _c(ev_count, I32)
+    order = torch.empty(c.shape[0], dtype=I32, device=c.device)
+    call("bats_sample_order", ptr(c), c.shape[0], ptr(order), stream_ptr())
+    return order
+
+
+def order_pays(batch: int, device) -> bool:
+    """Whether a longest-first sample order can shorten a one-CTA-per-sample launch of the counted sort:
+    only when the batch is wider than its resident CTAs (two per SM)."""
+    if not torch.cuda.is_available():
+        return batch > 2 * 152
+    return batch > 2 * torch.cuda.get_device_properties(device).multi_processor_count
+
+
 def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=None, out: Events | None = None,
-                bucketed: bool = True, bucket_width: int = BUCKET_WIDTH, pre_counts=None):
+                bucketed: bool = True, bucket_width: int = BUCKET_WIDTH, pre_counts=None, sample_order=None):
     """Per-sample time sort of all valid pre-spikes (replaces get_sorted_spikes_indices, the
     take_along_axis gathers and compute_pre_exps; bats/Layers/LIFLayer.py:66-84). With `bucketed`, also
     the bucketed copy used by the weight gradient. `pre_counts` (B, N) int32, the spike counts of a LIF
-    layer's output (slots past each count are +inf), lets the sort read only the slots below the counts."""
+    layer's output (slots past each count are +inf), lets the sort read only the slots below the counts;
+    with it, `sample_order` (B,) int32, a permutation of the samples (sample_order above), sets the order in
+    which the sort's CTAs take them (the results do not depend on it)."""
     t = _c(spike_times)
     B, N, K = t.shape
     if out is None:
@@ -121,10 +140,18 @@ def sort_events(spike_times, tau_s: float, tau: float, exp_tau_s=None, exp_tau=N
     if pre_counts is not None:
         pc = _c(pre_counts, I32)
         assert tuple(pc.shape) == (B, N), "pre_counts must be (B, N)"
+        if sample_order is not None:
+            so = _c(sample_order, I32)
+            assert tuple(so.shape) == (B,), "sample_order must be (B,)"
+            call("bats_sort_events_counted_ordered", ptr(t), ptr(pc), B, N, K, float(tau_s), float(tau), ptr(es),
+                 ptr(ee), ptr(out.events), ptr(out.slots), ptr(out.counts), ptr(out.bucketed),
+                 ptr(out.bucket_offsets), out.bucket_width, ptr(so), ptr(ws), ws_bytes, stream_ptr())
+            return out
         call("bats_sort_events_counted", ptr(t), ptr(pc), B, N, K, float(tau_s), float(tau), ptr(es), ptr(ee),
              ptr(out.events), ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets),
              out.bucket_width, ptr(ws), ws_bytes, stream_ptr())
         return out
+    assert sample_order is None, "sample_order needs pre_counts"
     call("bats_sort_events", ptr(t), B, N, K, float(tau_s), float(tau), ptr(es), ptr(ee), ptr(out.events),
          ptr(out.slots), ptr(out.counts), ptr(out.bucketed), ptr(out.bucket_offsets), out.bucket_width, ptr(ws),
          ws_bytes, stream_ptr())

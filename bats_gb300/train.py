@@ -86,6 +86,11 @@ class FCTrainStep:
                      K.call_size("bats_pre_errors_workspace_bytes", B, n_prev * k_prev, spec.n_neurons))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
         self.ws = torch.empty(max(ws, 256), dtype=torch.uint8, device=dev)
+        # Batches wider than the sort's resident CTAs sort each hidden layer's spikes with the samples longest
+        # first: a sample's input event count ranks its output spike count closely (the order of the work-queue
+        # forward), so the long samples start in the first wave instead of setting the launch's tail.
+        self.order = [torch.empty(B, dtype=i32, device=dev) if li > 0 and K.order_pays(B, dev) else None
+                      for li in range(len(self.specs))]
         # The gradient + Adam of every layer above the first runs on a second stream, beside the pre-spike
         # errors that read the layer's old transposed weights: it writes the new ones into a staging copy
         # (copied over Wt at the end of the step) and uses its own workspace (as large as the first, so that
@@ -132,12 +137,20 @@ class FCTrainStep:
                     "bats_sort_events", pt, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)), float(tau32),
                     None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed),
                     ptr(ev.bucket_offsets), K.BUCKET_WIDTH, ws, wsb, s)))
-            else:  # a LIF layer's output: only the slots below its spike counts
+            elif self.order[li] is None:  # a LIF layer's output: only the slots below its spike counts
                 L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), pc=ptr(pre_counts), ev=ev, spec=spec,
                           tau32=tau32: call(
                     "bats_sort_events_counted", pt, pc, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)),
                     float(tau32), None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed),
                     ptr(ev.bucket_offsets), K.BUCKET_WIDTH, ws, wsb, s)))
+            else:  # the same with the samples longest first, ranked by the previous layer's input event counts
+                L.append((f"{tag}.order", lambda s, c=ptr(self.ev[li - 1].counts), o=ptr(self.order[li]): call(
+                    "bats_sample_order", c, B, o, s)))
+                L.append((f"{tag}.sort", lambda s, pt=ptr(pre_times), pc=ptr(pre_counts), ev=ev, spec=spec,
+                          tau32=tau32, o=ptr(self.order[li]): call(
+                    "bats_sort_events_counted_ordered", pt, pc, B, ev.n_neurons, ev.k, float(np.float32(spec.tau_s)),
+                    float(tau32), None, None, ptr(ev.events), ptr(ev.slots), ptr(ev.counts), ptr(ev.bucketed),
+                    ptr(ev.bucket_offsets), K.BUCKET_WIDTH, o, ws, wsb, s)))
             n, a, x, t, z = self.out[li]
             L.append((f"{tag}.forward", lambda s, ev=ev, li=li, spec=spec, c=c, dtt=dtt, tau32=tau32, o=self.out[li]:
                       K.forward_fc_call(ev, self.Wt[li], spec.n_neurons, spec.max_n_spike, c, dtt, tau32,
@@ -264,7 +277,7 @@ class FCTrainStep:
             groups = -(-self.B // self.groups[li])  # several partials the reduction and the tiled Adam
             tiles = -(-n_pre // 32) * -(-spec.n_neurons // 32)
             return 3 if groups > 1 and tiles < 2 * 152 else 2
-        return 1  # sort, loss, prep, powers
+        return 1  # sort, order, loss, prep, powers
 
     def _count_launches(self):
         return sum(self._kernels_of(name) for name, _ in self.launches)

@@ -261,12 +261,17 @@ def build_train_step(variant, graph=True):
     return ts
 
 
-def kernel_breakdown(ts):
-    """Device time of each launch of one step (CUDA events around every launch)."""
+def kernel_breakdown(ts, reps=5):
+    """Device time of each launch of a step (CUDA events around every launch): the median over `reps` eager
+    steps, so that one slow launch does not pick the dominant kernel."""
     import torch
-    rec = ts.profile_step()
-    torch.cuda.synchronize()
-    return {k: s.elapsed_time(e) for k, (s, e) in rec.items()}
+    acc = {}
+    for _ in range(reps):
+        rec = ts.profile_step()
+        torch.cuda.synchronize()
+        for k, (s, e) in rec.items():
+            acc.setdefault(k, []).append(s.elapsed_time(e))
+    return {k: float(np.median(v)) for k, v in acc.items()}
 
 
 def spike_counts(ts):
@@ -425,7 +430,8 @@ def profile_kernels():
     API (per-sample gradients, Adam deltas), the conv train step (batch 128), and one call of each other
     entry point: pre-exponentials, the intensity encoder, event-list conversion of a 16-request serving
     batch, the TTFS and spike-time losses, untiled Adam, NAdam, both synaptic-scaling regularizers,
-    transpose, add_deltas, the generic backward prep (reset errors, factors), the conv backward for filters
+    transpose, add_deltas, the generic backward prep (reset errors, factors), the longest-first sample order
+    and the counted sort that takes it, the conv backward for filters
     too large for shared memory, the allocation-free gradient, and one 16-request batch of the serving loop
     (700-512-512-20 network, one foreign call: conversion, then per layer the sort and the forward)."""
     import ctypes
@@ -483,6 +489,12 @@ def profile_kernels():
     t1, a1, x1, z1 = (o.clone() for o in ts.out[0][1:])  # the padded first hidden layer after a step
     calls.append(("propagate_recurrent_errors", lambda: K.propagate_recurrent_errors(x1, z1, errs, dtt)))
     calls.append(("compute_factors", lambda: K.compute_factors(t1, a1, c, x1, z1, tau32)))
+    # The longest-first sample order and the ordered counted sort (the step uses them on wider batches).
+    so = K.sample_order(ts.ev[0].counts)
+    n1, h1 = ts.out[0][0].clone(), ts.out[0][3].clone()  # the first hidden layer's spike counts and times
+    calls.append(("sample_order", lambda: K.sample_order(ts.ev[0].counts)))
+    calls.append(("sort_events_counted_ordered", lambda: K.sort_events(h1, TAU_S, tau, pre_counts=n1,
+                                                                         sample_order=so)))
     # A conv layer whose per-sample filter gradient (128 x 5 x 5 x 15 floats) exceeds shared memory.
     ct = np.full((32, 12 * 12 * 15, 4), np.inf, np.float32)
     nf = rng.integers(0, 5, ct.shape[:2])
@@ -828,11 +840,10 @@ def conv_bench(steps: int = 5):
     ts = conv_train_step(t, labels)
     graphed = ts.try_capture()
     ms, _ = time_steps(ts.replay if graphed else ts.step, steps, 3, flush)
-    rec = ts.profile_step()
-    torch.cuda.synchronize()
+    kb = kernel_breakdown(ts)
     res = {"value": Bc * steps / (ms / 1e3), "unit": "samples/s", "ms_per_step": ms / steps, "steps": steps,
            "batch": Bc, "graph": graphed, "spikes_per_layer": spikes,
-           "kernels_ms": {k: round(a.elapsed_time(b), 4) for k, (a, b) in rec.items()},
+           "kernels_ms": {k: round(v, 4) for k, v in kb.items()},
            "network": "28x28x1 -> conv 5x5x15 -> pool -> conv 5x5x40 -> pool -> 300 -> 10, K 10",
            "what": "ConvTrainStep: batch-reduced filter gradients fused with Adam, whole step as one CUDA graph",
            "plain_api": {"value": Bc * steps / (ms_api / 1e3), "unit": "samples/s", "ms_per_step": ms_api / steps,

@@ -82,6 +82,23 @@ int bats_sort_events_counted(const float* pre_times, const int* pre_counts, int 
                              int* slot_out, int* ev_count, void* events_bucketed, int* bucket_offsets,
                              int bucket_width, void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+/* bats_sort_events_counted with the samples taken in the order sample_order (B ints, a permutation of
+ * 0 .. B-1): the sort's CTA b works on sample sample_order[b]. The outputs are identical for every order;
+ * longest samples first (bats_sample_order) shortens the launch on batches of uneven samples wider than the
+ * sort's resident CTAs (two per SM). An entry outside [0, B) leaves its CTA idle. No reference counterpart:
+ * the reference sorts the whole batch in one library call. */
+int bats_sort_events_counted_ordered(const float* pre_times, const int* pre_counts, int batch, int n_pre,
+                                     int k_pre, float tau_s, float tau, const float* exp_tau_s, const float* exp_tau,
+                                     void* events, int* slot_out, int* ev_count, void* events_bucketed,
+                                     int* bucket_offsets, int bucket_width, const int* sample_order, void* workspace,
+                                     size_t workspace_bytes, cudaStream_t stream);
+
+/* The samples ranked longest first by ev_count (B), into order (B ints): by descending count in logarithmic
+ * classes (16 per octave), the order inside a class unspecified. One CTA; the order of the work-queue
+ * forward (bats_lif_forward_fc_queue). Given the per-sample event counts of a layer's input, it is a close
+ * guess of the order of the layer's output spike counts, for bats_sort_events_counted_ordered. */
+int bats_sample_order(const int* ev_count, int batch, int* order, cudaStream_t stream);
+
 /* Fully-connected LIF forward: spike counts (B, N_post) and a, x, times, post_exp_tau (B, N_post, K_post);
  * times/post_exp_tau are +inf after the spikes, a/x are undefined there. c = theta/tau,
  * delta_theta_tau = delta_theta/tau. Replaces get_spike_weights + compute_spike_times

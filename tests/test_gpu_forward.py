@@ -246,6 +246,42 @@ def test_sort_events_counted_matches_full_scan(cuda, case):
     _events_equal(full, part, case)
 
 
+def _count_class(c):
+    """The logarithmic size class of bats_sample_order (16 per octave, 0 for the longest samples)."""
+    key = (np.float32(c + 1).reshape(-1).view(np.uint32) >> 19).astype(np.int64) - (127 << 4)
+    return 511 - np.clip(key, 0, 511)
+
+
+def test_sort_events_counted_ordered_matches_unordered(cuda):
+    """The counted sort with its CTAs taking the samples in a given order (longest first from
+    bats_sample_order, or a random permutation) returns the events, slots, counts and bucketed copy of the
+    unordered sort, on a batch of 400 uneven samples (wider than the resident CTAs), some above the
+    shared-memory capacity (the global-memory path), some empty; bats_sample_order ranks the samples by
+    descending size class."""
+    rng = np.random.default_rng(33)
+    B, N, Kp = 400, 700, 12
+    times = np.sort(rng.uniform(0, 1, (B, N, Kp)).astype(np.float32), axis=2)
+    per_sample = np.minimum(Kp, rng.lognormal(0.5, 0.9, B)).astype(np.float32)
+    counts = np.minimum(Kp, rng.poisson(per_sample[:, None], (B, N))).astype(np.int32)
+    counts[:5] = Kp        # 8400 events: the global-memory path
+    counts[5:9] = 0        # empty samples
+    times[np.arange(Kp)[None, None, :] >= counts[:, :, None]] = np.inf
+    tt = torch.tensor(times, device="cuda")
+    tc = torch.tensor(counts, device="cuda")
+    plain = K.sort_events(tt, np.float32(0.1), np.float32(0.2), pre_counts=tc)
+    order = K.sample_order(plain.counts)
+    perm = torch.tensor(rng.permutation(B).astype(np.int32), device="cuda")
+    for what, so in (("longest first", order), ("random", perm)):
+        got = K.sort_events(tt, np.float32(0.1), np.float32(0.2), pre_counts=tc, sample_order=so)
+        torch.cuda.synchronize()
+        _events_equal(plain, got, what)
+    o = order.cpu().numpy()
+    assert np.array_equal(np.sort(o), np.arange(B))
+    cls = _count_class(plain.counts.cpu().numpy()[o])
+    assert (np.diff(cls) >= 0).all()
+    assert set(o[:5].tolist()) == set(range(5))
+
+
 def test_edge_cases(cuda):
     rng = np.random.default_rng(9)
     W = rng.uniform(-1, 1, (37, 20)).astype(np.float32)

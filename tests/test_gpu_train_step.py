@@ -244,3 +244,24 @@ def test_second_stream_keeps_results(cuda):
             assert torch.equal(x, y), name
     assert torch.equal(one.loss, two.loss)
 
+
+
+def test_longest_first_sort_keeps_results(cuda):
+    """A batch wider than the sort's resident CTAs sorts the hidden layer's spikes with the samples longest
+    first (an order launch before the second layer's sort); the weights, moments and losses are those of the
+    same step without the order, bit for bit."""
+    B = 2 * torch.cuda.get_device_properties(0).multi_processor_count + 16
+    t, n, ws, labels = case(B=B, seed=9)
+    plain, ordered = make_step(t, ws, labels), make_step(t, ws, labels)
+    assert ordered.order[1] is not None and "L2.order" in [name for name, _ in ordered.launches]
+    plain.order = [None] * len(plain.order)
+    plain.launches = plain._build_launches()
+    assert "L2.order" not in [name for name, _ in plain.launches]
+    for _ in range(3):
+        plain.step()
+        ordered.step()
+    torch.cuda.synchronize()
+    for name in ("W", "Wt", "m", "v", "grad"):
+        for x, y in zip(getattr(plain, name), getattr(ordered, name)):
+            assert torch.equal(x, y), name
+    assert torch.equal(plain.loss, ordered.loss)
