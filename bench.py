@@ -162,7 +162,8 @@ def batching_cpu_baseline(budget_s=12.0, cores=None, stride=32):
 # GPU helpers
 
 class ClockSampler:
-    """nvidia-smi SM clock / throttle sampling during the timed region. The samples go to
+    """nvidia-smi SM clock / throttle sampling (every 50 ms) during the timed region, which starts after the
+    sampler's first sample; that sample is left out of the summary unless it is the only one. The samples go to
     clocks_<pid>.csv in BATS_GB300_CLOCKS_DIR (default: the system's temporary directory)."""
 
     def __init__(self, index=0):
@@ -180,10 +181,20 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return self
+        # nvidia-smi takes a while to start: wait (at most 5 s) for its first sample, so that the timed region
+        # that follows is sampled from its start.
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            self.f.flush()
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
+        self.skip = 1 if os.path.getsize(self.path) > 0 else 0  # that first sample predates the timed region
         return self
 
     def __exit__(self, *exc):
@@ -199,6 +210,7 @@ class ClockSampler:
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.count(",") >= 8]
+        rows = rows[getattr(self, "skip", 0):] or rows
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = [float(r[1]) for r in rows]
