@@ -1,9 +1,10 @@
 // One training step of a fully-connected network in a single call (bats_fc_train_step), for callers that
 // train through the C ABI instead of the Python layer classes. It enqueues, on one stream and with no host
 // synchronisation, exactly the entry-point sequence of the Python train step (bats_gb300/train.py,
-// FCTrainStep._build_launches): Adam's powers, per layer the sort and the forward, the loss, then per layer
-// from the last one the reset-error/factor/table pass, the pre-spike errors and the fused batch-mean
-// gradient + Adam update. Same calls, same arguments, so the results are bit-identical to that sequence.
+// FCTrainStep._build_launches): Adam's powers, per layer the sort (the hidden layers' sorts with the samples
+// longest first on batches wider than two CTAs per SM) and the forward, the loss, then per layer from the last
+// one the reset-error/factor/table pass, the pre-spike errors and the fused batch-mean gradient + Adam update.
+// Same calls, same arguments, so the results are bit-identical to that sequence.
 // Reference counterpart: the training iteration of experiments/mnist/train_spike_count.py:143-177.
 #include <algorithm>
 #include "abi_util.h"
@@ -24,6 +25,17 @@ int pad_flag(const BatsFcTrainLayer* layers, int n_layers, int l) {
     return (l + 1 == n_layers || layers[l].fwd.k_post > 32) ? 0 : BATS_FWD_NO_PAD;
 }
 
+// The sample order of the hidden layers' sorts at the workspace's start (its own 256-byte lines; the calls
+// share the rest), used when the batch is wider than the sort's resident CTAs (two per SM), as in the Python step.
+size_t order_bytes(int batch) { return ((size_t)(batch > 0 ? batch : 0) * sizeof(int) + 255) / 256 * 256; }
+bool order_pays(int batch) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return false;
+    return batch > 2 * sms;
+}
+
 }  // namespace
 
 extern "C" size_t bats_fc_train_step_workspace_bytes(int batch, const BatsFcTrainLayer* layers, int n_layers) {
@@ -36,7 +48,7 @@ extern "C" size_t bats_fc_train_step_workspace_bytes(int batch, const BatsFcTrai
         ws = std::max(ws, bats_weights_gradient_workspace_bytes(batch, F.n_post, F.n_pre, layers[l].grad_group));
         ws = std::max(ws, bats_pre_errors_workspace_bytes(batch, (long long)F.n_pre * F.k_pre, F.n_post));
     }
-    return ws;
+    return order_bytes(batch) + ws;
 }
 
 extern "C" int bats_fc_train_step(const float* in_times, const int* labels, int batch, BatsFcTrainLayer* layers,
@@ -59,6 +71,10 @@ extern "C" int bats_fc_train_step(const float* in_times, const int* labels, int 
     }
     BATS_REQUIRE(workspace_bytes >= bats_fc_train_step_workspace_bytes(batch, layers, n_layers), BATS_ERR_WORKSPACE,
                  "fc_train_step: workspace too small (bats_fc_train_step_workspace_bytes)");
+    int* order = reinterpret_cast<int*>(workspace);
+    const bool ordered = order_pays(batch);
+    workspace = reinterpret_cast<char*>(workspace) + order_bytes(batch);
+    workspace_bytes -= order_bytes(batch);
     int rc = bats_adam_powers_advance(powers, beta_1, beta_2, stream);
     if (rc != BATS_OK) return rc;
     // Forward.
@@ -69,11 +85,19 @@ extern "C" int bats_fc_train_step(const float* in_times, const int* labels, int 
             rc = bats_sort_events(in_times, batch, F.n_pre, F.k_pre, F.tau_s, F.tau, nullptr, nullptr, F.events,
                                   F.slots, F.ev_count, L.events_bucketed, L.bucket_offsets, TRAIN_BUCKET_WIDTH,
                                   workspace, workspace_bytes, stream);
-        else
+        else if (!ordered)
             rc = bats_sort_events_counted(layers[l - 1].fwd.times, layers[l - 1].fwd.n_spikes, batch, F.n_pre,
                                           F.k_pre, F.tau_s, F.tau, nullptr, nullptr, F.events, F.slots, F.ev_count,
                                           L.events_bucketed, L.bucket_offsets, TRAIN_BUCKET_WIDTH, workspace,
                                           workspace_bytes, stream);
+        else {  // the samples longest first, ranked by the previous layer's input event counts
+            rc = bats_sample_order(layers[l - 1].fwd.ev_count, batch, order, stream);
+            if (rc != BATS_OK) return rc;
+            rc = bats_sort_events_counted_ordered(layers[l - 1].fwd.times, layers[l - 1].fwd.n_spikes, batch,
+                                                  F.n_pre, F.k_pre, F.tau_s, F.tau, nullptr, nullptr, F.events,
+                                                  F.slots, F.ev_count, L.events_bucketed, L.bucket_offsets,
+                                                  TRAIN_BUCKET_WIDTH, order, workspace, workspace_bytes, stream);
+        }
         if (rc != BATS_OK) return rc;
         const long long cap = (long long)F.n_pre * F.k_pre;
         const int algo = F.algo | pad_flag(layers, n_layers, l);

@@ -85,7 +85,9 @@ class FCTrainStep:
                      K.call_size("bats_weights_gradient_workspace_bytes", B, spec.n_neurons, n_prev, grp),
                      K.call_size("bats_pre_errors_workspace_bytes", B, n_prev * k_prev, spec.n_neurons))
             n_prev, k_prev = spec.n_neurons, spec.max_n_spike
-        self.ws = torch.empty(max(ws, 256), dtype=torch.uint8, device=dev)
+        # (bats_fc_train_step, native_step, keeps its sample order in front of the same workspaces: B ints in
+        # 256-byte lines)
+        self.ws = torch.empty(max(ws, 256) + -(-B * 4 // 256) * 256, dtype=torch.uint8, device=dev)
         # Batches wider than the sort's resident CTAs sort each hidden layer's spikes with the samples longest
         # first: a sample's input event count ranks its output spike count closely (the order of the work-queue
         # forward), so the long samples start in the first wave instead of setting the launch's tail.

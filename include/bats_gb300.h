@@ -473,15 +473,16 @@ typedef struct BatsFcTrainLayer {
     int grad_group;
 } BatsFcTrainLayer;
 
-/* Workspace of bats_fc_train_step: the largest of the sort, work-queue, gradient and pre-error workspaces of
- * its layers. */
+/* Workspace of bats_fc_train_step: the sample order of the hidden layers' sorts (batch ints, rounded up to 256
+ * bytes), then the largest of the sort, work-queue, gradient and pre-error workspaces of its layers. */
 size_t bats_fc_train_step_workspace_bytes(int batch, const BatsFcTrainLayer* layers, int n_layers);
 
 /* One training step of a fully-connected network on device-resident inputs, enqueued on `stream` with no host
  * synchronisation and no allocation, so that it can be called from any language through this ABI (and
  * captured in a CUDA graph): Adam's bias-correction powers advanced on the device (`powers`: 4 doubles,
- * {1, 1, 0, 0} before the first step); per layer the event sort (bucketed copy included) and the LIF forward
- * (hidden layers unpadded); the spike-count class loss (targets target_true / target_false, per-sample loss
+ * {1, 1, 0, 0} before the first step); per layer the event sort (bucketed copy included; on batches wider than
+ * two CTAs per SM the hidden layers' sorts take the samples longest first, bats_sample_order of the previous
+ * layer's input event counts) and the LIF forward (hidden layers unpadded); the spike-count class loss (targets target_true / target_false, per-sample loss
  * (batch) and output-layer errors (batch, n_out, k_out)); then per layer from the last one the reset errors,
  * factors and suffix tables, the pre-spike errors (every layer but the first, with the weights before this
  * step's update) and the batch-mean gradient fused with Adam (weights, their transposed copy, m, v, grad).

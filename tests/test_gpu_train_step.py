@@ -194,14 +194,17 @@ def test_programmatic_dependent_launch_keeps_results(cuda, tmp_path):
         assert np.array_equal(w.cpu().numpy().view(np.uint32), pdl[f"arr_{q}"].view(np.uint32)), f"layer {q}"
 
 
-@pytest.mark.parametrize("tuned", [False, True])
-def test_c_abi_train_step_equals_the_launch_list(cuda, tuned):
+@pytest.mark.parametrize("tuned,wide", [(False, False), (True, False), (False, True)])
+def test_c_abi_train_step_equals_the_launch_list(cuda, tuned, wide):
     """bats_fc_train_step (the whole train step as one call of the C ABI, for foreign callers) enqueues the same
     entry points with the same arguments as FCTrainStep's launch list: after two steps the weights, their
     transposed copies, Adam's moments, the gradients and the losses are bit-identical; with the autotuner's
-    variants (work-queue forward, other gradient groups) too, and the call can be captured in a CUDA graph."""
-    t, n, ws, labels = case(B=48, seed=4)
+    variants (work-queue forward, other gradient groups) too, on a batch wider than two CTAs per SM (the hidden
+    layer's sort with the samples longest first), and the call can be captured in a CUDA graph."""
+    B = 2 * torch.cuda.get_device_properties(0).multi_processor_count + 16 if wide else 48
+    t, n, ws, labels = case(B=B, seed=4)
     a, b = make_step(t, ws, labels), make_step(t, ws, labels)
+    assert ("L2.order" in [name for name, _ in a.launches]) == wide
     if tuned:
         choice = a.autotune(Autotuner(path=None), force=True)
         b.fwd_algo, b.groups = list(a.fwd_algo), list(a.groups)
