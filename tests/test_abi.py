@@ -143,6 +143,16 @@ def test_shape_validation_without_a_gpu(lib):
     # batch 0 is a no-op
     assert L.bats_adam_step(None, None, None, 0, 0.9, 0.999, 1e-8, 1e-3, 0.1, 0.001, None, None, None, 0, 0, 0,
                             None) == 0
+    # the ordered sort needs its order and the counts; the order entry point its buffers (BATS_ERR_NULL)
+    st = L.bats_sort_events_counted_ordered(None, None, 4, 3, 2, 1.0, 1.0, None, None, None, None, None, None,
+                                            None, 32, None, None, 0, None)
+    assert st == 2 and b"pre_counts" in L.bats_last_error()
+    st = L.bats_sort_events_counted_ordered(None, ctypes.c_void_p(16), 4, 3, 2, 1.0, 1.0, None, None, None, None,
+                                            None, None, None, 32, None, None, 0, None)
+    assert st == 2 and b"sample_order" in L.bats_last_error()
+    assert L.bats_sample_order(None, 4, None, None) == 2
+    assert L.bats_sample_order(None, 0, None, None) == 0  # empty batch: nothing to order
+    assert L.bats_sample_order(None, -1, None, None) == 1
 
 
 def test_workspace_queries(lib):

@@ -280,6 +280,12 @@ def test_sort_events_counted_ordered_matches_unordered(cuda):
     cls = _count_class(plain.counts.cpu().numpy()[o])
     assert (np.diff(cls) >= 0).all()
     assert set(o[:5].tolist()) == set(range(5))
+    # More samples than the order kernel's 1024 threads, lognormal counts with zeros.
+    c3 = np.minimum(rng.lognormal(5, 1.5, 3000), 1e6).astype(np.int32)
+    c3[::97] = 0
+    o3 = K.sample_order(torch.tensor(c3, device="cuda")).cpu().numpy()
+    assert np.array_equal(np.sort(o3), np.arange(3000))
+    assert (np.diff(_count_class(c3[o3])) >= 0).all()
 
 
 def test_edge_cases(cuda):
